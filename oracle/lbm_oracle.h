@@ -1,0 +1,94 @@
+/*
+ * lbm_oracle.h -- CPU restatement of the MGLC reference lattice-Boltzmann step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA path:
+ * only the test suite, the smoke check and the CPU-baseline leg of bench.py
+ * may load it.  The product (libmglc_gb300.so) never links or calls it.
+ *
+ * Layout follows the reference exactly: Fortran column-major arrays with the
+ * population index fastest,
+ *   f(0:Q-1, 1:nx, 1:ny, 1:nz)                   -> f[a + Q*((i-1) + nx*((j-1) + ny*(k-1)))]
+ *   f_post(0:Q-1, 0:nx+1, 0:ny+1, 0:nz+1)        -> halo array, (nx+2)(ny+2)(nz+2)*Q doubles
+ *   rho/u/v/w/T(1:nx, 1:ny, 1:nz)                -> [ (i-1) + nx*((j-1) + ny*(k-1)) ]
+ * Arithmetic follows the reference's expression order; build with
+ * -O2 -ffp-contract=off (no FMA contraction, no reassociation).
+ *
+ * Parity pin: tests/golden/gen_golden.py executes the reference's own Fortran
+ * statements through a mechanical Fortran-subset interpreter and stores the
+ * results; the oracle reproduces those fixtures bit for bit.
+ */
+#ifndef MGLC_LBM_ORACLE_H
+#define MGLC_LBM_ORACLE_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- lid-driven cavity (MPI/Lid_driven_cavity/fortran/3d/mpi_3d_blocked) ---- */
+void orc_lid_params(int total_nx, double reynolds, double u0,
+                    double* tauf, double* snu, double* sq);
+void orc_lid_initial(int nx, int ny, int nz, double u0, double rho0, int top_layer_u0,
+                     double* f, double* rho, double* u, double* v, double* w);
+void orc_lid_collision(int nx, int ny, int nz, double snu, double sq,
+                       const double* f, const double* rho, const double* u,
+                       const double* v, const double* w, double* f_post);
+void orc_lid_streaming(int nx, int ny, int nz, double* f, const double* f_post);
+void orc_lid_bounceback(int nx, int ny, int nz, double u0, double* f,
+                        const double* f_post, const double* rho);
+void orc_lid_macro(int nx, int ny, int nz, const double* f,
+                   double* rho, double* u, double* v, double* w);
+double orc_lid_check(int nx, int ny, int nz, const double* u, const double* v,
+                     const double* w, double* up, double* vp, double* wp);
+/* nsteps of: collision, streaming, bounceback, macro (main.f90:85-102).  A
+ * residual check every check_every steps (0 = never) writes into up/vp/wp and
+ * returns the last errorU (or -1 when no check ran).  nthreads > 1 uses
+ * OpenMP over k for the cell-local sweeps (results are identical). */
+double orc_lid_run(int nx, int ny, int nz, double snu, double sq, double u0,
+                   int nsteps, int check_every, int nthreads,
+                   double* f, double* f_post, double* rho, double* u, double* v, double* w,
+                   double* up, double* vp, double* wp);
+
+/* ---- buoyancy-driven cavity (MPI/Buoyancy_driven_cavity/fortran/3d/bouyancy3d_mpi.F90) ---- */
+typedef struct {
+    double tauf, viscosity, diffusivity, omega_rot, para_a, gbeta, snu, sq, qd, qnu;
+} orc_th_consts;
+/* ekman <= 0 turns the Coriolis force off (omega_rot = 0). */
+void orc_th_params(int total_nz, double rayleigh, double prandtl, double mach,
+                   double ekman, orc_th_consts* out);
+/* bc_y / bc_z: 0 = adiabatic walls, 1 = constant-temperature walls (hot at the
+ * low face, cold at the high face).  x faces are always adiabatic. */
+void orc_th_initial(int nx, int ny, int nz, const orc_th_consts* c,
+                    double t_hot, double t_cold, int bc_y, int bc_z,
+                    double* f, double* g, double* rho, double* u, double* v, double* w,
+                    double* T);
+void orc_th_collision(int nx, int ny, int nz, const orc_th_consts* c, double t_ref,
+                      const double* f, const double* rho, const double* u,
+                      const double* v, const double* w, const double* T,
+                      double* f_post, double* Fx, double* Fy, double* Fz);
+void orc_th_streaming(int nx, int ny, int nz, double* f, const double* f_post);
+void orc_th_bounceback(int nx, int ny, int nz, double* f, const double* f_post);
+void orc_th_collisionT(int nx, int ny, int nz, const orc_th_consts* c,
+                       const double* g, const double* u, const double* v,
+                       const double* w, const double* T, double* g_post);
+void orc_th_streamingT(int nx, int ny, int nz, double* g, const double* g_post);
+void orc_th_bouncebackT(int nx, int ny, int nz, const orc_th_consts* c,
+                        double t_hot, double t_cold, int bc_y, int bc_z,
+                        double* g, const double* g_post);
+void orc_th_macro(int nx, int ny, int nz, const double* f, const double* Fx,
+                  const double* Fy, const double* Fz,
+                  double* rho, double* u, double* v, double* w);
+void orc_th_macroT(int nx, int ny, int nz, const double* g, double* T);
+void orc_th_check(int nx, int ny, int nz, const double* u, const double* v,
+                  const double* w, const double* T, double* up, double* vp,
+                  double* wp, double* Tp, double* error_u, double* error_t);
+/* nsteps in the order of bouyancy3d_mpi.F90:222-249. */
+void orc_th_run(int nx, int ny, int nz, const orc_th_consts* c, double t_ref,
+                double t_hot, double t_cold, int bc_y, int bc_z,
+                int nsteps, int nthreads,
+                double* f, double* f_post, double* g, double* g_post,
+                double* rho, double* u, double* v, double* w, double* T,
+                double* Fx, double* Fy, double* Fz);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,177 @@
+"""ctypes front end of the CPU oracle (``oracle/lbm_oracle.c``).
+
+TEST INFRASTRUCTURE ONLY: the test suite, the smoke check and bench.py's
+CPU-baseline leg use this module as the checker.  The product library never
+imports it.
+
+Arrays use the reference's Fortran layout (population index fastest,
+column-major), held in numpy as C-contiguous arrays of shape
+``(nz, ny, nx, Q)`` for ``f(0:Q-1,1:nx,1:ny,1:nz)`` and ``(nz, ny, nx)`` for the
+macroscopic fields.  The haloed post-collision arrays have shape
+``(nz+2, ny+2, nx+2, Q)``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liboracle.so")
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with gcc (-O2 -ffp-contract=off, OpenMP for the timed baseline)."""
+    src = os.path.join(HERE, "lbm_oracle.c")
+    os.makedirs(BUILD, exist_ok=True)
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
+        cmd = ["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC",
+               "-shared", "-o", LIB, src, "-lm"]
+        subprocess.check_call(cmd)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = ctypes.CDLL(LIB)
+        _declare(_lib)
+    return _lib
+
+
+_D = ctypes.c_double
+_I = ctypes.c_int
+_P = ctypes.POINTER(ctypes.c_double)
+
+
+class ThConsts(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in
+                ("tauf", "viscosity", "diffusivity", "omega_rot", "para_a", "gbeta",
+                 "snu", "sq", "qd", "qnu")]
+
+
+def _declare(L):
+    L.orc_lid_params.argtypes = [_I, _D, _D, _P, _P, _P]
+    L.orc_lid_initial.argtypes = [_I, _I, _I, _D, _D, _I, _P, _P, _P, _P, _P]
+    L.orc_lid_collision.argtypes = [_I, _I, _I, _D, _D, _P, _P, _P, _P, _P, _P]
+    L.orc_lid_streaming.argtypes = [_I, _I, _I, _P, _P]
+    L.orc_lid_bounceback.argtypes = [_I, _I, _I, _D, _P, _P, _P]
+    L.orc_lid_macro.argtypes = [_I, _I, _I, _P, _P, _P, _P, _P]
+    L.orc_lid_check.argtypes = [_I, _I, _I, _P, _P, _P, _P, _P, _P]
+    L.orc_lid_check.restype = _D
+    L.orc_lid_run.argtypes = [_I, _I, _I, _D, _D, _D, _I, _I, _I] + [_P] * 9
+    L.orc_lid_run.restype = _D
+    TP = ctypes.POINTER(ThConsts)
+    L.orc_th_params.argtypes = [_I, _D, _D, _D, _D, TP]
+    L.orc_th_initial.argtypes = [_I, _I, _I, TP, _D, _D, _I, _I] + [_P] * 7
+    L.orc_th_check.argtypes = [_I, _I, _I] + [_P] * 8 + [_P, _P]
+    L.orc_th_run.argtypes = [_I, _I, _I, TP, _D, _D, _D, _I, _I, _I, _I] + [_P] * 12
+
+
+def _p(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_P)
+
+
+def lid_params(total_nx: int, reynolds: float, u0: float):
+    t, s1, s2 = _D(), _D(), _D()
+    lib().orc_lid_params(total_nx, reynolds, u0, ctypes.byref(t), ctypes.byref(s1), ctypes.byref(s2))
+    return t.value, s1.value, s2.value
+
+
+@dataclass
+class LidState:
+    nx: int
+    ny: int
+    nz: int
+    f: np.ndarray
+    f_post: np.ndarray
+    rho: np.ndarray
+    u: np.ndarray
+    v: np.ndarray
+    w: np.ndarray
+    up: np.ndarray
+    vp: np.ndarray
+    wp: np.ndarray
+
+
+class LidOracle:
+    """Reference lid-driven cavity (mpi_3d_blocked on one rank)."""
+
+    def __init__(self, nx, ny, nz, reynolds, u0, rho0=1.0, top_layer_u0=True, total_nx=None):
+        self.nx, self.ny, self.nz = nx, ny, nz
+        self.u0 = u0
+        self.tauf, self.snu, self.sq = lid_params(total_nx or nx, reynolds, u0)
+        z = lambda *s: np.zeros(s, dtype=np.float64)
+        self.s = LidState(nx, ny, nz, z(nz, ny, nx, 19), z(nz + 2, ny + 2, nx + 2, 19),
+                          z(nz, ny, nx), z(nz, ny, nx), z(nz, ny, nx), z(nz, ny, nx),
+                          z(nz, ny, nx), z(nz, ny, nx), z(nz, ny, nx))
+        s = self.s
+        lib().orc_lid_initial(nx, ny, nz, u0, rho0, int(bool(top_layer_u0)), _p(s.f), _p(s.rho),
+                              _p(s.u), _p(s.v), _p(s.w))
+        self.itc = 0
+
+    def run(self, nsteps: int, check_every: int = 0, nthreads: int = 1) -> float:
+        s = self.s
+        err = lib().orc_lid_run(self.nx, self.ny, self.nz, self.snu, self.sq, self.u0, nsteps,
+                                check_every, nthreads, _p(s.f), _p(s.f_post), _p(s.rho),
+                                _p(s.u), _p(s.v), _p(s.w), _p(s.up), _p(s.vp), _p(s.wp))
+        self.itc += nsteps
+        return err
+
+    def check(self) -> float:
+        s = self.s
+        return lib().orc_lid_check(self.nx, self.ny, self.nz, _p(s.u), _p(s.v), _p(s.w),
+                                   _p(s.up), _p(s.vp), _p(s.wp))
+
+
+def th_params(total_nz, rayleigh, prandtl, mach, ekman) -> ThConsts:
+    c = ThConsts()
+    lib().orc_th_params(total_nz, rayleigh, prandtl, mach, ekman, ctypes.byref(c))
+    return c
+
+
+class ThermalOracle:
+    """Reference buoyancy-driven cavity (bouyancy3d_mpi.F90 on one rank)."""
+
+    def __init__(self, nx, ny, nz, rayleigh, prandtl, mach, ekman, t_hot, t_cold, t_ref,
+                 bc_y=1, bc_z=0, total_nz=None):
+        self.nx, self.ny, self.nz = nx, ny, nz
+        self.c = th_params(total_nz or nz, rayleigh, prandtl, mach, ekman)
+        self.t_hot, self.t_cold, self.t_ref = t_hot, t_cold, t_ref
+        self.bc_y, self.bc_z = bc_y, bc_z
+        z = lambda *s: np.zeros(s, dtype=np.float64)
+        self.f = z(nz, ny, nx, 19)
+        self.f_post = z(nz + 2, ny + 2, nx + 2, 19)
+        self.g = z(nz, ny, nx, 7)
+        self.g_post = z(nz + 2, ny + 2, nx + 2, 7)
+        self.rho, self.u, self.v, self.w, self.T = (z(nz, ny, nx) for _ in range(5))
+        self.Fx, self.Fy, self.Fz = (z(nz, ny, nx) for _ in range(3))
+        self.up, self.vp, self.wp, self.Tp = (z(nz, ny, nx) for _ in range(4))
+        lib().orc_th_initial(nx, ny, nz, ctypes.byref(self.c), t_hot, t_cold, bc_y, bc_z,
+                             _p(self.f), _p(self.g), _p(self.rho), _p(self.u), _p(self.v),
+                             _p(self.w), _p(self.T))
+        self.itc = 0
+
+    def run(self, nsteps: int, nthreads: int = 1):
+        lib().orc_th_run(self.nx, self.ny, self.nz, ctypes.byref(self.c), self.t_ref, self.t_hot,
+                         self.t_cold, self.bc_y, self.bc_z, nsteps, nthreads, _p(self.f),
+                         _p(self.f_post), _p(self.g), _p(self.g_post), _p(self.rho), _p(self.u),
+                         _p(self.v), _p(self.w), _p(self.T), _p(self.Fx), _p(self.Fy),
+                         _p(self.Fz))
+        self.itc += nsteps
+
+    def check(self):
+        eu, et = _D(), _D()
+        lib().orc_th_check(self.nx, self.ny, self.nz, _p(self.u), _p(self.v), _p(self.w),
+                           _p(self.T), _p(self.up), _p(self.vp), _p(self.wp), _p(self.Tp),
+                           ctypes.byref(eu), ctypes.byref(et))
+        return eu.value, et.value

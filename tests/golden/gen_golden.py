@@ -1,0 +1,172 @@
+"""Generate golden fixtures by executing the MGLC reference's own Fortran source.
+
+Run in a checkout that has the reference tree (default ``/root/reference``):
+
+    python tests/golden/gen_golden.py [--ref PATH]
+
+For each case the reference's module and hot-path subroutines are translated
+statement by statement by ``fortran_exec`` and called in the order of the
+reference's main loop, on one rank (every MPI exchange is a no-op, every
+``MPI_Allreduce`` a copy).  The outputs are written as ``*.npz`` next to this
+script.  The test suite checks the C oracle against these files bit for bit,
+which pins the oracle to the reference's own statements.
+
+Arrays are stored in numpy with the Fortran index order reversed:
+``f(0:18,1:nx,1:ny,1:nz)`` becomes shape ``(nz, ny, nx, 19)``.
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+from fortran_exec import FArr, Program, preprocess  # noqa: E402
+
+LID_DIR = "MPI/Lid_driven_cavity/fortran/3d/mpi_3d_blocked"
+THERMAL_FILE = "MPI/Buoyancy_driven_cavity/fortran/3d/bouyancy3d_mpi.F90"
+
+
+def _mpi_single_rank(ndim=3):
+    dims = FArr([(0, ndim - 1)], np.int64, 1)
+    coords = FArr([(0, ndim - 1)], np.int64, 0)
+    return {"rank": 0, "rank3d": 0, "num_process": 1, "dims": dims, "coords": coords,
+            "periods": FArr([(0, ndim - 1)], np.int64, 0)}
+
+
+def _interior(arr: FArr):
+    """Drop a one-cell halo on the three spatial axes (first numpy axes)."""
+    a = arr.numpy()
+    return a
+
+
+def lid_case(ref, nx, ny, nz, reynolds, nsteps, check_every, u0=0.1):
+    p = Program()
+    p.overrides = {"total_nx": nx, "total_ny": ny, "total_nz": nz, "reynolds": float(reynolds),
+                   "u0": float(u0), **_mpi_single_rank()}
+    mod = preprocess(open(os.path.join(ref, LID_DIR, "commondata.f90")).read(), p.defines)
+    p.load_module(mod)
+    p.ns.update({"nx": nx, "ny": ny, "nz": nz})
+    for fn in ("initial.f90", "collision.f90", "streaming.f90", "bounce_back.f90", "macro.f90",
+               "check.f90"):
+        p.load_subroutines(preprocess(open(os.path.join(ref, LID_DIR, fn)).read(), p.defines))
+    names = ["initial", "collision", "streaming", "bounceback", "macro", "check"]
+    p.build(names)
+    p.call("initial")
+    ns = p.ns
+    out = {"nx": nx, "ny": ny, "nz": nz, "reynolds": float(reynolds), "u0": float(u0),
+           "tauf": ns["tauf"], "snu": ns["snu"], "sq": ns["sq"], "nsteps": nsteps,
+           "check_every": check_every,
+           "f0": ns["f"].numpy(), "rho0": ns["rho"].numpy(), "u_init": ns["u"].numpy()}
+    errs = []
+    # main.f90:85-102 (message_passing_sendrecv is a no-op on one rank)
+    for itc in range(1, nsteps + 1):
+        ns["itc"] = itc
+        p.call("collision")
+        p.call("streaming")
+        p.call("bounceback")
+        p.call("macro")
+        if itc == 1:
+            out["f_step1"] = ns["f"].numpy()
+        if check_every and itc % check_every == 0:
+            p.call("check")
+            errs.append(ns["erroru"])
+    out.update(f=ns["f"].numpy(), rho=ns["rho"].numpy(), u=ns["u"].numpy(), v=ns["v"].numpy(),
+               w=ns["w"].numpy(), erroru=np.array(errs))
+    assert not np.isnan(out["f"]).any(), "NaN in f: a halo value was read"
+    return out
+
+
+def thermal_case(ref, nx, ny, nz, rayleigh, prandtl, mach, ekman, thot, tcold, tref, nsteps,
+                 check_every, variant="cavity"):
+    p = Program()
+    p.overrides = {"total_nx": nx, "total_ny": ny, "total_nz": nz, "rayleigh": float(rayleigh),
+                   "prandtl": float(prandtl), "mach": float(mach), "ekman": float(ekman),
+                   "thot": float(thot), "tcold": float(tcold), "tref": float(tref),
+                   **_mpi_single_rank()}
+    undef = set()
+    if variant == "rb":  # Rayleigh-Benard walls: const-T plates, adiabatic side walls
+        undef = {"benchmarkCavity", "LeftRightWallsConstT", "TopBottomPlatesAdiabatic"}
+        p.defines |= {"RBconvection", "LeftRightWallsAdiabatic", "TopBottomPlatesConstT"}
+    src = preprocess(open(os.path.join(ref, THERMAL_FILE)).read(), p.defines, undef)
+    p.load_module(src)
+    p.ns.update({"nx": nx, "ny": ny, "nz": nz})
+    p.load_subroutines(src)
+    names = ["initial", "collision", "streaming", "bounceback", "macro", "collisionT",
+             "streamingT", "bouncebackT", "macroT", "check"]
+    names = [n.lower() for n in names]
+    p.build(names)
+    p.call("initial")
+    ns = p.ns
+    out = {"nx": nx, "ny": ny, "nz": nz, "rayleigh": float(rayleigh), "prandtl": float(prandtl),
+           "mach": float(mach), "ekman": float(ekman), "thot": float(thot),
+           "tcold": float(tcold), "tref": float(tref), "nsteps": nsteps,
+           "check_every": check_every, "variant": variant,
+           "tauf": ns["tauf"], "paraa": ns["paraa"], "gbeta": ns["gbeta"],
+           "omegaratating": ns["omegaratating"],
+           "f0": ns["f"].numpy(), "g0": ns["g"].numpy(), "t_init": ns["t"].numpy()}
+    eu, et = [], []
+    # bouyancy3d_mpi.F90:222-249
+    for itc in range(1, nsteps + 1):
+        ns["itc"] = itc
+        p.call("collision")
+        p.call("streaming")
+        p.call("bounceback")
+        p.call("collisiont")
+        p.call("streamingt")
+        p.call("bouncebackt")
+        p.call("macro")
+        p.call("macrot")
+        if itc == 1:
+            out["f_step1"] = ns["f"].numpy()
+            out["g_step1"] = ns["g"].numpy()
+        if check_every and itc % check_every == 0:
+            p.call("check")
+            eu.append(ns["erroru"])
+            et.append(ns["errort"])
+    out.update(f=ns["f"].numpy(), g=ns["g"].numpy(), rho=ns["rho"].numpy(), u=ns["u"].numpy(),
+               v=ns["v"].numpy(), w=ns["w"].numpy(), T=ns["t"].numpy(), Fx=ns["fx"].numpy(),
+               Fy=ns["fy"].numpy(), Fz=ns["fz"].numpy(), erroru=np.array(eu),
+               errort=np.array(et))
+    assert not np.isnan(out["f"]).any() and not np.isnan(out["g"]).any()
+    return out
+
+
+CASES = {
+    # lid: non-cubic grid to catch axis mix-ups; Re chosen for tau ~ 0.6
+    "lid_7x6x5": lambda ref: lid_case(ref, 7, 6, 5, reynolds=21.0, nsteps=12, check_every=4),
+    "lid_6x6x6_re400": lambda ref: lid_case(ref, 6, 6, 6, reynolds=400.0, nsteps=6,
+                                            check_every=3),
+    # thermal as shipped (Thot=1, Tcold=0, Coriolis on via Ekman=1e-3)
+    "thermal_6x7x5_ref": lambda ref: thermal_case(ref, 6, 7, 5, 1e4, 0.71, 0.1, 1e-3, 1.0, 0.0,
+                                                  0.0, nsteps=8, check_every=4),
+    # benchmark-style walls T=+-0.5 and no rotation
+    "thermal_5x6x7_pm": lambda ref: thermal_case(ref, 5, 6, 7, 1e5, 0.71, 0.1, float("inf"), 0.5,
+                                                 -0.5, 0.0, nsteps=8, check_every=4),
+    # Rayleigh-Benard wall variant (const-T plates in z)
+    "thermal_6x5x6_rb": lambda ref: thermal_case(ref, 6, 5, 6, 1e4, 0.71, 0.1, 1e-3, 1.0, 0.0,
+                                                 0.0, nsteps=6, check_every=3, variant="rb"),
+}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", default=None)
+    a = ap.parse_args()
+    for name, fn in CASES.items():
+        if a.only and a.only != name:
+            continue
+        t0 = time.time()
+        out = fn(a.ref)
+        path = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(path, **{k: np.asarray(v) for k, v in out.items()})
+        print(f"{name}: {time.time() - t0:.1f}s -> {os.path.basename(path)}")
+
+
+if __name__ == "__main__":
+    main()
