@@ -1,0 +1,373 @@
+"""Benchmark of the MGLC lattice-Boltzmann step on GB300 (one JSON line).
+
+Default workload: the large lid-driven cavity, D3Q19 MRT, 384^3 cells,
+Re=1000, U=0.1, FP64 plain method (the drop-in).  A "step" is one fused time
+step over the whole lattice.  ``value`` is MLUPS with the state resident in
+HBM; ``e2e`` is the same metric through the C-ABI with host buffers (initial
+state uploaded from pinned host memory, K steps, macroscopic fields read back)
+inside the timed region.  The other storage forms (FP32 / FP16 / BF16
+deviations, FP32 arithmetic) are timed on the same workload and reported under
+``forms``.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mglc|reference]
+                    [--workload lid384|lid64|thermal128] [--form fp64|fp32|fp16|bf16]
+
+Multi-GPU: replicas only (one independent cavity per GPU, no inter-GPU
+traffic); launched by torchrun, rank 0 prints max-over-ranks timing.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MLUPS, %HBM roofline: mixed vs FP64 plain at ≤1e-3 err; serve p50/p99 ms"
+
+WORKLOADS = {
+    "lid384": dict(kind="lid", n=384, reynolds=1000.0, u0=0.1,
+                   desc="lid-driven cavity D3Q19 MRT 384^3 Re=1000 U=0.1"),
+    "lid64": dict(kind="lid", n=64, reynolds=400.0, u0=0.1,
+                  desc="lid-driven cavity D3Q19 MRT 64^3 Re=400 U=0.1"),
+    "thermal128": dict(kind="thermal", n=128, rayleigh=1e5, prandtl=0.71, mach=0.1,
+                       desc="differentially heated cavity D3Q19+D3Q7 128^3 Ra=1e5 Pr=0.71"),
+}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic():
+    """Per-cell DRAM bytes of the step kernels from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(p):
+        try:
+            return json.load(open(p))
+        except Exception:
+            return {}
+    return {}
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        for l in self.lines:
+            p = [x.strip() for x in l.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_solve(mg, wl, form):
+    n = wl["n"]
+    if wl["kind"] == "lid":
+        return mg.LidDrivenCavity(n, reynolds=wl["reynolds"], u0=wl["u0"], top_layer_u0=False,
+                                  precision=form)
+    return mg.BuoyancyCavity(n, rayleigh=wl["rayleigh"], prandtl=wl["prandtl"], mach=wl["mach"],
+                             t_hot=0.5, t_cold=-0.5, ekman=0.0, precision=form)
+
+
+def time_device(torch, mg, wl, form, steps, warmup, dist=None):
+    """Device-resident MLUPS: state in HBM, K fused steps between CUDA events."""
+    s = make_solve(mg, wl, form)
+    # the context runs on a dedicated (non-default) stream; the CUDA events
+    # are recorded on that same stream
+    stream = torch.cuda.Stream()
+    s.set_stream(stream.cuda_stream)
+    s.initial()
+    s.step(warmup)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    s.step(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    s.set_stream(None)
+    if dist:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    info = s.info()
+    s.close()
+    return ms, info
+
+
+def time_e2e(torch, mg, wl, form, steps, dist=None):
+    """End to end through the C-ABI: pinned host state -> device, K steps,
+    macroscopic fields -> pinned host, residual check."""
+    s = make_solve(mg, wl, form)
+    n = wl["n"]
+    cells = n ** 3
+    q_g = 7 if wl["kind"] == "thermal" else 0
+    f_h = torch.empty((n, n, n, 19), dtype=torch.float64, pin_memory=True).numpy()
+    g_h = torch.empty((n, n, n, 7), dtype=torch.float64, pin_memory=True).numpy() if q_g else None
+    fields = [torch.empty((n, n, n), dtype=torch.float64, pin_memory=True).numpy()
+              for _ in range(5 if q_g else 4)]
+    s.initial()
+    got = s.get_f()
+    if q_g:
+        f_h[...] = got[0]
+        g_h[...] = got[1]
+    else:
+        f_h[...] = got
+    del got
+    import ctypes
+    from mglc_gb300 import capi
+    L = capi.lib()
+    ptr = lambda a: None if a is None else a.ctypes.data
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    capi.check(s.handle, L.mglc_load_state(s.handle, ptr(f_h), ptr(g_h), None, None, None, None, None))
+    capi.check(s.handle, L.mglc_step(s.handle, steps))
+    capi.check(s.handle, L.mglc_get_macros(s.handle, *[ptr(a) for a in fields[:4]],
+                                           ptr(fields[4]) if q_g else None))
+    eu = ctypes.c_double()
+    capi.check(s.handle, L.mglc_check(s.handle, ctypes.byref(eu), None))
+    t1 = time.perf_counter()
+    dt = t1 - t0
+    if dist:
+        t = torch.tensor([dt], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dt = float(t.item())
+    s.close()
+    h2d = 8 * (19 + q_g) * cells
+    d2h = 8 * len(fields) * cells + 8
+    return dt, h2d / steps, d2h / steps, float(eu.value)
+
+
+def cpu_sample(wl, target_s=10.0):
+    """The oracle (restatement of the reference's CPU code) with OpenMP on all
+    host cores, on a bounded sample of the workload."""
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    n = wl["n"]
+    if wl["kind"] == "lid":
+        o = O.LidOracle(n, n, n, wl["reynolds"], wl["u0"], top_layer_u0=False)
+        run = lambda k: o.run(k, nthreads=threads)
+    else:
+        o = O.ThermalOracle(n, n, n, wl["rayleigh"], wl["prandtl"], wl["mach"], 0.0, 0.5, -0.5, 0.0)
+        run = lambda k: o.run(k, nthreads=threads)
+    t0 = time.perf_counter()
+    run(1)  # first touch + warm-up
+    t1 = time.perf_counter()
+    per = max(t1 - t0, 1e-3)
+    k = int(max(1, min(20, target_s / per)))
+    t0 = time.perf_counter()
+    run(k)
+    dt = time.perf_counter() - t0
+    return {"value": n ** 3 * k / dt / 1e6, "unit": "MLUPS", "cores": threads, "kind": "port",
+            "sample": f"{wl['desc']}: {k} steps after 1 warm-up step, oracle (C restatement of "
+                      f"the reference's Fortran loops) with {threads} OpenMP threads"}
+
+
+def reference_arm(args, wl):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    n = wl["n"]
+    # size the per-step sample so that warmup+steps finish within ~150 s
+    probe_n = min(n, 128)
+    if wl["kind"] == "lid":
+        mk = lambda m: O.LidOracle(m, m, m, wl["reynolds"], wl["u0"], top_layer_u0=False)
+    else:
+        mk = lambda m: O.ThermalOracle(m, m, m, wl["rayleigh"], wl["prandtl"], wl["mach"], 0.0,
+                                       0.5, -0.5, 0.0)
+    p = mk(probe_n)
+    t0 = time.perf_counter()
+    p.run(2, nthreads=threads)
+    rate = probe_n ** 3 * 2 / (time.perf_counter() - t0)
+    del p
+    total = args.steps + args.warmup
+    m = n
+    while m > 32 and total * m ** 3 / rate > 150.0:
+        m = int(m * 0.8) // 8 * 8
+    o = mk(m)
+    o.run(args.warmup, nthreads=threads)
+    t0 = time.perf_counter()
+    o.run(args.steps, nthreads=threads)
+    dt = time.perf_counter() - t0
+    val = m ** 3 * args.steps / dt / 1e6
+    sample = (f"{wl['desc'].replace(str(n) + '^3', str(m) + '^3')}: {args.steps} timed steps after "
+              f"{args.warmup} warm-up, C restatement of the reference's Fortran loops "
+              f"(no Fortran compiler here), {threads} OpenMP threads")
+    line = {"impl": "reference", "metric": METRIC, "value": round(val, 3), "unit": "MLUPS",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": wl["desc"], "form": "fp64", "sample_cells": m ** 3},
+            "cpu_baseline": {"value": round(val, 3), "unit": "MLUPS", "cores": threads,
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": round(val, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="mglc", choices=["mglc", "reference"])
+    ap.add_argument("--workload", default="lid384", choices=sorted(WORKLOADS))
+    ap.add_argument("--form", default="fp64", choices=["fp64", "fp32", "fp16", "bf16"])
+    ap.add_argument("--no-forms", action="store_true", help="skip timing the other storage forms")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--n", type=int, default=0, help="override the cube size (profiling runs)")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    wl = dict(WORKLOADS[args.workload])
+    if args.n:
+        wl["desc"] = wl["desc"].replace(f"{wl['n']}^3", f"{args.n}^3")
+        wl["n"] = args.n
+
+    if args.impl == "reference":
+        return reference_arm(args, wl)
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    import mglc_gb300
+    from mglc_gb300 import build as B
+    B.build()
+    mglc_gb300.lib()
+
+    cells = wl["n"] ** 3
+    peak, peak_kind = load_peaks()
+    with ClockSampler(local) as clk:
+        ms, info = time_device(torch, mglc_gb300, wl, args.form, args.steps, args.warmup, dist)
+    clocks = clk.summary()
+    value = world * cells * args.steps / (ms * 1e-3) / 1e6
+    ms_step = ms / args.steps
+    bpc = info.bytes_per_cell_step
+    achieved = bpc * cells / (ms_step * 1e-3) / 1e9
+    traffic_tab = load_traffic()
+    tkey = f"{wl['kind']}_{args.form}"
+    traffic = None
+    if tkey in traffic_tab:
+        traffic = traffic_tab[tkey]["dram_bytes_per_cell"] * cells
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "MLUPS", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.form == "fp64" else "f32",
+        "data": "synthetic (analytic cavity initial state, no dataset)",
+        "config": {"workload": wl["desc"], "form": args.form, "cells": cells,
+                   "parallelism": f"replicas{world}" if world > 1 else "single",
+                   "l2": "inputs larger than L2 (state >> 129 MB), no flush"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "peak_kind": f"hbm_gbs of {peak_kind}",
+                     "bytes_per_cell": bpc, "kernel": f"k_{wl['kind']}_step<{args.form}>"},
+        "clocks": clocks,
+        "gpu_launches": args.steps,
+    }
+    if rank == 0 and not args.no_e2e:
+        dt, h2d, d2h, eu = time_e2e(torch, mglc_gb300, wl, args.form, args.steps, dist)
+        line["e2e"] = {"value": round(world * cells * args.steps / dt / 1e6, 3), "unit": "MLUPS",
+                       "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                       "what": "mglc_load_state(host f) + mglc_step(K) + mglc_get_macros(host) "
+                               "+ mglc_check, wall clock"}
+    if rank == 0 and not args.no_forms:
+        forms = {}
+        for fm in ("fp64", "fp32", "fp16", "bf16"):
+            if fm == args.form:
+                continue
+            try:
+                m2, inf2 = time_device(torch, mglc_gb300, wl, fm, args.steps, args.warmup)
+                v2 = cells * args.steps / (m2 * 1e-3) / 1e6
+                a2 = inf2.bytes_per_cell_step * cells / (m2 / args.steps * 1e-3) / 1e9
+                forms[fm] = {"value": round(v2, 3), "ms_per_step": round(m2 / args.steps, 4),
+                             "bytes_per_cell": inf2.bytes_per_cell_step,
+                             "achieved_gbs": round(a2, 1), "frac": round(a2 / peak, 4)}
+            except Exception as e:  # report, never hide
+                forms[fm] = {"error": str(e)}
+        line["forms"] = forms
+    if rank == 0 and world == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_sample(wl)
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

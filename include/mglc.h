@@ -1,0 +1,136 @@
+/*
+ * mglc.h -- C-ABI of libmglc_gb300.so: the MGLC lattice-Boltzmann time step on
+ * one GB300 GPU (sm_103a).
+ *
+ * The reference (cheryli/MGLC, Fortran 90 + MPI) has no library interface:
+ * its hot path is a set of argument-less subroutines acting on module arrays,
+ * called from `program main`'s loop.  Each entry point below replaces one of
+ * those calls; the header comment of each names the reference routine (paths
+ * relative to the MGLC repository root).  A Fortran host binds these through
+ * iso_c_binding (fortran/mglc_iface.f90); C, C++ and Python (ctypes) call them
+ * directly.
+ *
+ * Conventions
+ *  - Every function returns an int status (MGLC_OK = 0).  On failure the
+ *    context keeps a message readable with mglc_last_error().  Nothing exits
+ *    or throws across the ABI.
+ *  - Host arrays are caller-owned and use the reference's Fortran layout:
+ *    populations f(0:18,1:nx,1:ny,1:nz) with the population index fastest,
+ *    g(0:6,1:nx,1:ny,1:nz), and scalar fields rho(1:nx,1:ny,1:nz), x fastest.
+ *    Device memory is owned by the context.
+ *  - A context is bound to one CUDA stream; calls on one context are not
+ *    thread-safe, different contexts may be driven from different threads.
+ *    mglc_step() is asynchronous; getters synchronise the context's stream.
+ */
+#ifndef MGLC_GB300_H
+#define MGLC_GB300_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MGLC_OK 0
+#define MGLC_ERR_INVALID 1     /* bad argument or size */
+#define MGLC_ERR_CUDA 2        /* CUDA runtime error */
+#define MGLC_ERR_NOMEM 3       /* device allocation failed */
+#define MGLC_ERR_STATE 4       /* call not valid for this context kind or state */
+#define MGLC_ERR_NUMERIC 5     /* NaN or Inf found in the state */
+#define MGLC_ERR_UNSUPPORTED 6 /* feature not built for this form */
+#define MGLC_ERR_PARTICLE 7    /* particle overlap or wall penetration */
+
+/* Storage / arithmetic form of the populations.
+ *  FP64: FP64 storage and FP64 arithmetic -- the drop-in for the reference.
+ *  FP32/FP16/BF16: populations stored as deviations f_i - w_i*rho0 in that
+ *  type, FP32 arithmetic; FP64 kept for reductions (residual, totals). */
+enum { MGLC_FP64 = 0, MGLC_FP32 = 1, MGLC_FP16 = 2, MGLC_BF16 = 3 };
+
+enum { MGLC_KIND_LID = 1, MGLC_KIND_THERMAL = 2, MGLC_KIND_PARTICLE = 3 };
+
+typedef struct mglc_ctx mglc_ctx;
+
+/* Lid-driven cavity parameters: MPI/Lid_driven_cavity/fortran/3d/mpi_3d_blocked/commondata.f90:4-9
+ * tauf = u0*total_nx/reynolds*3 + 0.5; lid moves along +x on the top z plane. */
+typedef struct mglc_lid_params {
+    int total_nx, total_ny, total_nz; /* lattice nodes per axis */
+    double reynolds;                  /* Re, based on total_nx */
+    double rho0;                      /* initial density (1.0) */
+    double u0;                        /* lid velocity (lattice units) */
+    int top_layer_u0; /* 1: initial u = u0 on the top layer (initial.f90:55-61); 0: u = 0 */
+    int precision;    /* MGLC_FP64 ... MGLC_BF16 */
+} mglc_lid_params;
+
+/* Buoyancy-driven cavity parameters:
+ * MPI/Buoyancy_driven_cavity/fortran/3d/bouyancy3d_mpi.F90:28-54.
+ * tauf = 0.5 + mach*total_nz*sqrt(3*prandtl/rayleigh); Boussinesq force
+ * F_z = rho*gbeta*(T - t_ref); Coriolis F_x = -2 rho v Omega, F_y = 2 rho u Omega
+ * with Omega = nu/2/ekman/total_nz^2 (ekman <= 0 turns rotation off). */
+typedef struct mglc_thermal_params {
+    int total_nx, total_ny, total_nz;
+    double rayleigh, prandtl, mach;
+    double t_hot, t_cold, t_ref;
+    double ekman;
+    int bc_y_const_t; /* 1: LeftRightWallsConstT (hot j=1, cold j=ny); 0: adiabatic */
+    int bc_z_const_t; /* 1: TopBottomPlatesConstT (hot k=1, cold k=nz); 0: adiabatic */
+    int precision;
+} mglc_thermal_params;
+
+/* Derived constants of a context (for logging and tests). */
+typedef struct mglc_info {
+    int kind, precision;
+    int nx, ny, nz;
+    long long itc;           /* time steps taken since initial()/load */
+    double tauf, snu, sq;    /* flow relaxation */
+    double viscosity, diffusivity, para_a, gbeta, omega_rot; /* thermal only */
+    double bytes_per_cell_step; /* algorithmic HBM bytes of one fused step per cell */
+    long long device_bytes;  /* device memory held by the context */
+} mglc_info;
+
+/* ---- lifetime ---------------------------------------------------------- */
+/* Replaces the allocation part of initial.f90:35-44 (lid). */
+int mglc_lid_create(const mglc_lid_params* p, mglc_ctx** out);
+/* Replaces the allocation part of bouyancy3d_mpi.F90:476-496 (thermal). */
+int mglc_thermal_create(const mglc_thermal_params* p, mglc_ctx** out);
+void mglc_destroy(mglc_ctx* ctx);
+const char* mglc_last_error(const mglc_ctx* ctx);
+/* Bind the context to a caller-owned cudaStream_t (NULL = the context's own stream). */
+int mglc_set_stream(mglc_ctx* ctx, void* cuda_stream);
+int mglc_get_info(const mglc_ctx* ctx, mglc_info* out);
+
+/* ---- state ------------------------------------------------------------- */
+/* Device-side initial(): lid initial.f90:46-73; thermal bouyancy3d_mpi.F90:497-629. */
+int mglc_initial(mglc_ctx* ctx);
+/* Load a state from host arrays in the reference layout (the reload path
+ * bouyancy3d_mpi.F90:598-611).  g is used by thermal contexts only.  rho,u,v,w
+ * (and T) are the macroscopic fields the next collision uses; pass NULL for
+ * all of them to derive them from f (and g) with the reference macro. */
+int mglc_load_state(mglc_ctx* ctx, const double* f, const double* g, const double* rho,
+                    const double* u, const double* v, const double* w, const double* T);
+/* Copy the post-stream populations f (and g) back in the reference layout. */
+int mglc_get_f(mglc_ctx* ctx, double* f, double* g);
+
+/* ---- the hot path ------------------------------------------------------ */
+/* nsteps fused time steps.  Lid: collision + streaming + bounceback + macro
+ * (main.f90:89-97).  Thermal: collision, streaming, bounceback, collisionT,
+ * streamingT, bouncebackT, macro, macroT (bouyancy3d_mpi.F90:226-244).
+ * Asynchronous on the context's stream. */
+int mglc_step(mglc_ctx* ctx, int nsteps);
+
+/* macro() / macroT() output: rho,u,v,w (and T) of the current state, host
+ * arrays (x fastest).  Any pointer may be NULL.  Synchronises. */
+int mglc_get_macros(mglc_ctx* ctx, double* rho, double* u, double* v, double* w, double* T);
+/* check(): lid check.f90:12-30 (errorU over u,v only in the numerator);
+ * thermal bouyancy3d_mpi.F90:1234-1281 (errorU over u,v,w; errorT).  Updates
+ * the stored previous fields like the reference.  error_t may be NULL. */
+int mglc_check(mglc_ctx* ctx, double* error_u, double* error_t);
+/* Conserved totals in FP64: mass = sum rho, energy = sum rho|u|^2/2,
+ * heat = sum T (thermal, else 0).  Any pointer may be NULL. */
+int mglc_totals(mglc_ctx* ctx, double* mass, double* energy, double* heat);
+
+/* ---- device-resident variants (no host copies) --------------------------- */
+/* Same as mglc_get_macros but into device buffers of nx*ny*nz doubles. */
+int mglc_get_macros_device(mglc_ctx* ctx, double* rho, double* u, double* v, double* w,
+                           double* T);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

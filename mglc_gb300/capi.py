@@ -1,0 +1,91 @@
+"""ctypes binding of ``libmglc_gb300.so`` (the C-ABI in include/mglc.h).
+
+This is the Python side of the same ABI a Fortran host binds through
+iso_c_binding.  Loading fails loudly when the library has not been built:
+there is no CPU fallback anywhere in the product.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libmglc_gb300.so")
+
+MGLC_OK = 0
+ERRORS = {1: "MGLC_ERR_INVALID", 2: "MGLC_ERR_CUDA", 3: "MGLC_ERR_NOMEM", 4: "MGLC_ERR_STATE",
+          5: "MGLC_ERR_NUMERIC", 6: "MGLC_ERR_UNSUPPORTED", 7: "MGLC_ERR_PARTICLE"}
+FORMS = {"fp64": 0, "fp32": 1, "fp16": 2, "bf16": 3}
+KIND_LID, KIND_THERMAL, KIND_PARTICLE = 1, 2, 3
+
+_D, _I, _LL = ctypes.c_double, ctypes.c_int, ctypes.c_longlong
+_DP = ctypes.POINTER(ctypes.c_double)
+_VP = ctypes.c_void_p
+
+
+class LidParams(ctypes.Structure):
+    _fields_ = [("total_nx", _I), ("total_ny", _I), ("total_nz", _I), ("reynolds", _D),
+                ("rho0", _D), ("u0", _D), ("top_layer_u0", _I), ("precision", _I)]
+
+
+class ThermalParams(ctypes.Structure):
+    _fields_ = [("total_nx", _I), ("total_ny", _I), ("total_nz", _I), ("rayleigh", _D),
+                ("prandtl", _D), ("mach", _D), ("t_hot", _D), ("t_cold", _D), ("t_ref", _D),
+                ("ekman", _D), ("bc_y_const_t", _I), ("bc_z_const_t", _I), ("precision", _I)]
+
+
+class Info(ctypes.Structure):
+    _fields_ = [("kind", _I), ("precision", _I), ("nx", _I), ("ny", _I), ("nz", _I),
+                ("itc", _LL), ("tauf", _D), ("snu", _D), ("sq", _D), ("viscosity", _D),
+                ("diffusivity", _D), ("para_a", _D), ("gbeta", _D), ("omega_rot", _D),
+                ("bytes_per_cell_step", _D), ("device_bytes", _LL)]
+
+
+# (name, argtypes, restype) of every exported symbol; tests check that the
+# library exports all of them
+SIGNATURES = {
+    "mglc_lid_create": ([ctypes.POINTER(LidParams), ctypes.POINTER(_VP)], _I),
+    "mglc_thermal_create": ([ctypes.POINTER(ThermalParams), ctypes.POINTER(_VP)], _I),
+    "mglc_destroy": ([_VP], None),
+    "mglc_last_error": ([_VP], ctypes.c_char_p),
+    "mglc_set_stream": ([_VP, _VP], _I),
+    "mglc_get_info": ([_VP, ctypes.POINTER(Info)], _I),
+    "mglc_initial": ([_VP], _I),
+    "mglc_load_state": ([_VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP], _I),
+    "mglc_get_f": ([_VP, _VP, _VP], _I),
+    "mglc_step": ([_VP, _I], _I),
+    "mglc_get_macros": ([_VP, _VP, _VP, _VP, _VP, _VP], _I),
+    "mglc_get_macros_device": ([_VP, _VP, _VP, _VP, _VP, _VP], _I),
+    "mglc_check": ([_VP, _DP, _DP], _I),
+    "mglc_totals": ([_VP, _DP, _DP, _DP], _I),
+}
+
+_lib = None
+
+
+class MglcError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def lib():
+    """Load the built library (raises if it is missing: no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with mglc_gb300.build.build() "
+                               "(or __graft_entry__.build()); there is no CPU fallback")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (argt, rest) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = argt
+            fn.restype = rest
+        _lib = L
+    return _lib
+
+
+def check(ctx, rc):
+    if rc != MGLC_OK:
+        msg = lib().mglc_last_error(ctx).decode() if ctx else ""
+        raise MglcError(rc, msg)

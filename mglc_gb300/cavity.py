@@ -1,0 +1,174 @@
+"""Python host API over the C-ABI, mirroring the reference's routines.
+
+The reference drives each solve from ``program main`` by calling argument-less
+subroutines on module arrays: ``initial()``, then a loop of
+``collision(); streaming(); bounceback(); macro()`` and ``check()`` every 2000
+steps (MPI/Lid_driven_cavity/fortran/3d/mpi_3d_blocked/main.f90:85-102; the
+thermal loop adds ``collisionT/streamingT/bouncebackT/macroT``,
+MPI/Buoyancy_driven_cavity/fortran/3d/bouyancy3d_mpi.F90:222-249).  Here one
+object holds one solve on the GPU and offers the same verbs:
+
+* ``initial()``            -- the reference initial()
+* ``step(n)``              -- n fused time steps (collision .. macro)
+* ``macro()``              -- rho, u, v, w (and T) arrays
+* ``check()``              -- errorU (and errorT), reference semantics
+* ``get_f()`` / ``load_state()`` -- populations in the reference layout
+
+Arrays are numpy, shaped ``(nz, ny, nx)`` for fields and ``(nz, ny, nx, Q)``
+for populations, i.e. the Fortran arrays with the index order reversed.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import capi
+
+_P = ctypes.c_void_p
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous, "need C-contiguous float64"
+    return a.ctypes.data
+
+
+class _Solve:
+    Q_G = 0
+
+    def __init__(self):
+        self._ctx = _P()
+
+    # -- lifetime --
+    def close(self):
+        if self._ctx:
+            capi.lib().mglc_destroy(self._ctx)
+            self._ctx = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _ck(self, rc):
+        capi.check(self._ctx, rc)
+
+    @property
+    def handle(self):
+        return self._ctx
+
+    def info(self) -> capi.Info:
+        i = capi.Info()
+        self._ck(capi.lib().mglc_get_info(self._ctx, ctypes.byref(i)))
+        return i
+
+    @property
+    def shape(self):
+        i = self.info()
+        return (i.nz, i.ny, i.nx)
+
+    # -- reference verbs --
+    def initial(self):
+        self._ck(capi.lib().mglc_initial(self._ctx))
+        return self
+
+    def step(self, nsteps: int = 1):
+        self._ck(capi.lib().mglc_step(self._ctx, int(nsteps)))
+        return self
+
+    def set_stream(self, stream_handle: int | None):
+        self._ck(capi.lib().mglc_set_stream(self._ctx, stream_handle))
+
+    def get_f(self):
+        nz, ny, nx = self.shape
+        f = np.empty((nz, ny, nx, 19))
+        g = np.empty((nz, ny, nx, 7)) if self.Q_G else None
+        self._ck(capi.lib().mglc_get_f(self._ctx, _ptr(f), _ptr(g)))
+        return (f, g) if self.Q_G else f
+
+    def totals(self):
+        m, e, h = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        self._ck(capi.lib().mglc_totals(self._ctx, ctypes.byref(m), ctypes.byref(e), ctypes.byref(h)))
+        return m.value, e.value, h.value
+
+
+class LidDrivenCavity(_Solve):
+    """D3Q19 MRT lid-driven cavity (reference: Lid_driven_cavity/fortran/3d)."""
+
+    def __init__(self, total_nx, total_ny=None, total_nz=None, reynolds=1000.0, u0=0.1,
+                 rho0=1.0, top_layer_u0=True, precision="fp64"):
+        super().__init__()
+        p = capi.LidParams(total_nx, total_ny or total_nx, total_nz or total_nx, float(reynolds),
+                           float(rho0), float(u0), int(bool(top_layer_u0)), capi.FORMS[precision])
+        ctx = _P()
+        rc = capi.lib().mglc_lid_create(ctypes.byref(p), ctypes.byref(ctx))
+        self._ctx = ctx
+        if rc != capi.MGLC_OK:
+            msg = capi.lib().mglc_last_error(ctx).decode() if ctx else ""
+            self.close()
+            raise capi.MglcError(rc, msg)
+
+    def macro(self):
+        nz, ny, nx = self.shape
+        rho, u, v, w = (np.empty((nz, ny, nx)) for _ in range(4))
+        self._ck(capi.lib().mglc_get_macros(self._ctx, _ptr(rho), _ptr(u), _ptr(v), _ptr(w), None))
+        return rho, u, v, w
+
+    def check(self) -> float:
+        e = ctypes.c_double()
+        self._ck(capi.lib().mglc_check(self._ctx, ctypes.byref(e), None))
+        return e.value
+
+    def load_state(self, f, rho=None, u=None, v=None, w=None):
+        self._ck(capi.lib().mglc_load_state(self._ctx, _ptr(np.ascontiguousarray(f)), None,
+                                            _ptr(rho), _ptr(u), _ptr(v), _ptr(w), None))
+        return self
+
+
+class BuoyancyCavity(_Solve):
+    """D3Q19 forced MRT flow + D3Q7 MRT temperature (reference:
+    Buoyancy_driven_cavity/fortran/3d/bouyancy3d_mpi.F90)."""
+
+    Q_G = 7
+
+    def __init__(self, total_nx, total_ny=None, total_nz=None, rayleigh=1e5, prandtl=0.71,
+                 mach=0.1, t_hot=0.5, t_cold=-0.5, t_ref=0.0, ekman=0.0, bc_y_const_t=True,
+                 bc_z_const_t=False, precision="fp64"):
+        super().__init__()
+        p = capi.ThermalParams(total_nx, total_ny or total_nx, total_nz or total_nx,
+                               float(rayleigh), float(prandtl), float(mach), float(t_hot),
+                               float(t_cold), float(t_ref), float(ekman), int(bool(bc_y_const_t)),
+                               int(bool(bc_z_const_t)), capi.FORMS[precision])
+        ctx = _P()
+        rc = capi.lib().mglc_thermal_create(ctypes.byref(p), ctypes.byref(ctx))
+        self._ctx = ctx
+        if rc != capi.MGLC_OK:
+            msg = capi.lib().mglc_last_error(ctx).decode() if ctx else ""
+            self.close()
+            raise capi.MglcError(rc, msg)
+
+    def macro(self):
+        nz, ny, nx = self.shape
+        rho, u, v, w, T = (np.empty((nz, ny, nx)) for _ in range(5))
+        self._ck(capi.lib().mglc_get_macros(self._ctx, _ptr(rho), _ptr(u), _ptr(v), _ptr(w), _ptr(T)))
+        return rho, u, v, w, T
+
+    def check(self):
+        eu, et = ctypes.c_double(), ctypes.c_double()
+        self._ck(capi.lib().mglc_check(self._ctx, ctypes.byref(eu), ctypes.byref(et)))
+        return eu.value, et.value
+
+    def load_state(self, f, g, rho=None, u=None, v=None, w=None, T=None):
+        self._ck(capi.lib().mglc_load_state(self._ctx, _ptr(np.ascontiguousarray(f)),
+                                            _ptr(np.ascontiguousarray(g)), _ptr(rho), _ptr(u),
+                                            _ptr(v), _ptr(w), _ptr(T)))
+        return self

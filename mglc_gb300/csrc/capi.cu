@@ -1,0 +1,565 @@
+// capi.cu -- the C-ABI of libmglc_gb300.so (declared in include/mglc.h).
+//
+// A context owns every device buffer of one solve: two population buffers
+// (ping-pong, SoA planes), the macroscopic fields the first collision after
+// initial()/load reads, the previous fields of the residual check, the
+// carried body force (thermal), and a small reduction scratch.  All work runs
+// on the context's stream.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mglc.h"
+#include "kernels.cuh"
+
+using namespace mglc;
+
+struct mglc_ctx {
+    int kind = 0, form = FORM_FP64;
+    Geom geom{};
+    long long n = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    // constants
+    double tauf = 0, snu = 0, sq = 0, u0 = 0, rho0 = 1.0;
+    int top_layer_u0 = 1;
+    double viscosity = 0, diffusivity = 0, para_a = 0, gbeta = 0, omega_rot = 0, qd = 0, qnu = 0;
+    double t_hot = 0, t_cold = 0, t_ref = 0;
+    int bc_y = 1, bc_z = 0;
+    float scale = 1.0f, inv_scale = 1.0f;
+    // device buffers
+    void* f[2] = {nullptr, nullptr};
+    void* g[2] = {nullptr, nullptr};
+    int cur = 0;
+    void* F = nullptr;  // carried force, 3 planes (thermal)
+    double *rho = nullptr, *u = nullptr, *v = nullptr, *w = nullptr, *T = nullptr;
+    double *up = nullptr, *vp = nullptr, *wp = nullptr, *Tp = nullptr;
+    double* partials = nullptr;  // reduction scratch
+    double* red_out = nullptr;   // 4 doubles
+    double* stage = nullptr;     // layout staging for host copies
+    size_t stage_bytes = 0;
+    long long device_bytes = 0;
+    // state flags
+    bool first_pending = false;  // next step reads the stored macroscopic fields
+    bool macros_valid = false;   // rho,u,v,w(,T) arrays describe the current state
+    long long itc = 0;
+    bool initialised = false;
+    std::string err;
+};
+
+namespace {
+
+int fail(mglc_ctx* c, int code, const char* fmt, ...) {
+    if (c) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        c->err = buf;
+    }
+    return code;
+}
+
+int cuda_fail(mglc_ctx* c, cudaError_t e, const char* what) {
+    return fail(c, MGLC_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(expr, what)                                    \
+    do {                                                  \
+        cudaError_t e_ = (expr);                          \
+        if (e_ != cudaSuccess) return cuda_fail(c, e_, what); \
+    } while (0)
+
+int dalloc(mglc_ctx* c, void** p, size_t bytes, const char* what) {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return fail(c, MGLC_ERR_NOMEM, "cudaMalloc(%zu bytes) for %s failed: %s", bytes, what,
+                    cudaGetErrorString(e));
+    }
+    c->device_bytes += (long long)bytes;
+    return MGLC_OK;
+}
+
+void release(mglc_ctx* c) {
+    void* ptrs[] = {c->f[0], c->f[1], c->g[0], c->g[1], c->F, c->rho, c->u, c->v, c->w, c->T,
+                    c->up, c->vp, c->wp, c->Tp, c->partials, c->red_out, c->stage};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+}
+
+bool valid_form(int f) { return f >= FORM_FP64 && f <= FORM_BF16; }
+
+// FP16 deviations are scaled so that typical |f - w rho0| (1e-5 .. 1e-1)
+// stays in the normal FP16 range
+constexpr float FP16_SCALE = 256.0f;
+
+int alloc_common(mglc_ctx* c, bool thermal) {
+    const long long n = c->n;
+    const size_t pb = form_bytes(c->form);
+    int rc;
+    for (int b = 0; b < 2; b++)
+        if ((rc = dalloc(c, &c->f[b], (size_t)Q19 * n * pb, "populations f"))) return rc;
+    if (thermal) {
+        for (int b = 0; b < 2; b++)
+            if ((rc = dalloc(c, &c->g[b], (size_t)Q7 * n * pb, "populations g"))) return rc;
+        const size_t cb = c->form == FORM_FP64 ? 8 : 4;
+        if ((rc = dalloc(c, &c->F, 3 * n * cb, "carried force"))) return rc;
+        CK(cudaMemsetAsync(c->F, 0, 3 * n * cb, c->stream), "memset F");
+    }
+    double** fields[] = {&c->rho, &c->u, &c->v, &c->w, &c->up, &c->vp, &c->wp};
+    for (double** fp : fields)
+        if ((rc = dalloc(c, (void**)fp, n * sizeof(double), "macroscopic field"))) return rc;
+    if (thermal) {
+        if ((rc = dalloc(c, (void**)&c->T, n * sizeof(double), "temperature"))) return rc;
+        if ((rc = dalloc(c, (void**)&c->Tp, n * sizeof(double), "temperature"))) return rc;
+    }
+    if ((rc = dalloc(c, (void**)&c->partials, (size_t)reduce_blocks(n) * 4 * sizeof(double),
+                     "reduction scratch")))
+        return rc;
+    if ((rc = dalloc(c, (void**)&c->red_out, 4 * sizeof(double), "reduction result"))) return rc;
+    return MGLC_OK;
+}
+
+int create_stream(mglc_ctx* c) {
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamCreate");
+    c->own_stream = true;
+    return MGLC_OK;
+}
+
+int ensure_stage(mglc_ctx* c, size_t want) {
+    if (c->stage_bytes >= want) return MGLC_OK;
+    if (c->stage) {
+        cudaFree(c->stage);
+        c->device_bytes -= (long long)c->stage_bytes;
+        c->stage = nullptr;
+        c->stage_bytes = 0;
+    }
+    int rc = dalloc(c, (void**)&c->stage, want, "layout staging");
+    if (rc == MGLC_OK) c->stage_bytes = want;
+    return rc;
+}
+
+// cells per host transfer chunk (whole z planes, at most ~64 MiB of AoS doubles)
+long long chunk_cells(const mglc_ctx* c, int Q) {
+    const long long plane = (long long)c->geom.nx * c->geom.ny;
+    long long kc = (64ll << 20) / ((long long)Q * 8 * plane);
+    if (kc < 1) kc = 1;
+    if (kc > c->geom.nz) kc = c->geom.nz;
+    return kc * plane;
+}
+
+int upload_pops(mglc_ctx* c, int Q, const double* host, void* dev, bool shifted) {
+    const long long cc = chunk_cells(c, Q);
+    int rc = ensure_stage(c, (size_t)cc * Q * sizeof(double));
+    if (rc) return rc;
+    for (long long c0 = 0; c0 < c->n; c0 += cc) {
+        long long nc = std::min(cc, c->n - c0);
+        CK(cudaMemcpyAsync(c->stage, host + (size_t)c0 * Q, (size_t)nc * Q * sizeof(double),
+                           cudaMemcpyHostToDevice, c->stream),
+           "copy populations to device");
+        CK(launch_aos_to_soa(c->form, Q, c->geom, c0, nc, c->stage, dev, c->rho0,
+                             Q == Q19 ? c->scale : 1.0f, shifted, c->stream),
+           "aos_to_soa");
+    }
+    return MGLC_OK;
+}
+
+int download_pops(mglc_ctx* c, int Q, const void* dev, double* host, bool shifted) {
+    const long long cc = chunk_cells(c, Q);
+    int rc = ensure_stage(c, (size_t)cc * Q * sizeof(double));
+    if (rc) return rc;
+    for (long long c0 = 0; c0 < c->n; c0 += cc) {
+        long long nc = std::min(cc, c->n - c0);
+        CK(launch_soa_to_aos(c->form, Q, c->geom, c0, nc, dev, c->stage, c->rho0,
+                             Q == Q19 ? c->inv_scale : 1.0f, shifted, c->stream),
+           "soa_to_aos");
+        CK(cudaMemcpyAsync(host + (size_t)c0 * Q, c->stage, (size_t)nc * Q * sizeof(double),
+                           cudaMemcpyDeviceToHost, c->stream),
+           "copy populations to host");
+    }
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
+    return MGLC_OK;
+}
+
+bool thermal(const mglc_ctx* c) { return c->kind == MGLC_KIND_THERMAL; }
+
+// bring rho,u,v,w(,T) up to date with the current populations
+int refresh_macros(mglc_ctx* c) {
+    if (c->macros_valid) return MGLC_OK;
+    CK(launch_macro(c->form, thermal(c), c->geom, c->f[c->cur], thermal(c) ? c->g[c->cur] : nullptr,
+                    c->F, c->rho0, c->inv_scale, c->rho, c->u, c->v, c->w, c->T, c->stream),
+       "macro");
+    c->macros_valid = true;
+    return MGLC_OK;
+}
+
+int check_geom(mglc_ctx* c, int nx, int ny, int nz) {
+    if (nx < 2 || ny < 2 || nz < 2)
+        return fail(c, MGLC_ERR_INVALID, "grid %dx%dx%d: each axis needs at least 2 nodes", nx, ny, nz);
+    if (ny > 65535 || nz > 65535)
+        return fail(c, MGLC_ERR_INVALID, "grid %dx%dx%d: ny and nz are limited to 65535", nx, ny, nz);
+    return MGLC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mglc_lid_create(const mglc_lid_params* p, mglc_ctx** out) {
+    if (!p || !out) return MGLC_ERR_INVALID;
+    *out = nullptr;
+    mglc_ctx* c = new mglc_ctx();
+    int rc = check_geom(c, p->total_nx, p->total_ny, p->total_nz);
+    if (!rc && !valid_form(p->precision)) rc = fail(c, MGLC_ERR_INVALID, "unknown precision %d", p->precision);
+    if (!rc && !(p->reynolds > 0.0)) rc = fail(c, MGLC_ERR_INVALID, "reynolds must be positive");
+    if (rc) {
+        *out = c;  // caller reads the message, then destroys
+        return rc;
+    }
+    c->kind = MGLC_KIND_LID;
+    c->form = p->precision;
+    c->geom = {p->total_nx, p->total_ny, p->total_nz,
+               (long long)p->total_nx * p->total_ny * p->total_nz};
+    c->n = c->geom.plane;
+    c->u0 = p->u0;
+    c->rho0 = p->rho0;
+    c->top_layer_u0 = p->top_layer_u0;
+    // commondata.f90:9,42
+    c->tauf = p->u0 * (double)p->total_nx / p->reynolds * 3.0 + 0.5;
+    c->snu = 1.0 / c->tauf;
+    c->sq = 8.0 * (2.0 * c->tauf - 1.0) / (8.0 * c->tauf - 1.0);
+    if (c->form == FORM_FP16) {
+        c->scale = FP16_SCALE;
+        c->inv_scale = 1.0f / FP16_SCALE;
+    }
+    if ((rc = create_stream(c)) || (rc = alloc_common(c, false))) {
+        *out = c;
+        return rc;
+    }
+    *out = c;
+    return MGLC_OK;
+}
+
+int mglc_thermal_create(const mglc_thermal_params* p, mglc_ctx** out) {
+    if (!p || !out) return MGLC_ERR_INVALID;
+    *out = nullptr;
+    mglc_ctx* c = new mglc_ctx();
+    int rc = check_geom(c, p->total_nx, p->total_ny, p->total_nz);
+    if (!rc && !valid_form(p->precision)) rc = fail(c, MGLC_ERR_INVALID, "unknown precision %d", p->precision);
+    if (!rc && !(p->rayleigh > 0.0 && p->prandtl > 0.0 && p->mach > 0.0))
+        rc = fail(c, MGLC_ERR_INVALID, "rayleigh, prandtl and mach must be positive");
+    if (rc) {
+        *out = c;
+        return rc;
+    }
+    c->kind = MGLC_KIND_THERMAL;
+    c->form = p->precision;
+    c->geom = {p->total_nx, p->total_ny, p->total_nz,
+               (long long)p->total_nx * p->total_ny * p->total_nz};
+    c->n = c->geom.plane;
+    // bouyancy3d_mpi.F90:34-54,80-81
+    const int nz = p->total_nz;
+    c->tauf = 0.5 + p->mach * (double)nz * std::sqrt(3.0 * p->prandtl / p->rayleigh);
+    c->viscosity = (c->tauf - 0.5) / 3.0;
+    c->diffusivity = c->viscosity / p->prandtl;
+    c->omega_rot = p->ekman > 0.0 ? c->viscosity / 2.0 / p->ekman / (double)(nz * nz) : 0.0;
+    c->para_a = 42.0 * std::sqrt(3.0) * c->diffusivity - 6.0;
+    c->gbeta = p->rayleigh * c->viscosity * c->diffusivity / (double)nz / (double)(nz * nz);
+    c->snu = 1.0 / c->tauf;
+    c->sq = 8.0 * (2.0 * c->tauf - 1.0) / (8.0 * c->tauf - 1.0);
+    c->qd = 3.0 - std::sqrt(3.0);
+    c->qnu = 4.0 * std::sqrt(3.0) - 6.0;
+    c->t_hot = p->t_hot;
+    c->t_cold = p->t_cold;
+    c->t_ref = p->t_ref;
+    c->bc_y = p->bc_y_const_t ? 1 : 0;
+    c->bc_z = p->bc_z_const_t ? 1 : 0;
+    c->rho0 = 1.0;
+    if (c->form == FORM_FP16) {
+        c->scale = FP16_SCALE;
+        c->inv_scale = 1.0f / FP16_SCALE;
+    }
+    if ((rc = create_stream(c)) || (rc = alloc_common(c, true))) {
+        *out = c;
+        return rc;
+    }
+    *out = c;
+    return MGLC_OK;
+}
+
+void mglc_destroy(mglc_ctx* c) {
+    if (!c) return;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    release(c);
+    delete c;
+}
+
+const char* mglc_last_error(const mglc_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int mglc_set_stream(mglc_ctx* c, void* s) {
+    if (!c) return MGLC_ERR_INVALID;
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
+    if (c->own_stream) cudaStreamDestroy(c->stream);
+    if (s) {
+        c->stream = (cudaStream_t)s;
+        c->own_stream = false;
+        return MGLC_OK;
+    }
+    return create_stream(c);
+}
+
+int mglc_get_info(const mglc_ctx* c, mglc_info* o) {
+    if (!c || !o) return MGLC_ERR_INVALID;
+    std::memset(o, 0, sizeof *o);
+    o->kind = c->kind;
+    o->precision = c->form;
+    o->nx = c->geom.nx;
+    o->ny = c->geom.ny;
+    o->nz = c->geom.nz;
+    o->itc = c->itc;
+    o->tauf = c->tauf;
+    o->snu = c->snu;
+    o->sq = c->sq;
+    o->viscosity = c->kind == MGLC_KIND_LID ? (c->tauf - 0.5) / 3.0 : c->viscosity;
+    o->diffusivity = c->diffusivity;
+    o->para_a = c->para_a;
+    o->gbeta = c->gbeta;
+    o->omega_rot = c->omega_rot;
+    const double pb = (double)form_bytes(c->form);
+    if (c->kind == MGLC_KIND_LID) {
+        o->bytes_per_cell_step = 2.0 * Q19 * pb;
+    } else {
+        const double cb = c->form == FORM_FP64 ? 8.0 : 4.0;
+        // carried force: read and written once per step (F_z only without rotation)
+        const double carried = 2.0 * (c->omega_rot != 0.0 ? 3.0 : 1.0) * cb;
+        o->bytes_per_cell_step = 2.0 * (Q19 + Q7) * pb + carried;
+    }
+    o->device_bytes = c->device_bytes;
+    return MGLC_OK;
+}
+
+int mglc_initial(mglc_ctx* c) {
+    if (!c || !c->kind) return MGLC_ERR_INVALID;
+    const long long n = c->n;
+    const Geom& g = c->geom;
+    // rho = rho0, u = v = w = 0 (and T); lid top layer u = U0; hot/cold walls
+    std::vector<double> hr(n, c->kind == MGLC_KIND_LID ? c->rho0 : 1.0), hu(n, 0.0), hz(n, 0.0);
+    std::vector<double> ht;
+    if (c->kind == MGLC_KIND_LID && c->top_layer_u0) {
+        const long long top = (long long)g.nx * g.ny * (g.nz - 1);
+        for (long long q = 0; q < (long long)g.nx * g.ny; q++) hu[top + q] = c->u0;
+    }
+    if (thermal(c)) {
+        ht.assign(n, 0.0);
+        if (c->bc_y)
+            for (int k = 0; k < g.nz; k++)
+                for (int i = 0; i < g.nx; i++) {
+                    ht[i + (long long)g.nx * (0 + (long long)g.ny * k)] = c->t_hot;
+                    ht[i + (long long)g.nx * ((g.ny - 1) + (long long)g.ny * k)] = c->t_cold;
+                }
+        if (c->bc_z)
+            for (int j = 0; j < g.ny; j++)
+                for (int i = 0; i < g.nx; i++) {
+                    ht[i + (long long)g.nx * j] = c->t_hot;
+                    ht[i + (long long)g.nx * (j + (long long)g.ny * (g.nz - 1))] = c->t_cold;
+                }
+    }
+    const size_t b = n * sizeof(double);
+    CK(cudaMemcpyAsync(c->rho, hr.data(), b, cudaMemcpyHostToDevice, c->stream), "copy rho");
+    CK(cudaMemcpyAsync(c->u, hu.data(), b, cudaMemcpyHostToDevice, c->stream), "copy u");
+    CK(cudaMemcpyAsync(c->v, hz.data(), b, cudaMemcpyHostToDevice, c->stream), "copy v");
+    CK(cudaMemcpyAsync(c->w, hz.data(), b, cudaMemcpyHostToDevice, c->stream), "copy w");
+    CK(cudaMemsetAsync(c->up, 0, b, c->stream), "zero up");
+    CK(cudaMemsetAsync(c->vp, 0, b, c->stream), "zero vp");
+    CK(cudaMemsetAsync(c->wp, 0, b, c->stream), "zero wp");
+    if (thermal(c)) {
+        CK(cudaMemcpyAsync(c->T, ht.data(), b, cudaMemcpyHostToDevice, c->stream), "copy T");
+        CK(cudaMemsetAsync(c->Tp, 0, b, c->stream), "zero Tp");
+    }
+    CK(launch_equilibrium(c->form, thermal(c), g, c->rho, c->u, c->v, c->w, c->T, c->para_a,
+                          c->rho0, c->scale, c->f[0], thermal(c) ? c->g[0] : nullptr, c->stream),
+       "equilibrium");
+    CK(cudaStreamSynchronize(c->stream), "synchronize");  // host vectors go out of scope
+    c->cur = 0;
+    c->itc = 0;
+    c->first_pending = true;
+    c->macros_valid = true;
+    c->initialised = true;
+    return MGLC_OK;
+}
+
+int mglc_load_state(mglc_ctx* c, const double* f, const double* g, const double* rho,
+                    const double* u, const double* v, const double* w, const double* T) {
+    if (!c || !c->kind || !f) return c ? fail(c, MGLC_ERR_INVALID, "f is required") : MGLC_ERR_INVALID;
+    if (thermal(c) && !g) return fail(c, MGLC_ERR_INVALID, "thermal contexts need g");
+    const bool shifted = c->form != FORM_FP64;
+    int rc;
+    if ((rc = upload_pops(c, Q19, f, c->f[0], shifted))) return rc;
+    if (thermal(c) && (rc = upload_pops(c, Q7, g, c->g[0], false))) return rc;
+    const size_t b = c->n * sizeof(double);
+    const bool any = rho || u || v || w || T;
+    if (any) {
+        if (!(u && v && w) || (thermal(c) && !T))
+            return fail(c, MGLC_ERR_INVALID, "u, v, w (and T) must be given together");
+        if (rho) {
+            CK(cudaMemcpyAsync(c->rho, rho, b, cudaMemcpyHostToDevice, c->stream), "copy rho");
+        } else {
+            // reference reload path keeps rho = 1 (bouyancy3d_mpi.F90:556,598-611)
+            std::vector<double> ones(c->n, c->rho0);
+            CK(cudaMemcpyAsync(c->rho, ones.data(), b, cudaMemcpyHostToDevice, c->stream), "copy rho");
+            CK(cudaStreamSynchronize(c->stream), "synchronize");
+        }
+        CK(cudaMemcpyAsync(c->u, u, b, cudaMemcpyHostToDevice, c->stream), "copy u");
+        CK(cudaMemcpyAsync(c->v, v, b, cudaMemcpyHostToDevice, c->stream), "copy v");
+        CK(cudaMemcpyAsync(c->w, w, b, cudaMemcpyHostToDevice, c->stream), "copy w");
+        if (thermal(c)) CK(cudaMemcpyAsync(c->T, T, b, cudaMemcpyHostToDevice, c->stream), "copy T");
+        c->macros_valid = true;
+    } else {
+        if (thermal(c)) {
+            const size_t cb = c->form == FORM_FP64 ? 8 : 4;
+            CK(cudaMemsetAsync(c->F, 0, 3 * c->n * cb, c->stream), "zero F");
+        }
+        c->cur = 0;
+        c->macros_valid = false;
+        if ((rc = refresh_macros(c))) return rc;
+    }
+    CK(cudaMemsetAsync(c->up, 0, b, c->stream), "zero up");
+    CK(cudaMemsetAsync(c->vp, 0, b, c->stream), "zero vp");
+    CK(cudaMemsetAsync(c->wp, 0, b, c->stream), "zero wp");
+    if (thermal(c)) CK(cudaMemsetAsync(c->Tp, 0, b, c->stream), "zero Tp");
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
+    c->cur = 0;
+    c->itc = 0;
+    c->first_pending = true;
+    c->initialised = true;
+    return MGLC_OK;
+}
+
+int mglc_get_f(mglc_ctx* c, double* f, double* g) {
+    if (!c || !c->kind) return MGLC_ERR_INVALID;
+    if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial or mglc_load_state first");
+    const bool shifted = c->form != FORM_FP64;
+    int rc;
+    if (f && (rc = download_pops(c, Q19, c->f[c->cur], f, shifted))) return rc;
+    if (g && thermal(c) && (rc = download_pops(c, Q7, c->g[c->cur], g, false))) return rc;
+    return MGLC_OK;
+}
+
+int mglc_step(mglc_ctx* c, int nsteps) {
+    if (!c || !c->kind) return MGLC_ERR_INVALID;
+    if (nsteps < 0) return fail(c, MGLC_ERR_INVALID, "nsteps must be >= 0");
+    if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial or mglc_load_state first");
+    for (int s = 0; s < nsteps; s++) {
+        const int nxt = c->cur ^ 1;
+        cudaError_t e;
+        if (c->kind == MGLC_KIND_LID) {
+            LidStepArgs a;
+            a.g = c->geom;
+            a.cd = make_mrt_coef(c->snu, c->sq);
+            a.u0 = c->u0;
+            a.rho0 = c->rho0;
+            a.scale = c->scale;
+            a.inv_scale = c->inv_scale;
+            a.rho = c->rho; a.u = c->u; a.v = c->v; a.w = c->w;
+            e = launch_lid_step(c->form, c->first_pending, c->f[c->cur], c->f[nxt], a, c->stream);
+        } else {
+            ThermalStepArgs a;
+            a.g = c->geom;
+            a.cd = make_mrt_coef(c->snu, c->sq);
+            a.gbeta = c->gbeta; a.omega_rot = c->omega_rot; a.t_ref = c->t_ref;
+            a.para_a = c->para_a; a.qd = c->qd; a.qnu = c->qnu;
+            a.t_hot = c->t_hot; a.t_cold = c->t_cold; a.rho0 = c->rho0;
+            a.bc_y = c->bc_y; a.bc_z = c->bc_z;
+            a.scale = c->scale; a.inv_scale = c->inv_scale;
+            a.rho = c->rho; a.u = c->u; a.v = c->v; a.w = c->w; a.T = c->T;
+            e = launch_thermal_step(c->form, c->first_pending, c->f[c->cur], c->f[nxt], c->g[c->cur],
+                                    c->g[nxt], c->F, a, c->stream);
+        }
+        if (e != cudaSuccess) return cuda_fail(c, e, "step kernel launch");
+        c->cur = nxt;
+        c->first_pending = false;
+        c->macros_valid = false;
+        c->itc++;
+    }
+    return MGLC_OK;
+}
+
+int mglc_get_macros_device(mglc_ctx* c, double* rho, double* u, double* v, double* w, double* T) {
+    if (!c || !c->kind) return MGLC_ERR_INVALID;
+    if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial or mglc_load_state first");
+    int rc = refresh_macros(c);
+    if (rc) return rc;
+    const size_t b = c->n * sizeof(double);
+    if (rho) CK(cudaMemcpyAsync(rho, c->rho, b, cudaMemcpyDeviceToDevice, c->stream), "copy rho");
+    if (u) CK(cudaMemcpyAsync(u, c->u, b, cudaMemcpyDeviceToDevice, c->stream), "copy u");
+    if (v) CK(cudaMemcpyAsync(v, c->v, b, cudaMemcpyDeviceToDevice, c->stream), "copy v");
+    if (w) CK(cudaMemcpyAsync(w, c->w, b, cudaMemcpyDeviceToDevice, c->stream), "copy w");
+    if (T && thermal(c)) CK(cudaMemcpyAsync(T, c->T, b, cudaMemcpyDeviceToDevice, c->stream), "copy T");
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
+    return MGLC_OK;
+}
+
+int mglc_get_macros(mglc_ctx* c, double* rho, double* u, double* v, double* w, double* T) {
+    if (!c || !c->kind) return MGLC_ERR_INVALID;
+    if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial or mglc_load_state first");
+    int rc = refresh_macros(c);
+    if (rc) return rc;
+    const size_t b = c->n * sizeof(double);
+    if (rho) CK(cudaMemcpyAsync(rho, c->rho, b, cudaMemcpyDeviceToHost, c->stream), "copy rho");
+    if (u) CK(cudaMemcpyAsync(u, c->u, b, cudaMemcpyDeviceToHost, c->stream), "copy u");
+    if (v) CK(cudaMemcpyAsync(v, c->v, b, cudaMemcpyDeviceToHost, c->stream), "copy v");
+    if (w) CK(cudaMemcpyAsync(w, c->w, b, cudaMemcpyDeviceToHost, c->stream), "copy w");
+    if (T && thermal(c)) CK(cudaMemcpyAsync(T, c->T, b, cudaMemcpyDeviceToHost, c->stream), "copy T");
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
+    return MGLC_OK;
+}
+
+int mglc_check(mglc_ctx* c, double* error_u, double* error_t) {
+    if (!c || !c->kind) return MGLC_ERR_INVALID;
+    if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial or mglc_load_state first");
+    int rc = refresh_macros(c);
+    if (rc) return rc;
+    CK(launch_residual(c->n, c->u, c->v, c->w, thermal(c) ? c->T : nullptr, c->up, c->vp, c->wp,
+                       c->Tp, thermal(c), c->partials, c->red_out, c->stream),
+       "residual");
+    double e[4];
+    CK(cudaMemcpyAsync(e, c->red_out, sizeof e, cudaMemcpyDeviceToHost, c->stream), "copy residual");
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
+    const double eu = std::sqrt(e[0]) / std::sqrt(e[1]);
+    if (error_u) *error_u = eu;
+    if (error_t) *error_t = thermal(c) ? e[2] / e[3] : 0.0;
+    if (!std::isfinite(e[0]) || !std::isfinite(e[1]))
+        return fail(c, MGLC_ERR_NUMERIC, "non-finite velocity field at step %lld", c->itc);
+    return MGLC_OK;
+}
+
+int mglc_totals(mglc_ctx* c, double* mass, double* energy, double* heat) {
+    if (!c || !c->kind) return MGLC_ERR_INVALID;
+    if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial or mglc_load_state first");
+    int rc = refresh_macros(c);
+    if (rc) return rc;
+    CK(launch_totals(c->n, c->rho, c->u, c->v, c->w, thermal(c) ? c->T : nullptr, c->partials,
+                     c->red_out, c->stream),
+       "totals");
+    double e[3];
+    CK(cudaMemcpyAsync(e, c->red_out, sizeof e, cudaMemcpyDeviceToHost, c->stream), "copy totals");
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
+    if (mass) *mass = e[0];
+    if (energy) *energy = e[1];
+    if (heat) *heat = e[2];
+    if (!std::isfinite(e[0]) || !std::isfinite(e[1]))
+        return fail(c, MGLC_ERR_NUMERIC, "non-finite totals at step %lld", c->itc);
+    return MGLC_OK;
+}
+
+}  // extern "C"

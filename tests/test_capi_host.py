@@ -1,0 +1,62 @@
+"""CPU-only checks of the C-ABI library: it loads, exports every symbol that
+include/mglc.h declares, and rejects bad parameters before touching the GPU."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from mglc_gb300 import build as B
+from mglc_gb300 import capi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "mglc.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(mglc_\w+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    B.build()
+    return capi.lib()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    names = declared_symbols()
+    assert len(names) >= 14
+    for n in names:
+        assert hasattr(lib, n), n
+    # the Python binding declares the same set
+    assert set(names) == set(capi.SIGNATURES)
+
+
+def test_invalid_parameters_are_rejected_without_a_gpu(lib):
+    ctx = ctypes.c_void_p()
+    p = capi.LidParams(1, 8, 8, 400.0, 1.0, 0.1, 1, 0)
+    rc = lib.mglc_lid_create(ctypes.byref(p), ctypes.byref(ctx))
+    assert rc == 1
+    assert b"at least 2" in lib.mglc_last_error(ctx)
+    lib.mglc_destroy(ctx)
+    p = capi.LidParams(8, 8, 8, -1.0, 1.0, 0.1, 1, 0)
+    ctx = ctypes.c_void_p()
+    assert lib.mglc_lid_create(ctypes.byref(p), ctypes.byref(ctx)) == 1
+    lib.mglc_destroy(ctx)
+    p = capi.LidParams(8, 8, 8, 400.0, 1.0, 0.1, 1, 9)
+    ctx = ctypes.c_void_p()
+    assert lib.mglc_lid_create(ctypes.byref(p), ctypes.byref(ctx)) == 1
+    assert b"precision" in lib.mglc_last_error(ctx)
+    lib.mglc_destroy(ctx)
+    t = capi.ThermalParams(8, 8, 8, -1.0, 0.71, 0.1, 0.5, -0.5, 0.0, 0.0, 1, 0, 0)
+    ctx = ctypes.c_void_p()
+    assert lib.mglc_thermal_create(ctypes.byref(t), ctypes.byref(ctx)) == 1
+    lib.mglc_destroy(ctx)
+
+
+def test_null_arguments(lib):
+    assert lib.mglc_lid_create(None, None) == 1
+    assert lib.mglc_step(None, 1) == 1
+    assert lib.mglc_last_error(None) == b"null context"
+    lib.mglc_destroy(None)
