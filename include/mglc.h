@@ -130,6 +130,26 @@ int mglc_totals(mglc_ctx* ctx, double* mass, double* energy, double* heat);
 int mglc_get_macros_device(mglc_ctx* ctx, double* rho, double* u, double* v, double* w,
                            double* T);
 
+/* ---- no-allocation variant ----------------------------------------------- */
+/* No counterpart in the reference.  The residual of check() (errorU, and errorT
+ * when T and Tp are given) over caller-owned DEVICE arrays of n cells, for
+ * callers that cannot allocate device memory: hosts whose device memory is
+ * owned by another runtime's fixed pool, or latency-critical loops that must
+ * not pay cudaMalloc's implicit synchronisation.  Allocates nothing: the
+ * reduction's partial sums live in a static device array (512 KiB + 32 B per
+ * GPU, held until exit).  n is limited to 67,108,864 cells; larger n returns
+ * MGLC_ERR_INVALID.  with_w = 0 is the lid residual (w left out of the
+ * numerator), 1 the thermal one.  up, vp, wp (and Tp) receive the current
+ * fields like the reference's check().  All calls share the static array:
+ * calls that overlap on the GPU race.  The first call on a device looks up the
+ * array's address; make it before any stream capture.  Synchronises
+ * cuda_stream (NULL = legacy default stream).  On failure a message is written
+ * to errbuf (may be NULL). */
+int mglc_residual_noalloc(long long n, const double* u, const double* v, const double* w,
+                          const double* T, double* up, double* vp, double* wp, double* Tp,
+                          int with_w, void* cuda_stream, double* error_u, double* error_t,
+                          char* errbuf, int errbuf_len);
+
 #ifdef __cplusplus
 }
 #endif
