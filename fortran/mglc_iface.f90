@@ -1,0 +1,105 @@
+!! mglc_iface.f90 -- iso_c_binding interface to libmglc_gb300.so for the MGLC
+!! Fortran drivers.  Source only in this repository: no Fortran compiler is
+!! available where it is built and tested; the same C-ABI is exercised from
+!! C/C++ and Python.  Every function returns an integer status (0 = OK);
+!! mglc_last_error_f returns the context's message.
+!!
+!! Array arguments are the reference's own arrays, passed without copies:
+!!   f(0:18,1:nx,1:ny,1:nz), g(0:6,1:nx,1:ny,1:nz), rho/u/v/w/T(1:nx,1:ny,1:nz).
+module mglc_iface
+    use iso_c_binding
+    implicit none
+
+    integer(c_int), parameter :: MGLC_OK = 0
+    integer(c_int), parameter :: MGLC_FP64 = 0, MGLC_FP32 = 1, MGLC_FP16 = 2, MGLC_BF16 = 3
+
+    type, bind(C) :: mglc_lid_params
+        integer(c_int) :: total_nx, total_ny, total_nz
+        real(c_double) :: reynolds, rho0, u0
+        integer(c_int) :: top_layer_u0, precision
+    end type
+
+    type, bind(C) :: mglc_thermal_params
+        integer(c_int) :: total_nx, total_ny, total_nz
+        real(c_double) :: rayleigh, prandtl, mach
+        real(c_double) :: t_hot, t_cold, t_ref
+        real(c_double) :: ekman
+        integer(c_int) :: bc_y_const_t, bc_z_const_t, precision
+    end type
+
+    interface
+        integer(c_int) function mglc_lid_create(p, ctx) bind(C, name="mglc_lid_create")
+            import :: c_int, c_ptr, mglc_lid_params
+            type(mglc_lid_params), intent(in) :: p
+            type(c_ptr), intent(out) :: ctx
+        end function
+        integer(c_int) function mglc_thermal_create(p, ctx) bind(C, name="mglc_thermal_create")
+            import :: c_int, c_ptr, mglc_thermal_params
+            type(mglc_thermal_params), intent(in) :: p
+            type(c_ptr), intent(out) :: ctx
+        end function
+        subroutine mglc_destroy(ctx) bind(C, name="mglc_destroy")
+            import :: c_ptr
+            type(c_ptr), value :: ctx
+        end subroutine
+        type(c_ptr) function mglc_last_error(ctx) bind(C, name="mglc_last_error")
+            import :: c_ptr
+            type(c_ptr), value :: ctx
+        end function
+        integer(c_int) function mglc_initial(ctx) bind(C, name="mglc_initial")
+            import :: c_int, c_ptr
+            type(c_ptr), value :: ctx
+        end function
+        integer(c_int) function mglc_load_state(ctx, f, g, rho, u, v, w, T) &
+                bind(C, name="mglc_load_state")
+            import :: c_int, c_ptr
+            type(c_ptr), value :: ctx, f, g, rho, u, v, w, T
+        end function
+        integer(c_int) function mglc_get_f(ctx, f, g) bind(C, name="mglc_get_f")
+            import :: c_int, c_ptr
+            type(c_ptr), value :: ctx, f, g
+        end function
+        integer(c_int) function mglc_step(ctx, nsteps) bind(C, name="mglc_step")
+            import :: c_int, c_ptr
+            type(c_ptr), value :: ctx
+            integer(c_int), value :: nsteps
+        end function
+        integer(c_int) function mglc_get_macros(ctx, rho, u, v, w, T) bind(C, name="mglc_get_macros")
+            import :: c_int, c_ptr
+            type(c_ptr), value :: ctx, rho, u, v, w, T
+        end function
+        integer(c_int) function mglc_check(ctx, error_u, error_t) bind(C, name="mglc_check")
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), intent(out) :: error_u, error_t
+        end function
+        integer(c_int) function mglc_totals(ctx, mass, energy, heat) bind(C, name="mglc_totals")
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), intent(out) :: mass, energy, heat
+        end function
+        integer(c_int) function mglc_nusselt(ctx, nu_vol, re_vol, nu_hot, nu_cold) &
+                bind(C, name="mglc_nusselt")
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), intent(out) :: nu_vol, re_vol, nu_hot, nu_cold
+        end function
+    end interface
+
+contains
+
+    !! Fortran string of the context's last error message.
+    function mglc_last_error_f(ctx) result(msg)
+        type(c_ptr), intent(in) :: ctx
+        character(len=512) :: msg
+        character(kind=c_char), pointer :: p(:)
+        integer :: i
+        msg = ''
+        call c_f_pointer(mglc_last_error(ctx), p, [512])
+        do i = 1, 512
+            if (p(i) == c_null_char) exit
+            msg(i:i) = p(i)
+        enddo
+    end function
+
+end module mglc_iface

@@ -125,6 +125,14 @@ int mglc_check(mglc_ctx* ctx, double* error_u, double* error_t);
  * heat = sum T (thermal, else 0).  Any pointer may be NULL. */
 int mglc_totals(mglc_ctx* ctx, double* mass, double* energy, double* heat);
 
+/* Thermal statistics of the current state.  nu_vol and re_vol restate the
+ * reference's calNuRe (mpi_blocked/RaNu.F90:13-47): Nu = <w T> nz/kappa + 1,
+ * Re = sqrt(<|u|^2>) nz/nu.  nu_hot / nu_cold are wall Nusselt numbers at the
+ * constant-temperature walls (no reference counterpart): -L/dT times the
+ * wall-averaged temperature gradient, taken second order at the halfway wall.
+ * Any pointer may be NULL.  Synchronises. */
+int mglc_nusselt(mglc_ctx* ctx, double* nu_vol, double* re_vol, double* nu_hot, double* nu_cold);
+
 /* ---- device-resident variants (no host copies) --------------------------- */
 /* Same as mglc_get_macros but into device buffers of nx*ny*nz doubles. */
 int mglc_get_macros_device(mglc_ctx* ctx, double* rho, double* u, double* v, double* w,

@@ -58,6 +58,7 @@ SIGNATURES = {
     "mglc_get_macros_device": ([_VP, _VP, _VP, _VP, _VP, _VP], _I),
     "mglc_check": ([_VP, _DP, _DP], _I),
     "mglc_totals": ([_VP, _DP, _DP, _DP], _I),
+    "mglc_nusselt": ([_VP, _DP, _DP, _DP, _DP], _I),
     "mglc_residual_noalloc": ([_LL, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _I, _VP, _DP, _DP,
                                ctypes.c_char_p, _I], _I),
 }

@@ -167,6 +167,12 @@ class BuoyancyCavity(_Solve):
         self._ck(capi.lib().mglc_check(self._ctx, ctypes.byref(eu), ctypes.byref(et)))
         return eu.value, et.value
 
+    def nusselt(self):
+        """(Nu_vol, Re_vol, Nu_hot, Nu_cold): calNuRe plus wall Nusselt numbers."""
+        vals = [ctypes.c_double() for _ in range(4)]
+        self._ck(capi.lib().mglc_nusselt(self._ctx, *[ctypes.byref(v) for v in vals]))
+        return tuple(v.value for v in vals)
+
     def load_state(self, f, g, rho=None, u=None, v=None, w=None, T=None):
         self._ck(capi.lib().mglc_load_state(self._ctx, _ptr(np.ascontiguousarray(f)),
                                             _ptr(np.ascontiguousarray(g)), _ptr(rho), _ptr(u),

@@ -109,8 +109,10 @@ int alloc_common(mglc_ctx* c, bool thermal) {
     for (int b = 0; b < 2; b++)
         if ((rc = dalloc(c, &c->f[b], (size_t)Q19 * n * pb, "populations f"))) return rc;
     if (thermal) {
+        // temperature populations in the arithmetic type (FP64 or FP32)
+        const size_t gb = c->form == FORM_FP64 ? 8 : 4;
         for (int b = 0; b < 2; b++)
-            if ((rc = dalloc(c, &c->g[b], (size_t)Q7 * n * pb, "populations g"))) return rc;
+            if ((rc = dalloc(c, &c->g[b], (size_t)Q7 * n * gb, "populations g"))) return rc;
         const size_t cb = c->form == FORM_FP64 ? 8 : 4;
         if ((rc = dalloc(c, &c->F, 3 * n * cb, "carried force"))) return rc;
         CK(cudaMemsetAsync(c->F, 0, 3 * n * cb, c->stream), "memset F");
@@ -158,6 +160,12 @@ long long chunk_cells(const mglc_ctx* c, int Q) {
     return kc * plane;
 }
 
+// storage form of a population set: f in the context's form, g in FP64/FP32
+int pop_form(const mglc_ctx* c, int Q) {
+    if (Q == Q19) return c->form;
+    return c->form == FORM_FP64 ? FORM_FP64 : FORM_FP32;
+}
+
 int upload_pops(mglc_ctx* c, int Q, const double* host, void* dev, bool shifted) {
     const long long cc = chunk_cells(c, Q);
     int rc = ensure_stage(c, (size_t)cc * Q * sizeof(double));
@@ -167,7 +175,7 @@ int upload_pops(mglc_ctx* c, int Q, const double* host, void* dev, bool shifted)
         CK(cudaMemcpyAsync(c->stage, host + (size_t)c0 * Q, (size_t)nc * Q * sizeof(double),
                            cudaMemcpyHostToDevice, c->stream),
            "copy populations to device");
-        CK(launch_aos_to_soa(c->form, Q, c->geom, c0, nc, c->stage, dev, c->rho0,
+        CK(launch_aos_to_soa(pop_form(c, Q), Q, c->geom, c0, nc, c->stage, dev, c->rho0,
                              Q == Q19 ? c->scale : 1.0f, shifted, c->stream),
            "aos_to_soa");
     }
@@ -180,7 +188,7 @@ int download_pops(mglc_ctx* c, int Q, const void* dev, double* host, bool shifte
     if (rc) return rc;
     for (long long c0 = 0; c0 < c->n; c0 += cc) {
         long long nc = std::min(cc, c->n - c0);
-        CK(launch_soa_to_aos(c->form, Q, c->geom, c0, nc, dev, c->stage, c->rho0,
+        CK(launch_soa_to_aos(pop_form(c, Q), Q, c->geom, c0, nc, dev, c->stage, c->rho0,
                              Q == Q19 ? c->inv_scale : 1.0f, shifted, c->stream),
            "soa_to_aos");
         CK(cudaMemcpyAsync(host + (size_t)c0 * Q, c->stage, (size_t)nc * Q * sizeof(double),
@@ -340,9 +348,10 @@ int mglc_get_info(const mglc_ctx* c, mglc_info* o) {
         o->bytes_per_cell_step = 2.0 * Q19 * pb;
     } else {
         const double cb = c->form == FORM_FP64 ? 8.0 : 4.0;
-        // carried force: read and written once per step (F_z only without rotation)
+        // carried force: read and written once per step (F_z only without rotation);
+        // g is kept in the arithmetic type
         const double carried = 2.0 * (c->omega_rot != 0.0 ? 3.0 : 1.0) * cb;
-        o->bytes_per_cell_step = 2.0 * (Q19 + Q7) * pb + carried;
+        o->bytes_per_cell_step = 2.0 * Q19 * pb + 2.0 * Q7 * cb + carried;
     }
     o->device_bytes = c->device_bytes;
     return MGLC_OK;
@@ -559,6 +568,34 @@ int mglc_totals(mglc_ctx* c, double* mass, double* energy, double* heat) {
     if (heat) *heat = e[2];
     if (!std::isfinite(e[0]) || !std::isfinite(e[1]))
         return fail(c, MGLC_ERR_NUMERIC, "non-finite totals at step %lld", c->itc);
+    return MGLC_OK;
+}
+
+int mglc_nusselt(mglc_ctx* c, double* nu_vol, double* re_vol, double* nu_hot, double* nu_cold) {
+    if (!c || !c->kind) return MGLC_ERR_INVALID;
+    if (!thermal(c)) return fail(c, MGLC_ERR_STATE, "mglc_nusselt needs a thermal context");
+    if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial or mglc_load_state first");
+    int rc = refresh_macros(c);
+    if (rc) return rc;
+    const int axis = c->bc_y ? 1 : (c->bc_z ? 2 : 0);
+    CK(launch_thermal_stats(c->geom, c->u, c->v, c->w, c->T, axis, c->partials, c->red_out,
+                            c->stream),
+       "thermal statistics");
+    double e[4];
+    CK(cudaMemcpyAsync(e, c->red_out, sizeof e, cudaMemcpyDeviceToHost, c->stream), "copy stats");
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
+    const Geom& g = c->geom;
+    const double ncell = (double)g.nx * g.ny * g.nz;
+    // RaNu.F90:23,47
+    if (nu_vol) *nu_vol = e[0] / ncell * (double)g.nz / c->diffusivity + 1.0;
+    if (re_vol) *re_vol = std::sqrt(e[1] / ncell) * (double)g.nz / c->viscosity;
+    const double dT = c->t_hot - c->t_cold;
+    double L = 0.0, nwall = 0.0;
+    if (axis == 1) { L = g.ny; nwall = (double)g.nx * g.nz; }
+    if (axis == 2) { L = g.nz; nwall = (double)g.nx * g.ny; }
+    // dT/dn at the hot wall = (9T1 - T2 - 8Th)/3, heat leaves the hot wall: Nu = -L/dT * dT/dn
+    if (nu_hot) *nu_hot = axis ? -L / dT * ((e[2] / nwall - 8.0 * c->t_hot) / 3.0) : 0.0;
+    if (nu_cold) *nu_cold = axis ? L / dT * ((e[3] / nwall - 8.0 * c->t_cold) / 3.0) : 0.0;
     return MGLC_OK;
 }
 

@@ -49,8 +49,13 @@ __device__ __forceinline__ double pop_abs(const S* p, long long idx, int q, doub
 // the order of the alpha loop (macro.f90:6-25 / bouyancy3d_mpi.F90:986-1010),
 // with the thermal half-force shift.  Uses IEEE-rounded adds, multiplies and
 // divisions so that for FP64 storage the fields equal the reference's.
+// storage type of the temperature populations for a given f storage type
+template <typename S> struct GType { using T = float; };
+template <> struct GType<double> { using T = double; };
+
 template <typename S, bool THERMAL>
-__global__ void k_macro(const S* __restrict__ f, const S* __restrict__ gt, const void* Fv,
+__global__ void k_macro(const S* __restrict__ f, const typename GType<S>::T* __restrict__ gt,
+                        const void* Fv,
                         Geom g, double rho0, double inv_scale, double* rho, double* u, double* v,
                         double* w, double* T) {
     const long long n = g.plane;
@@ -83,9 +88,9 @@ __global__ void k_macro(const S* __restrict__ f, const S* __restrict__ gt, const
             jx = __dadd_rn(jx, __dmul_rn(0.5, Fx));
             jy = __dadd_rn(jy, __dmul_rn(0.5, Fy));
             jz = __dadd_rn(jz, __dmul_rn(0.5, Fz));
-            double t = to_d<S>(gt[c]);
+            double t = (double)gt[c];
 #pragma unroll
-            for (int q = 1; q < Q7; q++) t = __dadd_rn(t, to_d<S>(gt[q * n + c]));
+            for (int q = 1; q < Q7; q++) t = __dadd_rn(t, (double)gt[q * n + c]);
             T[c] = t;
         }
         rho[c] = r;
@@ -108,7 +113,7 @@ static cudaError_t macro_go(bool thermal, const Geom& g, const void* f, const vo
                             double* v, double* w, double* T, cudaStream_t s) {
     int gr = grid_for(g.plane, 256);
     if (thermal)
-        k_macro<S, true><<<gr, 256, 0, s>>>((const S*)f, (const S*)gt, F, g, rho0, inv, rho, u, v, w, T);
+        k_macro<S, true><<<gr, 256, 0, s>>>((const S*)f, (const typename GType<S>::T*)gt, F, g, rho0, inv, rho, u, v, w, T);
     else
         k_macro<S, false><<<gr, 256, 0, s>>>((const S*)f, nullptr, nullptr, g, rho0, inv, rho, u, v, w, T);
     return cudaGetLastError();
@@ -133,7 +138,7 @@ cudaError_t launch_macro(int form, bool thermal, const Geom& g, const void* f, c
 template <typename S, bool THERMAL>
 __global__ void k_equilibrium(Geom g, const double* rho, const double* u, const double* v,
                               const double* w, const double* T, double para_a, double rho0,
-                              double scale, S* f, S* gt) {
+                              double scale, S* f, typename GType<S>::T* gt) {
     const long long n = g.plane;
     const bool shifted = !std::is_same<S, double>::value;
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
@@ -160,7 +165,7 @@ __global__ void k_equilibrium(Geom g, const double* rho, const double* u, const 
                 double un = __dadd_rn(__dadd_rn(__dmul_rn(uu, (double)ex19(q)), __dmul_rn(vv, (double)ey19(q))),
                                       __dmul_rn(ww, (double)ez19(q)));
                 double ge = __dmul_rn(__dmul_rn(q == 0 ? wt0 : wt, t), __dadd_rn(1.0, __dmul_rn(coef, un)));
-                gt[q * n + c] = from_d<S>(ge);
+                gt[q * n + c] = (typename GType<S>::T)ge;
             }
         }
     }
@@ -172,7 +177,8 @@ static cudaError_t eq_go(bool thermal, const Geom& g, const double* rho, const d
                          double rho0, double scale, void* f, void* gt, cudaStream_t s) {
     int gr = grid_for(g.plane, 256);
     if (thermal)
-        k_equilibrium<S, true><<<gr, 256, 0, s>>>(g, rho, u, v, w, T, para_a, rho0, scale, (S*)f, (S*)gt);
+        k_equilibrium<S, true><<<gr, 256, 0, s>>>(g, rho, u, v, w, T, para_a, rho0, scale, (S*)f,
+                                                  (typename GType<S>::T*)gt);
     else
         k_equilibrium<S, false><<<gr, 256, 0, s>>>(g, rho, u, v, w, T, para_a, rho0, scale, (S*)f, nullptr);
     return cudaGetLastError();
@@ -350,6 +356,42 @@ cudaError_t launch_totals(long long n, const double* rho, const double* u, const
     int nb = reduce_blocks(n);
     k_totals<<<nb, RED_BLOCK, 0, s>>>(n, rho, u, v, w, T, partials);
     k_finish<3><<<1, 32, 0, s>>>(nb, partials, out3);
+    return cudaGetLastError();
+}
+
+// calNuRe (mpi_blocked/RaNu.F90:13-47) sums plus the wall-gradient sums of the
+// hot/cold wall Nusselt numbers.  The wall sits half a cell outside the first
+// node, so dT/dn|wall = (9 T_1 - T_2 - 8 T_wall)/3 (second order).
+__global__ void __launch_bounds__(RED_BLOCK)
+    k_thermal_stats(Geom g, const double* u, const double* v, const double* w, const double* T,
+                    int wall_axis, double* partials) {
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    const long long n = g.plane;
+    const long long sxy = (long long)g.nx * g.ny;
+    for (long long c = blockIdx.x * (long long)RED_BLOCK + threadIdx.x; c < n;
+         c += (long long)gridDim.x * RED_BLOCK) {
+        const double uu = u[c], vv = v[c], ww = w[c], t = T[c];
+        acc[0] += ww * t;
+        acc[1] += uu * uu + vv * vv + ww * ww;
+        if (wall_axis == 1) {
+            const int j = (int)((c / g.nx) % g.ny);
+            if (j == 0) acc[2] += 9.0 * t - T[c + g.nx];
+            if (j == g.ny - 1) acc[3] += 9.0 * t - T[c - g.nx];
+        } else if (wall_axis == 2) {
+            const long long k = c / sxy;
+            if (k == 0) acc[2] += 9.0 * t - T[c + sxy];
+            if (k == g.nz - 1) acc[3] += 9.0 * t - T[c - sxy];
+        }
+    }
+    block_sum<4>(acc, partials + 4 * blockIdx.x);
+}
+
+cudaError_t launch_thermal_stats(const Geom& g, const double* u, const double* v, const double* w,
+                                 const double* T, int wall_axis, double* partials, double* out4,
+                                 cudaStream_t s) {
+    int nb = reduce_blocks(g.plane);
+    k_thermal_stats<<<nb, RED_BLOCK, 0, s>>>(g, u, v, w, T, wall_axis, partials);
+    k_finish<4><<<1, 32, 0, s>>>(nb, partials, out4);
     return cudaGetLastError();
 }
 

@@ -55,96 +55,152 @@ struct St<__nv_bfloat16> {
     __device__ static void st(__nv_bfloat16* p, C v, float sc) { *p = __float2bfloat16_rn(v * sc); }
 };
 
+// Reciprocal of the density (rho is within a few percent of 1 in every
+// cavity flow).  FP32: the hardware reciprocal.  FP64: Newton-Raphson
+// refinement r <- r + r(1 - x r) of a single-precision seed; two steps take
+// the 2^-23 seed error below 2^-52 with four FP64 FMAs, about half the FP64
+// work of an IEEE division.
+__device__ __forceinline__ float recip(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double recip(double x) {
+    double r = (double)__frcp_rn((float)x);
+    double e = fma(-x, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-x, r, 1.0);
+    return fma(r, e, r);
+}
+
+// Scalar constants converted once on the host to the arithmetic type.
 template <typename C>
-__device__ __forceinline__ C recip(C x) {
-    return C(1) / x;
+struct StepK {
+    int nx, ny, nz;
+    C u0, rho0;
+    float scale, inv_scale;
+    MrtCoef<C> c;
+    // thermal
+    C gbeta, omega_rot, t_ref, para_a, qd, qnu, chot, ccold;
+    int bc_y, bc_z;
+};
+
+template <typename C>
+static StepK<C> make_k(const Geom& g, const MrtCoef<double>& cd, double u0, double rho0,
+                       float scale, float inv_scale) {
+    StepK<C> k{};
+    k.nx = g.nx; k.ny = g.ny; k.nz = g.nz;
+    k.u0 = (C)u0; k.rho0 = (C)rho0;
+    k.scale = scale; k.inv_scale = inv_scale;
+    k.c = cast_coef<C>(cd);
+    return k;
+}
+
+// Face mask of a cell: bit 0/1 = low/high x face, 2/3 = y, 4/5 = z.
+__device__ __forceinline__ unsigned face_mask(int i, int j, int k, int nx, int ny, int nz) {
+    return (unsigned)(i == 0) | ((unsigned)(i == nx - 1) << 1) | ((unsigned)(j == 0) << 2) |
+           ((unsigned)(j == ny - 1) << 3) | ((unsigned)(k == 0) << 4) |
+           ((unsigned)(k == nz - 1) << 5);
+}
+// does direction (dx,dy,dz) leave the domain from a cell with face mask m
+__host__ __device__ constexpr unsigned leave_bits(int dx, int dy, int dz) {
+    return (dx < 0 ? 1u : 0u) | (dx > 0 ? 2u : 0u) | (dy < 0 ? 4u : 0u) | (dy > 0 ? 8u : 0u) |
+           (dz < 0 ? 16u : 0u) | (dz > 0 ? 32u : 0u);
 }
 
 // ------------------------------------------------------------ lid kernel --
-template <typename S, bool FIRST>
-__global__ void __launch_bounds__(128) k_lid_step(const S* __restrict__ fin, S* __restrict__ fout,
-                                                  LidStepArgs a, MrtCoef<typename St<S>::C> c) {
+// IDX: 32-bit element indices when Q*cells < 2^31, 64-bit otherwise.
+template <typename S, bool FIRST, typename IDX>
+__global__ void __launch_bounds__(128)
+    k_lid_step(const S* __restrict__ fin, S* __restrict__ fout, StepK<typename St<S>::C> K,
+               IDX P, const double* __restrict__ mrho, const double* __restrict__ mu,
+               const double* __restrict__ mv, const double* __restrict__ mw) {
     using C = typename St<S>::C;
-    const int nx = a.g.nx, ny = a.g.ny, nz = a.g.nz;
+    const int nx = K.nx, ny = K.ny, nz = K.nz;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y, k = blockIdx.z;
     if (i >= nx) return;
-    const long long P = a.g.plane;
-    const long long cell = i + (long long)nx * (j + (long long)ny * k);
+    const IDX cell = (IDX)i + (IDX)nx * ((IDX)j + (IDX)ny * (IDX)k);
     C f[Q19];
 #pragma unroll
-    for (int q = 0; q < Q19; q++) f[q] = St<S>::ld(fin + q * P + cell, a.inv_scale);
+    for (int q = 0; q < Q19; q++) f[q] = St<S>::ld(fin + ((IDX)q * P + cell), K.inv_scale);
     C rho_m, rho, ux, uy, uz;
     if (FIRST) {
-        rho = (C)a.rho[cell];
-        ux = (C)a.u[cell];
-        uy = (C)a.v[cell];
-        uz = (C)a.w[cell];
-        rho_m = St<S>::SHIFT ? rho - (C)a.rho0 : rho;
+        rho = (C)mrho[cell];
+        ux = (C)mu[cell];
+        uy = (C)mv[cell];
+        uz = (C)mw[cell];
+        rho_m = St<S>::SHIFT ? rho - K.rho0 : rho;
     } else {
         C jx, jy, jz;
         moments0(f, rho_m, jx, jy, jz);
-        rho = St<S>::SHIFT ? (C)a.rho0 + rho_m : rho_m;
+        rho = St<S>::SHIFT ? K.rho0 + rho_m : rho_m;
         const C inv = recip(rho);
         ux = jx * inv;
         uy = jy * inv;
         uz = jz * inv;
     }
-    mrt_collide<C, false, true>(f, rho_m, rho, ux, uy, uz, C(0), C(0), C(0), c);
-    // moving lid: f(14) = f_post(11) - rho/6*U0, f(13) = f_post(12) + rho/6*U0 (bounce_back.f90:77-78)
+    mrt_collide<C, false, true>(f, rho_m, rho, ux, uy, uz, C(0), C(0), C(0), K.c);
+    const IDX sy = (IDX)nx, sz = (IDX)nx * (IDX)ny;
+    const unsigned bm = face_mask(i, j, k, nx, ny, nz);
+    if (bm == 0) {  // interior cell: every population streams
+#pragma unroll
+        for (int q = 0; q < Q19; q++) {
+            const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
+            St<S>::st(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), f[q],
+                      K.scale);
+        }
+        return;
+    }
+    // moving lid: f(14) = f_post(11) - rho/6*U0, f(13) = f_post(12) + rho/6*U0
+    // (bounce_back.f90:77-78); the lid face is written last, so it wins on edges
     C lid = C(0);
-    if (k == nz - 1) lid = rho / C(6) * (C)a.u0;
-    const long long sy = nx, sz = (long long)nx * ny;
+    if (k == nz - 1) lid = rho / C(6) * K.u0;
 #pragma unroll
     for (int q = 0; q < Q19; q++) {
         const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
-        bool in = true;
-        if (dx > 0) in = in && (i + 1 < nx);
-        if (dx < 0) in = in && (i > 0);
-        if (dy > 0) in = in && (j + 1 < ny);
-        if (dy < 0) in = in && (j > 0);
-        if (dz > 0) in = in && (k + 1 < nz);
-        if (dz < 0) in = in && (k > 0);
-        if (in) {
-            St<S>::st(fout + q * P + cell + dx + dy * sy + dz * sz, f[q], a.scale);
+        if ((bm & leave_bits(dx, dy, dz)) == 0) {
+            St<S>::st(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), f[q],
+                      K.scale);
         } else {
             C val = f[q];
-            if (dz > 0 && dx != 0) val = val - C(dx) * lid;  // lid face written last: wins on edges
-            St<S>::st(fout + opp19(q) * P + cell, val, a.scale);
+            if (dz > 0 && dx != 0) val = val - C(dx) * lid;
+            St<S>::st(fout + ((IDX)opp19(q) * P + cell), val, K.scale);
         }
     }
 }
 
 // -------------------------------------------------------- thermal kernel --
-template <typename S, bool FIRST, bool ROT>
+// Temperature populations are kept in the arithmetic type (FP64, or FP32 for
+// the reduced forms): g_0 ~ 0.7 T has a 16-bit ulp (~2e-4) far above the
+// per-step diffusive increments, so 16-bit g would stagnate.
+template <typename S, bool FIRST, bool ROT, typename IDX>
 __global__ void __launch_bounds__(128)
-    k_thermal_step(const S* __restrict__ fin, S* __restrict__ fout, const S* __restrict__ gin,
-                   S* __restrict__ gout, typename St<S>::C* __restrict__ F, ThermalStepArgs a,
-                   MrtCoef<typename St<S>::C> c) {
+    k_thermal_step(const S* __restrict__ fin, S* __restrict__ fout,
+                   const typename St<S>::C* __restrict__ gin, typename St<S>::C* __restrict__ gout,
+                   typename St<S>::C* __restrict__ F,
+                   StepK<typename St<S>::C> K, IDX P, const double* __restrict__ mrho,
+                   const double* __restrict__ mu, const double* __restrict__ mv,
+                   const double* __restrict__ mw, const double* __restrict__ mT) {
     using C = typename St<S>::C;
-    const int nx = a.g.nx, ny = a.g.ny, nz = a.g.nz;
+    const int nx = K.nx, ny = K.ny, nz = K.nz;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y, k = blockIdx.z;
     if (i >= nx) return;
-    const long long P = a.g.plane;
-    const long long cell = i + (long long)nx * (j + (long long)ny * k);
+    const IDX cell = (IDX)i + (IDX)nx * ((IDX)j + (IDX)ny * (IDX)k);
     C f[Q19], g[Q7];
 #pragma unroll
-    for (int q = 0; q < Q19; q++) f[q] = St<S>::ld(fin + q * P + cell, a.inv_scale);
+    for (int q = 0; q < Q19; q++) f[q] = St<S>::ld(fin + ((IDX)q * P + cell), K.inv_scale);
 #pragma unroll
-    for (int q = 0; q < Q7; q++) g[q] = St<S>::ld(gin + q * P + cell, 1.0f);
+    for (int q = 0; q < Q7; q++) g[q] = gin[(IDX)q * P + cell];
     C rho_m, rho, ux, uy, uz, temp;
     if (FIRST) {
-        rho = (C)a.rho[cell];
-        ux = (C)a.u[cell];
-        uy = (C)a.v[cell];
-        uz = (C)a.w[cell];
-        temp = (C)a.T[cell];
-        rho_m = St<S>::SHIFT ? rho - (C)a.rho0 : rho;
+        rho = (C)mrho[cell];
+        ux = (C)mu[cell];
+        uy = (C)mv[cell];
+        uz = (C)mw[cell];
+        temp = (C)mT[cell];
+        rho_m = St<S>::SHIFT ? rho - K.rho0 : rho;
     } else {
         C jx, jy, jz;
         moments0(f, rho_m, jx, jy, jz);
-        rho = St<S>::SHIFT ? (C)a.rho0 + rho_m : rho_m;
+        rho = St<S>::SHIFT ? K.rho0 + rho_m : rho_m;
         const C inv = recip(rho);
         // u^n = (sum f e + F^n/2)/rho^n with the force carried from the previous step
         C fxp = C(0), fyp = C(0);
@@ -152,7 +208,7 @@ __global__ void __launch_bounds__(128)
             fxp = F[cell];
             fyp = F[P + cell];
         }
-        const C fzp = F[2 * P + cell];
+        const C fzp = F[(IDX)2 * P + cell];
         ux = (jx + C(0.5) * fxp) * inv;
         uy = (jy + C(0.5) * fyp) * inv;
         uz = (jz + C(0.5) * fzp) * inv;
@@ -161,53 +217,53 @@ __global__ void __launch_bounds__(128)
     // body force from (rho,u,T) of the previous macro (bouyancy3d_mpi.F90:743-745)
     C fx = C(0), fy = C(0);
     if (ROT) {
-        fx = C(-2) * rho * uy * (C)a.omega_rot;
-        fy = C(2) * rho * ux * (C)a.omega_rot;
+        fx = C(-2) * rho * uy * K.omega_rot;
+        fy = C(2) * rho * ux * K.omega_rot;
         F[cell] = fx;
         F[P + cell] = fy;
     }
-    const C fz = rho * (C)a.gbeta * (temp - (C)a.t_ref);
-    F[2 * P + cell] = fz;
-    mrt_collide<C, true, false>(f, rho_m, rho, ux, uy, uz, fx, fy, fz, c);
-    mrt_collide_t<C>(g, temp, ux, uy, uz, (C)a.para_a, (C)a.qd, (C)a.qnu);
+    const C fz = rho * K.gbeta * (temp - K.t_ref);
+    F[(IDX)2 * P + cell] = fz;
+    mrt_collide<C, true, false>(f, rho_m, rho, ux, uy, uz, fx, fy, fz, K.c);
+    mrt_collide_t<C>(g, temp, ux, uy, uz, K.para_a, K.qd, K.qnu);
 
-    const long long sy = nx, sz = (long long)nx * ny;
+    const IDX sy = (IDX)nx, sz = (IDX)nx * (IDX)ny;
+    const unsigned bm = face_mask(i, j, k, nx, ny, nz);
+    if (bm == 0) {
+#pragma unroll
+        for (int q = 0; q < Q19; q++) {
+            const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
+            St<S>::st(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), f[q],
+                      K.scale);
+        }
+#pragma unroll
+        for (int q = 0; q < Q7; q++) {
+            const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
+            gout[(IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz] = g[q];
+        }
+        return;
+    }
 #pragma unroll
     for (int q = 0; q < Q19; q++) {
         const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
-        bool in = true;
-        if (dx > 0) in = in && (i + 1 < nx);
-        if (dx < 0) in = in && (i > 0);
-        if (dy > 0) in = in && (j + 1 < ny);
-        if (dy < 0) in = in && (j > 0);
-        if (dz > 0) in = in && (k + 1 < nz);
-        if (dz < 0) in = in && (k > 0);
-        if (in)
-            St<S>::st(fout + q * P + cell + dx + dy * sy + dz * sz, f[q], a.scale);
+        if ((bm & leave_bits(dx, dy, dz)) == 0)
+            St<S>::st(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), f[q],
+                      K.scale);
         else
-            St<S>::st(fout + opp19(q) * P + cell, f[q], a.scale);
+            St<S>::st(fout + ((IDX)opp19(q) * P + cell), f[q], K.scale);
     }
     // D3Q7: adiabatic walls reflect, constant-T walls anti-bounce-back
     // g_in = -g_out + (6+paraA)/21 * T_wall (bouyancy3d_mpi.F90:1101-1210)
-    const C chot = (C)((6.0 + a.para_a) / 21.0 * a.t_hot);
-    const C ccold = (C)((6.0 + a.para_a) / 21.0 * a.t_cold);
 #pragma unroll
     for (int q = 0; q < Q7; q++) {
         const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
-        bool in = true;
-        if (dx > 0) in = in && (i + 1 < nx);
-        if (dx < 0) in = in && (i > 0);
-        if (dy > 0) in = in && (j + 1 < ny);
-        if (dy < 0) in = in && (j > 0);
-        if (dz > 0) in = in && (k + 1 < nz);
-        if (dz < 0) in = in && (k > 0);
-        if (in) {
-            St<S>::st(gout + q * P + cell + dx + dy * sy + dz * sz, g[q], 1.0f);
+        if ((bm & leave_bits(dx, dy, dz)) == 0) {
+            gout[(IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz] = g[q];
         } else {
             C val = g[q];
-            if (dy != 0 && a.bc_y) val = -val + (dy < 0 ? chot : ccold);
-            if (dz != 0 && a.bc_z) val = -val + (dz < 0 ? chot : ccold);
-            St<S>::st(gout + opp19(q) * P + cell, val, 1.0f);
+            if (dy != 0 && K.bc_y) val = -val + (dy < 0 ? K.chot : K.ccold);
+            if (dz != 0 && K.bc_z) val = -val + (dz < 0 ? K.chot : K.ccold);
+            gout[(IDX)opp19(q) * P + cell] = val;
         }
     }
 }
@@ -226,12 +282,18 @@ template <typename S>
 static cudaError_t lid_go(bool first, const void* fin, void* fout, const LidStepArgs& a,
                           cudaStream_t s) {
     using C = typename St<S>::C;
-    MrtCoef<C> c = cast_coef<C>(a.cd);
+    StepK<C> K = make_k<C>(a.g, a.cd, a.u0, a.rho0, a.scale, a.inv_scale);
     dim3 b = step_block(a.g.nx), gr = step_grid(a.g, b);
-    if (first)
-        k_lid_step<S, true><<<gr, b, 0, s>>>((const S*)fin, (S*)fout, a, c);
-    else
-        k_lid_step<S, false><<<gr, b, 0, s>>>((const S*)fin, (S*)fout, a, c);
+    const bool small = (long long)Q19 * a.g.plane < (1ll << 31);
+#define LID_LAUNCH(FI, IT)                                                                    \
+    k_lid_step<S, FI, IT><<<gr, b, 0, s>>>((const S*)fin, (S*)fout, K, (IT)a.g.plane, a.rho, a.u, \
+                                           a.v, a.w)
+    if (small) {
+        if (first) LID_LAUNCH(true, unsigned); else LID_LAUNCH(false, unsigned);
+    } else {
+        if (first) LID_LAUNCH(true, long long); else LID_LAUNCH(false, long long);
+    }
+#undef LID_LAUNCH
     return cudaGetLastError();
 }
 
@@ -250,16 +312,30 @@ template <typename S>
 static cudaError_t th_go(bool first, const void* fin, void* fout, const void* gin, void* gout,
                          void* F, const ThermalStepArgs& a, cudaStream_t s) {
     using C = typename St<S>::C;
-    MrtCoef<C> c = cast_coef<C>(a.cd);
+    StepK<C> K = make_k<C>(a.g, a.cd, 0.0, a.rho0, a.scale, a.inv_scale);
+    K.gbeta = (C)a.gbeta; K.omega_rot = (C)a.omega_rot; K.t_ref = (C)a.t_ref;
+    K.para_a = (C)a.para_a; K.qd = (C)a.qd; K.qnu = (C)a.qnu;
+    K.chot = (C)((6.0 + a.para_a) / 21.0 * a.t_hot);
+    K.ccold = (C)((6.0 + a.para_a) / 21.0 * a.t_cold);
+    K.bc_y = a.bc_y; K.bc_z = a.bc_z;
     dim3 b = step_block(a.g.nx), gr = step_grid(a.g, b);
     const bool rot = a.omega_rot != 0.0;
-#define TH_LAUNCH(FI, RO)                                                                   \
-    k_thermal_step<S, FI, RO><<<gr, b, 0, s>>>((const S*)fin, (S*)fout, (const S*)gin, (S*)gout, \
-                                               (C*)F, a, c)
-    if (first && rot) TH_LAUNCH(true, true);
-    else if (first) TH_LAUNCH(true, false);
-    else if (rot) TH_LAUNCH(false, true);
-    else TH_LAUNCH(false, false);
+    const bool small = (long long)Q19 * a.g.plane < (1ll << 31);
+#define TH_LAUNCH(FI, RO, IT)                                                                  \
+    k_thermal_step<S, FI, RO, IT><<<gr, b, 0, s>>>((const S*)fin, (S*)fout, (const C*)gin,     \
+                                                   (C*)gout, (C*)F, K, (IT)a.g.plane, a.rho,  \
+                                                   a.u, a.v, a.w, a.T)
+#define TH_ROT(IT)                                       \
+    if (first && rot) TH_LAUNCH(true, true, IT);          \
+    else if (first) TH_LAUNCH(true, false, IT);           \
+    else if (rot) TH_LAUNCH(false, true, IT);             \
+    else TH_LAUNCH(false, false, IT);
+    if (small) {
+        TH_ROT(unsigned)
+    } else {
+        TH_ROT(long long)
+    }
+#undef TH_ROT
 #undef TH_LAUNCH
     return cudaGetLastError();
 }

@@ -79,4 +79,11 @@ cudaError_t launch_totals(long long n, const double* rho, const double* u, const
                           const double* w, const double* T, double* partials, double* out3,
                           cudaStream_t s);
 
+// thermal statistics: out[0] = sum w*T, out[1] = sum |u|^2,
+// out[2] = sum over the low const-T wall of (9 T_1 - T_2), out[3] = the same at
+// the high wall (9 T_n - T_{n-1}); wall_axis 1 = y, 2 = z, 0 = none
+cudaError_t launch_thermal_stats(const Geom& g, const double* u, const double* v, const double* w,
+                                 const double* T, int wall_axis, double* partials, double* out4,
+                                 cudaStream_t s);
+
 }  // namespace mglc

@@ -96,3 +96,30 @@ def test_macro_of_identical_state_is_bit_exact(mg):
     # load_state without macros derives them with F = 0; rho and T do not depend on F
     assert np.array_equal(T, o.T)
     assert np.array_equal(rho, o.rho)
+
+
+def _nu_numpy(o, axis_y=True):
+    """calNuRe (RaNu.F90:13-47) and the wall Nusselt numbers from oracle fields."""
+    nz, ny, nx = o.T.shape
+    n = nx * ny * nz
+    nu_vol = (o.w * o.T).sum() / n * nz / o.c.diffusivity + 1.0
+    re_vol = np.sqrt((o.u ** 2 + o.v ** 2 + o.w ** 2).sum() / n) * nz / o.c.viscosity
+    dT = o.t_hot - o.t_cold
+    T = o.T
+    g_hot = (9 * T[:, 0, :] - T[:, 1, :] - 8 * o.t_hot).mean() / 3
+    g_cold = (9 * T[:, -1, :] - T[:, -2, :] - 8 * o.t_cold).mean() / 3
+    return nu_vol, re_vol, -ny / dT * g_hot, ny / dT * g_cold
+
+
+def test_nusselt_matches_oracle_fields(mg):
+    n, steps = 20, 400
+    o = O.ThermalOracle(n, n, n, 1e5, 0.71, 0.1, 0.0, 0.5, -0.5, 0.0)
+    o.run(steps, nthreads=NT)
+    ref = _nu_numpy(o)
+    with mg.BuoyancyCavity(n, rayleigh=1e5, t_hot=0.5, t_cold=-0.5) as c:
+        c.initial()
+        c.step(steps)
+        got = c.nusselt()
+    np.testing.assert_allclose(got, ref, rtol=1e-9)
+    # heat enters at the hot wall and leaves at the cold wall
+    assert got[2] > 1.0 and got[3] > 1.0
