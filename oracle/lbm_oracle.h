@@ -88,6 +88,29 @@ void orc_th_run(int nx, int ny, int nz, const orc_th_consts* c, double t_ref,
                 double* rho, double* u, double* v, double* w, double* T,
                 double* Fx, double* Fy, double* Fz);
 
+/* ---- moving particles (MPI/Micro_particles/fortran/case4/mpi_particle) ---- */
+typedef struct {
+    int dim;        /* 2: literal D2Q9 case4; 3: D3Q19 spheres */
+    int nx, ny, nz; /* nz = 1 in 2-D */
+    int periodic_x; /* 3-D channel */
+    int np;
+    double tauf, rho0, rho_solid, radius;
+    double gravity[3];    /* acceleration on the particles; 2-D reference: (0,-g,0) */
+    double body_force[3]; /* fluid body-force acceleration (3-D, MRT source) */
+    double threshold_wall, stiff_wall, threshold_particle, stiff_particle;
+    double spring_scale_wall, spring_scale_particle; /* 3-D spring scales */
+    int qmode; /* 0: bisection calQ (reference), 1: analytic calQ2 */
+} orc_pp;
+typedef struct orc_particles orc_particles;
+orc_particles* orc_pt_create(const orc_pp* p, const double* centers /* np*3 */);
+/* returns 0, or 1 no owning particle, 2 q out of range, 3 particle overlap,
+ * 4 wall penetration, 5 no refill direction */
+int orc_pt_step(orc_particles* s, int nsteps);
+void orc_pt_get(const orc_particles* s, double* f, double* f_post, double* rho, double* u,
+                double* v, double* w, int* obst, double* xc, double* uc, double* om,
+                double* force, double* torque, double* rho_avg);
+void orc_pt_destroy(orc_particles* s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -26,11 +26,13 @@ LIB = os.path.join(BUILD, "liboracle.so")
 
 def build(force: bool = False) -> str:
     """Compile the oracle with gcc (-O2 -ffp-contract=off, OpenMP for the timed baseline)."""
-    src = os.path.join(HERE, "lbm_oracle.c")
+    srcs = [os.path.join(HERE, f) for f in ("lbm_oracle.c", "particle_oracle.c")]
+    hdr = os.path.join(HERE, "lbm_oracle.h")
     os.makedirs(BUILD, exist_ok=True)
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
+    newest = max(os.path.getmtime(x) for x in srcs + [hdr])
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
         cmd = ["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC",
-               "-shared", "-o", LIB, src, "-lm"]
+               "-shared", "-o", LIB, *srcs, "-lm"]
         subprocess.check_call(cmd)
     return LIB
 
@@ -74,6 +76,21 @@ def _declare(L):
     L.orc_th_initial.argtypes = [_I, _I, _I, TP, _D, _D, _I, _I] + [_P] * 7
     L.orc_th_check.argtypes = [_I, _I, _I] + [_P] * 8 + [_P, _P]
     L.orc_th_run.argtypes = [_I, _I, _I, TP, _D, _D, _D, _I, _I, _I, _I] + [_P] * 12
+    L.orc_pt_create.argtypes = [ctypes.POINTER(ParticleParams), _P]
+    L.orc_pt_create.restype = ctypes.c_void_p
+    L.orc_pt_step.argtypes = [ctypes.c_void_p, _I]
+    L.orc_pt_step.restype = _I
+    _IP = ctypes.POINTER(ctypes.c_int)
+    L.orc_pt_get.argtypes = [ctypes.c_void_p, _P, _P, _P, _P, _P, _P, _IP, _P, _P, _P, _P, _P, _P]
+    L.orc_pt_destroy.argtypes = [ctypes.c_void_p]
+
+
+class ParticleParams(ctypes.Structure):
+    _fields_ = [("dim", _I), ("nx", _I), ("ny", _I), ("nz", _I), ("periodic_x", _I), ("np", _I),
+                ("tauf", _D), ("rho0", _D), ("rho_solid", _D), ("radius", _D),
+                ("gravity", _D * 3), ("body_force", _D * 3), ("threshold_wall", _D),
+                ("stiff_wall", _D), ("threshold_particle", _D), ("stiff_particle", _D),
+                ("spring_scale_wall", _D), ("spring_scale_particle", _D), ("qmode", _I)]
 
 
 def _p(a: np.ndarray):
@@ -175,3 +192,55 @@ class ThermalOracle:
                            _p(self.T), _p(self.up), _p(self.vp), _p(self.wp), _p(self.Tp),
                            ctypes.byref(eu), ctypes.byref(et))
         return eu.value, et.value
+
+
+class ParticleOracle:
+    """Moving particles: dim=2 is the literal case4 D2Q9 restatement, dim=3
+    the D3Q19 sphere generalisation."""
+
+    def __init__(self, centers, **kw):
+        centers = np.ascontiguousarray(np.asarray(centers, dtype=np.float64).reshape(-1, 3))
+        p = ParticleParams()
+        defaults = dict(dim=3, nx=16, ny=16, nz=16, periodic_x=0, np=len(centers), tauf=0.65,
+                        rho0=1.0, rho_solid=1.2, radius=3.0, gravity=(0.0, 0.0, 0.0),
+                        body_force=(0.0, 0.0, 0.0), threshold_wall=6.0, stiff_wall=0.02,
+                        threshold_particle=6.0, stiff_particle=0.08, spring_scale_wall=0.0,
+                        spring_scale_particle=0.0, qmode=0)
+        defaults.update(kw)
+        defaults["np"] = len(centers)
+        for k, v in defaults.items():
+            if k in ("gravity", "body_force"):
+                getattr(p, k)[:] = list(v)
+            else:
+                setattr(p, k, v)
+        self.p = p
+        self.Q = 9 if p.dim == 2 else 19
+        self._s = lib().orc_pt_create(ctypes.byref(p), _p(centers))
+
+    def step(self, n=1) -> int:
+        return lib().orc_pt_step(self._s, n)
+
+    def get(self):
+        p = self.p
+        nz = p.nz if p.dim == 3 else 1
+        shp = (nz, p.ny, p.nx)
+        out = {k: np.zeros(shp) for k in ("rho", "u", "v", "w")}
+        out["f"] = np.zeros(shp + (self.Q,))
+        out["f_post"] = np.zeros(shp + (self.Q,))
+        out["obst"] = np.zeros(shp, dtype=np.int32)
+        for k in ("xc", "uc", "om", "force", "torque"):
+            out[k] = np.zeros((p.np, 3))
+        ra = ctypes.c_double()
+        lib().orc_pt_get(self._s, _p(out["f"]), _p(out["f_post"]), _p(out["rho"]), _p(out["u"]),
+                         _p(out["v"]), _p(out["w"]),
+                         out["obst"].ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _p(out["xc"]),
+                         _p(out["uc"]), _p(out["om"]), _p(out["force"]), _p(out["torque"]),
+                         ctypes.byref(ra))
+        out["rho_avg"] = ra.value
+        return out
+
+    def __del__(self):
+        try:
+            lib().orc_pt_destroy(self._s)
+        except Exception:
+            pass

@@ -71,6 +71,10 @@ def _fint(x):
     return int(x)  # truncation toward zero
 
 
+def _sq(x):
+    return x * x
+
+
 def _nint(x):
     return int(math.floor(x + 0.5)) if x >= 0 else -int(math.floor(-x + 0.5))
 
@@ -172,7 +176,10 @@ def split_top(s: str, sep=","):
 class Program:
     def __init__(self, defines=None):
         self.ns = {"math": math, "np": np, "FArr": FArr, "_r4": _r4, "_fmod": _fmod,
-                   "_fint": _fint, "_nint": _nint}
+                   "_fint": _fint, "_nint": _nint, "_sq": _sq}
+        self.random_values: list[float] = []  # values returned by random_number, in order
+        self.ns["_rand"] = lambda: float(self.random_values.pop(0))
+        self.sub_args: dict[str, list[str]] = {}
         self.defines = set(defines or ())
         self.arrays: set[str] = set()
         self.int_arrays: set[str] = set()
@@ -181,8 +188,39 @@ class Program:
         self.overrides: dict[str, object] = {}
 
     # ---------------- expression translation ----------------
+    @staticmethod
+    def _squares(e: str) -> str:
+        """Rewrite OPERAND**2.0d0 (or **2) as _sq(OPERAND): the square as a product."""
+        pat = re.compile(r"\*\*\s*2(\.0*)?(d0)?(?![\w.])", re.I)
+        while True:
+            m = pat.search(e)
+            if not m:
+                return e
+            k = m.start() - 1
+            while k >= 0 and e[k] == " ":
+                k -= 1
+            end = k + 1
+            if e[k] == ")":
+                depth = 0
+                while k >= 0:
+                    if e[k] == ")":
+                        depth += 1
+                    elif e[k] == "(":
+                        depth -= 1
+                        if depth == 0:
+                            break
+                    k -= 1
+                k -= 1
+                while k >= 0 and (e[k].isalnum() or e[k] == "_"):
+                    k -= 1
+            else:
+                while k >= 0 and (e[k].isalnum() or e[k] in "_."):
+                    k -= 1
+            start = k + 1
+            e = e[:start] + "_sq(" + e[start:end] + ")" + e[m.end():]
+
     def expr(self, e: str, local_arrays=frozenset()) -> str:
-        e = e.strip()
+        e = self._squares(e.strip())
         # array constructor (/ ... /)
         if e.startswith("(/") and e.endswith("/)"):
             return self._constructor(e[2:-2], local_arrays)
@@ -224,7 +262,7 @@ class Program:
             m = re.match(r"([a-z_]\w*)\s*\(", e[i:])
             if m and (i == 0 or not (e[i - 1].isalnum() or e[i - 1] == "_")):
                 n = m.group(1)
-                if n in ("and", "or", "not", "_r4"):
+                if n in ("and", "or", "not", "_r4", "_sq", "_rand"):
                     out.append(e[i:i + m.end()])
                     i += m.end()
                     continue
@@ -349,7 +387,9 @@ class Program:
                     elif n not in self.ns:
                         self.ns[n] = 0 if is_int else float("nan")
             else:
-                if dims:
+                if dims and dims.replace(",", "").replace(":", "").strip() == "":
+                    local_arrays.add(n)  # deferred shape: created by allocate
+                elif dims:
                     local_arrays.add(n)
                     code.append(f"{indent}{n} = FArr({self._bounds_src(dims)}, "
                                 f"{'np.int64' if is_int else 'np.float64'})")
@@ -359,6 +399,10 @@ class Program:
                     self._local_scalars.add(n)
                     if init is not None:
                         code.append(f"{indent}{n} = {self.expr(init)}")
+                    elif n not in getattr(self, "_dummies", []):
+                        # Fortran leaves locals undefined; bind them so that they can be
+                        # passed as output arguments (NaN exposes any read before write)
+                        code.append(f"{indent}{n} = {'0' if is_int else 'float(\'nan\')'}")
 
     def _bounds_src(self, dims):
         out = []
@@ -375,6 +419,7 @@ class Program:
             m = re.match(r"^subroutine\s+(\w+)\s*(\((.*)\))?", sl)
             if m and cur is None:
                 cur, body = m.group(1), []
+                self.sub_args[cur] = [a.strip() for a in m.group(3).split(",")] if m.group(3) and m.group(3).strip() else []
                 continue
             if cur and re.match(r"^end\s*subroutine", sl):
                 self.subs[cur] = body
@@ -385,6 +430,7 @@ class Program:
 
     def compile(self, name: str):
         body = self.subs[name]
+        self._dummies = self.sub_args.get(name, [])
         local_arrays: set[str] = set()
         self._local_scalars: set[str] = set()
         code: list[str] = []
@@ -403,7 +449,7 @@ class Program:
                 code.append(f"{ind}pass")
                 continue
             if sl == "return":
-                code.append(f"{ind}return")
+                code.append(f"{ind}return {self._ret()}")
                 continue
             if sl == "stop" or sl.startswith("stop "):
                 code.append(f"{ind}raise RuntimeError('reference STOP')")
@@ -462,13 +508,17 @@ class Program:
             if re.match(r"^deallocate\s*\(", sl):
                 continue
             code.extend(self._simple(st, ind, local_arrays, assigned))
-        glob = sorted((assigned & self.scalars) - self._local_scalars)
-        src = [f"def {name}():"]
+        glob = sorted((assigned & self.scalars) - self._local_scalars - set(self._dummies))
+        src = [f"def {name}({', '.join(self._dummies)}):"]
         if glob:
             src.append("    global " + ", ".join(glob))
         src.append("    pass")
         src.extend(code)
+        src.append(f"    return {self._ret()}")
         return "\n".join(src)
+
+    def _ret(self):
+        return "(" + "".join(d + ", " for d in self._dummies) + ")" if self._dummies else "None"
 
     def _split_cond(self, s):
         depth = 0
@@ -487,6 +537,14 @@ class Program:
             m = re.match(r"^call\s+(\w+)\s*(\((.*)\))?$", st.strip(), re.I)
             n = m.group(1).lower()
             args = split_top(m.group(3)) if m.group(3) else []
+            if n == "random_number":
+                tgt = args[0].strip().lower()
+                return [f"{ind}{self.expr(args[0], local_arrays) if '(' in tgt else tgt} = _rand()"]
+            if n == "random_seed":
+                outs = [a.split("=")[1].strip().lower() for a in args if a.lower().startswith("size")]
+                return [f"{ind}{o} = 1" for o in outs] or [f"{ind}pass"]
+            if n == "mpi_abort":
+                return [f"{ind}raise RuntimeError('reference MPI_Abort')"]
             if n == "mpi_allreduce":
                 src, dst = self.expr(args[0], local_arrays), args[1].strip().lower()
                 assigned.add(dst)
@@ -496,9 +554,25 @@ class Program:
             if n.startswith("mpi_") or n.startswith("omp_"):
                 return [f"{ind}pass"]
             if n in self.subs:
-                if args:
-                    raise ValueError("subroutine arguments are not supported: " + st)
-                return [f"{ind}{n}()"]
+                if not args:
+                    return [f"{ind}{n}()"]
+                # by-reference: plain names and array elements receive the dummies' final values
+                out = [f"{ind}_r = {n}({', '.join(self.expr(a, local_arrays) for a in args)})"]
+                for k, a in enumerate(args):
+                    a = a.strip()
+                    mm = re.match(r"^(\w+)\s*(\((.*)\))?$", a)
+                    if not mm:
+                        continue
+                    nm = mm.group(1).lower()
+                    if nm in INTRINSICS and nm not in self.arrays and nm not in local_arrays:
+                        continue
+                    if mm.group(2):
+                        if nm in self.arrays or nm in local_arrays:
+                            out.append(f"{ind}{self.expr(a, local_arrays)} = _r[{k}]")
+                    elif not re.match(r"^\d", nm):
+                        out.append(f"{ind}{nm} = _r[{k}]")
+                        assigned.add(nm)
+                return out
             return [f"{ind}pass  # skipped call {n}"]
         if re.match(r"^(write|print)\b", sl):
             return [f"{ind}pass"]

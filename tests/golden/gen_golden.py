@@ -28,6 +28,7 @@ sys.path.insert(0, HERE)
 from fortran_exec import FArr, Program, preprocess  # noqa: E402
 
 LID_DIR = "MPI/Lid_driven_cavity/fortran/3d/mpi_3d_blocked"
+PART_DIR = "MPI/Micro_particles/fortran/case4/mpi_particle"
 THERMAL_FILE = "MPI/Buoyancy_driven_cavity/fortran/3d/bouyancy3d_mpi.F90"
 
 
@@ -136,7 +137,62 @@ def thermal_case(ref, nx, ny, nz, rayleigh, prandtl, mach, ekman, thot, tcold, t
     return out
 
 
+def particle2d_case(ref, nx, ny, radius0, gravity, rnd, nsteps):
+    """case4 (D2Q9 moving circles) on one rank, main.F90:35-73 order.
+
+    The particle centres come from initial.F90:59-72 with random_number
+    returning the values in ``rnd`` (the reference seeds gfortran's generator,
+    which is not reproducible here)."""
+    p = Program()
+    p.overrides = {"total_nx": nx, "total_ny": ny, "cnummax": 2, "radius0": float(radius0),
+                   "gravity": float(gravity), "rank": 0, "num_process": 1, "comm2d": 0,
+                   "dims": FArr([(0, 1)], np.int64, 1), "coords": FArr([(0, 1)], np.int64, 0),
+                   "periods": FArr([(0, 1)], np.int64, 0)}
+    mod = preprocess(open(os.path.join(ref, PART_DIR, "commondata.F90")).read(), p.defines)
+    p.load_module(mod)
+    p.ns.update({"nx": nx, "ny": ny, "i_start_global": 0, "j_start_global": 0})
+    for fn in ("freeall.F90", "initial.F90", "fluid.F90", "particle_bounceback.F90",
+               "particle_force.F90", "particle_update.F90", "message_particle.F90"):
+        p.load_subroutines(preprocess(open(os.path.join(ref, PART_DIR, fn)).read(), p.defines))
+    names = ["allocate_all", "initial", "collision", "streaming", "bounceback",
+             "bounceback_particle", "calq", "macro", "calforce", "updatecenter",
+             "update_particle_mask"]
+    p.build(names)
+    p.random_values = list(rnd)
+    p.call("allocate_all")
+    p.call("initial")
+    ns = p.ns
+    interior = lambda a, lo: a.numpy()[(slice(1 - lo[1], 1 - lo[1] + ny), slice(1 - lo[0], 1 - lo[0] + nx))]
+    out = {"nx": nx, "ny": ny, "radius0": float(radius0), "gravity": float(gravity),
+           "nsteps": nsteps, "tauf": ns["tauf"], "rhosolid": ns["rhosolid"],
+           "xc0": np.stack([ns["xcenter"].numpy(), ns["ycenter"].numpy()], axis=1)}
+    for itc in range(nsteps):
+        p.call("collision")
+        p.call("streaming")
+        p.call("bounceback")
+        p.call("bounceback_particle")
+        p.call("macro")
+        p.call("calforce")
+        ns["itc"] = ns["itc"] + 1
+        p.call("updatecenter")
+    f = ns["f"].numpy()            # (ny+6, nx+6, 9) with lower bound -2
+    fp = ns["f_post"].numpy()      # (ny+4, nx+4, 9) with lower bound -1
+    out.update(f=f[3:3 + ny, 3:3 + nx, :], f_post=fp[2:2 + ny, 2:2 + nx, :],
+               rho=ns["rho"].numpy(), u=ns["u"].numpy(), v=ns["v"].numpy(),
+               obst=ns["obst"].numpy()[1:1 + ny, 1:1 + nx],
+               xc=np.stack([ns["xcenter"].numpy(), ns["ycenter"].numpy()], axis=1),
+               uc=np.stack([ns["uc"].numpy(), ns["vc"].numpy()], axis=1),
+               omega=ns["rationalomega"].numpy(),
+               force=np.stack([ns["walltotalforcex"].numpy(), ns["walltotalforcey"].numpy()], axis=1),
+               torque=ns["totaltorque"].numpy(), rho_avg=ns["rhoavg"])
+    assert not np.isnan(out["f"]).any()
+    return out
+
+
 CASES = {
+    # case4 moving circles: two particles settling, mask updates and refills
+    "particle2d_80x50": lambda ref: particle2d_case(ref, 80, 50, 6.0, 0.04,
+                                                    [0.513, 0.47, 0.421, 0.552], nsteps=30),
     # lid: non-cubic grid to catch axis mix-ups; Re chosen for tau ~ 0.6
     "lid_7x6x5": lambda ref: lid_case(ref, 7, 6, 5, reynolds=21.0, nsteps=12, check_every=4),
     "lid_6x6x6_re400": lambda ref: lid_case(ref, 6, 6, 6, reynolds=400.0, nsteps=6,
