@@ -73,6 +73,22 @@ typedef struct mglc_thermal_params {
     int precision;
 } mglc_thermal_params;
 
+/* Moving spheres in a D3Q19 flow: the 3-D generalisation of
+ * MPI/Micro_particles/fortran/case4/mpi_particle (commondata.F90:26-60).
+ * x is periodic or walled; y and z are no-slip walls. */
+typedef struct mglc_particle_params {
+    int total_nx, total_ny, total_nz;
+    int periodic_x;            /* 1: periodic in x (channel); 0: walls on the x faces */
+    double tauf;               /* relaxation time, 3*viscosity + 0.5 (commondata.F90:33) */
+    double rho0, rho_solid;    /* fluid reference density, particle density */
+    double radius;             /* sphere radius (lattice units) */
+    double gravity[3];         /* acceleration on the particles: (rho_s - rho_avg) V g */
+    double body_force[3];      /* fluid body-force acceleration; rho_avg V a acts on particles */
+    double threshold_wall, threshold_particle;       /* spring ranges (particle_force.F90:100-178) */
+    double spring_scale_wall, spring_scale_particle; /* spring force scales */
+    int precision;             /* MGLC_FP64 or MGLC_FP32 (FP32: deviation storage, FP32 arithmetic) */
+} mglc_particle_params;
+
 /* Derived constants of a context (for logging and tests). */
 typedef struct mglc_info {
     int kind, precision;
@@ -89,6 +105,10 @@ typedef struct mglc_info {
 int mglc_lid_create(const mglc_lid_params* p, mglc_ctx** out);
 /* Replaces the allocation part of bouyancy3d_mpi.F90:476-496 (thermal). */
 int mglc_thermal_create(const mglc_thermal_params* p, mglc_ctx** out);
+/* Replaces allocate_all + the placement part of initial.F90:48-116 (particles);
+ * centers = np x (x,y,z) in node coordinates (node i sits at x = i, 1-based). */
+int mglc_particle_create(const mglc_particle_params* p, const double* centers, int np,
+                         mglc_ctx** out);
 void mglc_destroy(mglc_ctx* ctx);
 const char* mglc_last_error(const mglc_ctx* ctx);
 /* Bind the context to a caller-owned cudaStream_t (NULL = the context's own stream). */
@@ -111,7 +131,10 @@ int mglc_get_f(mglc_ctx* ctx, double* f, double* g);
 /* nsteps fused time steps.  Lid: collision + streaming + bounceback + macro
  * (main.f90:89-97).  Thermal: collision, streaming, bounceback, collisionT,
  * streamingT, bouncebackT, macro, macroT (bouyancy3d_mpi.F90:226-244).
- * Asynchronous on the context's stream. */
+ * Particles: collision, streaming, bounceback, bounceback_particle, macro,
+ * calForce, updateCenter (case4 main.F90:37-71).  Asynchronous on the
+ * context's stream, except for particle contexts, which synchronise at the
+ * end to report MGLC_ERR_PARTICLE (overlap, wall penetration). */
 int mglc_step(mglc_ctx* ctx, int nsteps);
 
 /* macro() / macroT() output: rho,u,v,w (and T) of the current state, host
@@ -124,6 +147,15 @@ int mglc_check(mglc_ctx* ctx, double* error_u, double* error_t);
 /* Conserved totals in FP64: mass = sum rho, energy = sum rho|u|^2/2,
  * heat = sum T (thermal, else 0).  Any pointer may be NULL. */
 int mglc_totals(mglc_ctx* ctx, double* mass, double* energy, double* heat);
+
+/* Particle centres, velocities, angular velocities, and the total force and
+ * torque of the last step (particle_force.F90:184-190), each np x 3 doubles.
+ * Any pointer may be NULL.  Synchronises. */
+int mglc_particle_state(mglc_ctx* ctx, double* xc, double* uc, double* omega, double* force,
+                        double* torque);
+/* Owner of every node: -1 fluid, p >= 0 inside particle p (the reference's
+ * obst, particle_update.F90:80-93, with the particle index).  Synchronises. */
+int mglc_get_mask(mglc_ctx* ctx, int* owner);
 
 /* Thermal statistics of the current state.  nu_vol and re_vol restate the
  * reference's calNuRe (mpi_blocked/RaNu.F90:13-47): Nu = <w T> nz/kappa + 1,

@@ -5,6 +5,6 @@ kernels for sm_103a under csrc/).  This package builds it and offers a thin
 Python host API that mirrors the reference's routines.
 """
 from .capi import FORMS, MglcError, lib  # noqa: F401
-from .cavity import BuoyancyCavity, LidDrivenCavity  # noqa: F401
+from .cavity import BuoyancyCavity, LidDrivenCavity, ParticleFlow  # noqa: F401
 
-__all__ = ["LidDrivenCavity", "BuoyancyCavity", "MglcError", "FORMS", "lib"]
+__all__ = ["LidDrivenCavity", "BuoyancyCavity", "ParticleFlow", "MglcError", "FORMS", "lib"]

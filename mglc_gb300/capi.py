@@ -34,6 +34,14 @@ class ThermalParams(ctypes.Structure):
                 ("ekman", _D), ("bc_y_const_t", _I), ("bc_z_const_t", _I), ("precision", _I)]
 
 
+class ParticleParams(ctypes.Structure):
+    _fields_ = [("total_nx", _I), ("total_ny", _I), ("total_nz", _I), ("periodic_x", _I),
+                ("tauf", _D), ("rho0", _D), ("rho_solid", _D), ("radius", _D),
+                ("gravity", _D * 3), ("body_force", _D * 3), ("threshold_wall", _D),
+                ("threshold_particle", _D), ("spring_scale_wall", _D),
+                ("spring_scale_particle", _D), ("precision", _I)]
+
+
 class Info(ctypes.Structure):
     _fields_ = [("kind", _I), ("precision", _I), ("nx", _I), ("ny", _I), ("nz", _I),
                 ("itc", _LL), ("tauf", _D), ("snu", _D), ("sq", _D), ("viscosity", _D),
@@ -46,6 +54,9 @@ class Info(ctypes.Structure):
 SIGNATURES = {
     "mglc_lid_create": ([ctypes.POINTER(LidParams), ctypes.POINTER(_VP)], _I),
     "mglc_thermal_create": ([ctypes.POINTER(ThermalParams), ctypes.POINTER(_VP)], _I),
+    "mglc_particle_create": ([ctypes.POINTER(ParticleParams), _VP, _I, ctypes.POINTER(_VP)], _I),
+    "mglc_particle_state": ([_VP, _VP, _VP, _VP, _VP, _VP], _I),
+    "mglc_get_mask": ([_VP, _VP], _I),
     "mglc_destroy": ([_VP], None),
     "mglc_last_error": ([_VP], ctypes.c_char_p),
     "mglc_set_stream": ([_VP, _VP], _I),

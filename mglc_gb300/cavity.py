@@ -178,3 +178,48 @@ class BuoyancyCavity(_Solve):
                                             _ptr(np.ascontiguousarray(g)), _ptr(rho), _ptr(u),
                                             _ptr(v), _ptr(w), _ptr(T)))
         return self
+
+
+class ParticleFlow(_Solve):
+    """Moving spheres in a D3Q19 flow (reference: Micro_particles/fortran/case4,
+    generalised to 3-D): interpolated bounce-back, momentum-exchange force and
+    torque, springs, explicit update and refill."""
+
+    def __init__(self, total_nx, total_ny, total_nz, centers, radius, tauf=0.65, rho0=1.0,
+                 rho_solid=1.2, periodic_x=True, gravity=(0.0, 0.0, 0.0),
+                 body_force=(0.0, 0.0, 0.0), threshold_wall=2.0, threshold_particle=2.0,
+                 spring_scale_wall=1.0, spring_scale_particle=1.0, precision="fp64"):
+        super().__init__()
+        c = np.ascontiguousarray(np.asarray(centers, dtype=np.float64).reshape(-1, 3))
+        self.np = len(c)
+        p = capi.ParticleParams(total_nx, total_ny, total_nz, int(bool(periodic_x)), float(tauf),
+                                float(rho0), float(rho_solid), float(radius),
+                                (ctypes.c_double * 3)(*gravity), (ctypes.c_double * 3)(*body_force),
+                                float(threshold_wall), float(threshold_particle),
+                                float(spring_scale_wall), float(spring_scale_particle),
+                                capi.FORMS[precision])
+        ctx = _P()
+        rc = capi.lib().mglc_particle_create(ctypes.byref(p), c.ctypes.data, len(c), ctypes.byref(ctx))
+        self._ctx = ctx
+        if rc != capi.MGLC_OK:
+            msg = capi.lib().mglc_last_error(ctx).decode() if ctx else ""
+            self.close()
+            raise capi.MglcError(rc, msg)
+
+    def macro(self):
+        nz, ny, nx = self.shape
+        rho, u, v, w = (np.empty((nz, ny, nx)) for _ in range(4))
+        self._ck(capi.lib().mglc_get_macros(self._ctx, _ptr(rho), _ptr(u), _ptr(v), _ptr(w), None))
+        return rho, u, v, w
+
+    def state(self):
+        out = {k: np.zeros((self.np, 3)) for k in ("xc", "uc", "omega", "force", "torque")}
+        self._ck(capi.lib().mglc_particle_state(self._ctx, *[_ptr(out[k]) for k in
+                                                             ("xc", "uc", "omega", "force", "torque")]))
+        return out
+
+    def mask(self):
+        nz, ny, nx = self.shape
+        m = np.empty((nz, ny, nx), dtype=np.int32)
+        self._ck(capi.lib().mglc_get_mask(self._ctx, m.ctypes.data))
+        return m

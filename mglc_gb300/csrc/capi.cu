@@ -16,6 +16,7 @@
 
 #include "../../include/mglc.h"
 #include "kernels.cuh"
+#include "particles.cuh"
 
 using namespace mglc;
 
@@ -50,6 +51,10 @@ struct mglc_ctx {
     long long itc = 0;
     bool initialised = false;
     std::string err;
+    // moving particles
+    PartParams pp{};
+    PartDev pd{};
+    std::vector<double> centers0;
 };
 
 namespace {
@@ -92,6 +97,12 @@ void release(mglc_ctx* c) {
     void* ptrs[] = {c->f[0], c->f[1], c->g[0], c->g[1], c->F, c->rho, c->u, c->v, c->w, c->T,
                     c->up, c->vp, c->wp, c->Tp, c->partials, c->red_out, c->stage};
     for (void* p : ptrs)
+        if (p) cudaFree(p);
+    PartDev& d = c->pd;
+    void* pptrs[] = {d.owner_cur, d.owner_new, d.xc, d.uc, d.om, d.xc_old, d.uc_old, d.om_old,
+                     d.flink, d.tlink, d.corr, d.ftot, d.ttot, d.prep_sum, d.prep_cnt,
+                     d.partials, d.n_fluid, d.rho_avg, d.status};
+    for (void* p : pptrs)
         if (p) cudaFree(p);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
 }
@@ -204,6 +215,13 @@ bool thermal(const mglc_ctx* c) { return c->kind == MGLC_KIND_THERMAL; }
 // bring rho,u,v,w(,T) up to date with the current populations
 int refresh_macros(mglc_ctx* c) {
     if (c->macros_valid) return MGLC_OK;
+    if (c->kind == MGLC_KIND_PARTICLE) {
+        CK(launch_particle_macro(c->form, c->first_pending, c->f[c->cur], c->pp, c->pd, c->rho,
+                                 c->u, c->v, c->w, c->stream),
+           "particle macro");
+        c->macros_valid = true;
+        return MGLC_OK;
+    }
     CK(launch_macro(c->form, thermal(c), c->geom, c->f[c->cur], thermal(c) ? c->g[c->cur] : nullptr,
                     c->F, c->rho0, c->inv_scale, c->rho, c->u, c->v, c->w, c->T, c->stream),
        "macro");
@@ -346,6 +364,8 @@ int mglc_get_info(const mglc_ctx* c, mglc_info* o) {
     const double pb = (double)form_bytes(c->form);
     if (c->kind == MGLC_KIND_LID) {
         o->bytes_per_cell_step = 2.0 * Q19 * pb;
+    } else if (c->kind == MGLC_KIND_PARTICLE) {
+        o->bytes_per_cell_step = 2.0 * Q19 * pb + 4.0;  // populations + owner mask read
     } else {
         const double cb = c->form == FORM_FP64 ? 8.0 : 4.0;
         // carried force: read and written once per step (F_z only without rotation);
@@ -357,8 +377,11 @@ int mglc_get_info(const mglc_ctx* c, mglc_info* o) {
     return MGLC_OK;
 }
 
+int particle_initial(mglc_ctx* c);
+
 int mglc_initial(mglc_ctx* c) {
     if (!c || !c->kind) return MGLC_ERR_INVALID;
+    if (c->kind == MGLC_KIND_PARTICLE) return particle_initial(c);
     const long long n = c->n;
     const Geom& g = c->geom;
     // rho = rho0, u = v = w = 0 (and T); lid top layer u = U0; hot/cold walls
@@ -468,6 +491,35 @@ int mglc_step(mglc_ctx* c, int nsteps) {
     if (!c || !c->kind) return MGLC_ERR_INVALID;
     if (nsteps < 0) return fail(c, MGLC_ERR_INVALID, "nsteps must be >= 0");
     if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial or mglc_load_state first");
+    if (c->kind == MGLC_KIND_PARTICLE) {
+        for (int s = 0; s < nsteps; s++) {
+            const int nxt = c->cur ^ 1;
+            cudaError_t e = launch_particle_step(c->form, c->first_pending, c->f[c->cur],
+                                                 c->f[nxt], c->pp, c->pd, c->stream);
+            if (e != cudaSuccess) return cuda_fail(c, e, "particle step launch");
+            std::swap(c->pd.owner_cur, c->pd.owner_new);
+            c->cur = nxt;
+            c->first_pending = false;
+            c->macros_valid = false;
+            c->itc++;
+        }
+        // particle failures (overlap, wall penetration, ...) are reported here
+        int st[3] = {0, 0, 0};
+        CK(cudaMemcpyAsync(st, c->pd.status, sizeof st, cudaMemcpyDeviceToHost, c->stream),
+           "read particle status");
+        CK(cudaStreamSynchronize(c->stream), "synchronize");
+        if (st[0]) {
+            static const char* what[] = {"", "no particle owns a solid boundary node",
+                                         "interpolation fraction q outside [0,1]",
+                                         "particle-particle interpenetration",
+                                         "particle penetrates a wall",
+                                         "no refill direction for a node leaving a particle",
+                                         "too many nodes left one particle in one step"};
+            return fail(c, MGLC_ERR_PARTICLE, "%s (particle %d, other %d); the state is frozen at that step",
+                        what[st[0] < 7 ? st[0] : 0], st[1], st[2]);
+        }
+        return MGLC_OK;
+    }
     for (int s = 0; s < nsteps; s++) {
         const int nxt = c->cur ^ 1;
         cudaError_t e;
@@ -596,6 +648,137 @@ int mglc_nusselt(mglc_ctx* c, double* nu_vol, double* re_vol, double* nu_hot, do
     // dT/dn at the hot wall = (9T1 - T2 - 8Th)/3, heat leaves the hot wall: Nu = -L/dT * dT/dn
     if (nu_hot) *nu_hot = axis ? -L / dT * ((e[2] / nwall - 8.0 * c->t_hot) / 3.0) : 0.0;
     if (nu_cold) *nu_cold = axis ? L / dT * ((e[3] / nwall - 8.0 * c->t_cold) / 3.0) : 0.0;
+    return MGLC_OK;
+}
+
+int mglc_particle_create(const mglc_particle_params* p, const double* centers, int np,
+                         mglc_ctx** out) {
+    if (!p || !out || (np > 0 && !centers)) return MGLC_ERR_INVALID;
+    *out = nullptr;
+    mglc_ctx* c = new mglc_ctx();
+    *out = c;
+    int rc = check_geom(c, p->total_nx, p->total_ny, p->total_nz);
+    if (rc) return rc;
+    if (p->precision != FORM_FP64 && p->precision != FORM_FP32)
+        return fail(c, MGLC_ERR_INVALID, "particle flows support MGLC_FP64 and MGLC_FP32");
+    if (!(p->tauf > 0.5)) return fail(c, MGLC_ERR_INVALID, "tauf must exceed 0.5");
+    if (!(p->radius > 0.5)) return fail(c, MGLC_ERR_INVALID, "radius must exceed 0.5");
+    if (np < 0 || np > 65536) return fail(c, MGLC_ERR_INVALID, "np must be in [0, 65536]");
+    {   // the per-particle node boxes (2 ceil(R) + 6 wide) must not wrap onto themselves
+        const int need = 2 * (int)std::ceil(p->radius) + 6;
+        if (p->total_nx < need || p->total_ny < 8 || p->total_nz < 8)
+            return fail(c, MGLC_ERR_INVALID, "grid %dx%dx%d too small for radius %g (nx >= %d, ny, nz >= 8)",
+                        p->total_nx, p->total_ny, p->total_nz, p->radius, need);
+    }
+    if (!(p->threshold_wall > 0.0 && p->threshold_particle > 0.0))
+        return fail(c, MGLC_ERR_INVALID, "spring thresholds must be positive");
+    for (int q = 0; q < np; q++) {
+        const double* X = centers + 3 * q;
+        if (!(X[0] >= 0.5 && X[0] <= p->total_nx + 0.5 && X[1] >= 0.5 && X[1] <= p->total_ny + 0.5 &&
+              X[2] >= 0.5 && X[2] <= p->total_nz + 0.5))
+            return fail(c, MGLC_ERR_INVALID, "centre of particle %d lies outside the domain", q);
+    }
+    c->kind = MGLC_KIND_PARTICLE;
+    c->form = p->precision;
+    c->geom = {p->total_nx, p->total_ny, p->total_nz,
+               (long long)p->total_nx * p->total_ny * p->total_nz};
+    c->n = c->geom.plane;
+    c->rho0 = p->rho0;
+    c->tauf = p->tauf;
+    // case4 commondata.F90:33-34
+    c->snu = 1.0 / p->tauf;
+    c->sq = 8.0 * (2.0 * p->tauf - 1.0) / (8.0 * p->tauf - 1.0);
+    PartParams& pp = c->pp;
+    pp.nx = p->total_nx; pp.ny = p->total_ny; pp.nz = p->total_nz;
+    pp.periodic_x = p->periodic_x ? 1 : 0;
+    pp.np = np;
+    pp.rho0 = p->rho0; pp.rho_solid = p->rho_solid; pp.radius = p->radius;
+    pp.pi = 4.0 * std::atan(1.0);
+    for (int q = 0; q < 3; q++) {
+        pp.gravity[q] = p->gravity[q];
+        pp.body_force[q] = p->body_force[q];
+    }
+    pp.thr_wall = p->threshold_wall; pp.thr_part = p->threshold_particle;
+    pp.scale_wall = p->spring_scale_wall; pp.scale_part = p->spring_scale_particle;
+    pp.snu = c->snu; pp.sq = c->sq;
+    c->centers0.assign(centers, centers + 3 * (size_t)np);
+    if ((rc = create_stream(c))) return rc;
+    const size_t pb = form_bytes(c->form), n = (size_t)c->n;
+    for (int b = 0; b < 2; b++)
+        if ((rc = dalloc(c, &c->f[b], Q19 * n * pb, "populations f"))) return rc;
+    double** fields[] = {&c->rho, &c->u, &c->v, &c->w, &c->up, &c->vp, &c->wp};
+    for (double** fp : fields)
+        if ((rc = dalloc(c, (void**)fp, n * sizeof(double), "macroscopic field"))) return rc;
+    if ((rc = dalloc(c, (void**)&c->partials, (size_t)reduce_blocks(c->n) * 4 * sizeof(double), "reduction scratch")))
+        return rc;
+    if ((rc = dalloc(c, (void**)&c->red_out, 4 * sizeof(double), "reduction result"))) return rc;
+    PartDev& d = c->pd;
+    if ((rc = dalloc(c, (void**)&d.owner_cur, n * sizeof(int), "owner mask"))) return rc;
+    if ((rc = dalloc(c, (void**)&d.owner_new, n * sizeof(int), "owner mask"))) return rc;
+    const size_t v3 = sizeof(double) * 3 * (size_t)(np > 0 ? np : 1);
+    double** p3[] = {&d.xc, &d.uc, &d.om, &d.xc_old, &d.uc_old, &d.om_old, &d.flink, &d.tlink, &d.ftot, &d.ttot};
+    for (double** a : p3)
+        if ((rc = dalloc(c, (void**)a, v3, "particle state"))) return rc;
+    if ((rc = dalloc(c, (void**)&d.corr, v3 / 3, "particle sums"))) return rc;
+    if ((rc = dalloc(c, (void**)&d.prep_sum, v3 / 3, "particle sums"))) return rc;
+    if ((rc = dalloc(c, (void**)&d.prep_cnt, sizeof(int) * (size_t)(np > 0 ? np : 1), "particle sums"))) return rc;
+    d.nblocks = particle_bulk_blocks(pp);
+    if ((rc = dalloc(c, (void**)&d.partials, sizeof(double) * 2 * (size_t)d.nblocks, "bulk partials"))) return rc;
+    if ((rc = dalloc(c, (void**)&d.n_fluid, 2 * sizeof(long long), "fluid count"))) return rc;
+    if ((rc = dalloc(c, (void**)&d.rho_avg, 4 * sizeof(double), "average density"))) return rc;
+    if ((rc = dalloc(c, (void**)&d.status, 3 * sizeof(int), "particle status"))) return rc;
+    return MGLC_OK;
+}
+
+int particle_initial(mglc_ctx* c) {
+    PartDev& d = c->pd;
+    const int np = c->pp.np;
+    const size_t v3 = sizeof(double) * 3 * (size_t)(np > 0 ? np : 1);
+    if (np > 0)
+        CK(cudaMemcpyAsync(d.xc, c->centers0.data(), sizeof(double) * 3 * np, cudaMemcpyHostToDevice, c->stream),
+           "copy centres");
+    CK(cudaMemsetAsync(d.uc, 0, v3, c->stream), "zero velocities");
+    CK(cudaMemsetAsync(d.om, 0, v3, c->stream), "zero rotation");
+    CK(cudaMemsetAsync(d.ftot, 0, v3, c->stream), "zero forces");
+    CK(cudaMemsetAsync(d.ttot, 0, v3, c->stream), "zero torques");
+    CK(cudaMemsetAsync(d.status, 0, 3 * sizeof(int), c->stream), "zero status");
+    CK(cudaMemsetAsync(d.rho_avg, 0, 4 * sizeof(double), c->stream), "zero average");
+    const size_t b = c->n * sizeof(double);
+    CK(cudaMemsetAsync(c->up, 0, b, c->stream), "zero up");
+    CK(cudaMemsetAsync(c->vp, 0, b, c->stream), "zero vp");
+    CK(cudaMemsetAsync(c->wp, 0, b, c->stream), "zero wp");
+    CK(launch_particle_init(c->form, c->f[0], c->pp, d, c->stream), "particle initial");
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
+    c->cur = 0;
+    c->itc = 0;
+    c->first_pending = true;
+    c->macros_valid = false;
+    c->initialised = true;
+    return MGLC_OK;
+}
+
+int mglc_particle_state(mglc_ctx* c, double* xc, double* uc, double* omega, double* force,
+                        double* torque) {
+    if (!c || c->kind != MGLC_KIND_PARTICLE)
+        return c ? fail(c, MGLC_ERR_STATE, "mglc_particle_state needs a particle context") : MGLC_ERR_INVALID;
+    const size_t b = sizeof(double) * 3 * (size_t)c->pp.np;
+    if (b == 0) return MGLC_OK;
+    if (xc) CK(cudaMemcpyAsync(xc, c->pd.xc, b, cudaMemcpyDeviceToHost, c->stream), "copy centres");
+    if (uc) CK(cudaMemcpyAsync(uc, c->pd.uc, b, cudaMemcpyDeviceToHost, c->stream), "copy velocities");
+    if (omega) CK(cudaMemcpyAsync(omega, c->pd.om, b, cudaMemcpyDeviceToHost, c->stream), "copy rotation");
+    if (force) CK(cudaMemcpyAsync(force, c->pd.ftot, b, cudaMemcpyDeviceToHost, c->stream), "copy forces");
+    if (torque) CK(cudaMemcpyAsync(torque, c->pd.ttot, b, cudaMemcpyDeviceToHost, c->stream), "copy torques");
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
+    return MGLC_OK;
+}
+
+int mglc_get_mask(mglc_ctx* c, int* owner) {
+    if (!c || c->kind != MGLC_KIND_PARTICLE || !owner)
+        return c ? fail(c, MGLC_ERR_STATE, "mglc_get_mask needs a particle context and a buffer") : MGLC_ERR_INVALID;
+    if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial first");
+    CK(cudaMemcpyAsync(owner, c->pd.owner_cur, sizeof(int) * (size_t)c->n, cudaMemcpyDeviceToHost, c->stream),
+       "copy mask");
+    CK(cudaStreamSynchronize(c->stream), "synchronize");
     return MGLC_OK;
 }
 

@@ -1,0 +1,727 @@
+// k_particle.cu -- moving spheres in a D3Q19 channel (periodic x, no-slip y/z
+// walls): the 3-D generalisation of the reference's Micro_particles step
+// (MPI/Micro_particles/fortran/case4/mpi_particle, main.F90:35-73).
+//
+// Per time step:
+//   k_pbulk     fluid cells: macro, forced MRT collision, push to the
+//               neighbours (x wraps, y/z walls bounce back in place);
+//               solid cells do nothing.  Block partials of sum rho and of
+//               the post-collision mass feed the average density.
+//   k_pfinish   fixed-order sums -> rho_avg (particle_bounceback.F90:15-35)
+//   k_plinks    one CTA per particle: every fluid node x with a neighbour
+//               x+e inside the particle is a boundary link.  The
+//               post-collision values the quadratic interpolated bounce-back
+//               needs (particle_bounceback.F90:65-75) are read from the
+//               streamed array: fp(a,y) sits in f(a, y+e_a) after the push
+//               (including solid destination cells, which only fluid pushes
+//               write).  Writes f(abar,x) and accumulates the Wen 2014
+//               momentum exchange (particle_force.F90:59-66) in FP64.
+//   k_pupdate   one CTA: springs, gravity, body force, explicit update
+//               (particle_force.F90:96-190, particle_update.F90:26-50).
+//   k_pmark     new owner mask from the new centres (particle_update.F90:80-93)
+//   k_pprep     density bookkeeping of nodes that change phase
+//   k_prefill   refill of nodes that left a particle (:134-193), two phases
+//               per particle (all reads, then all writes).
+// Any kernel that detects a failure (no owner, q out of range, overlap, wall
+// penetration) writes a status code; every kernel returns at once while the
+// status is set, so the state freezes at the failing step and the host
+// reports MGLC_ERR_PARTICLE.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "particles.cuh"
+
+namespace mglc {
+
+constexpr int PB = 256;             // threads of the per-particle kernels
+constexpr int REFILL_MAX = 256;     // refilled nodes one particle may produce per step
+
+template <typename S>
+struct PSt;
+template <>
+struct PSt<double> {
+    static constexpr bool SHIFT = false;
+    __device__ static double ld(const double* p) { return *p; }
+    __device__ static void st(double* p, double v) { *p = v; }
+};
+template <>
+struct PSt<float> {
+    static constexpr bool SHIFT = true;
+    __device__ static double ld(const float* p) { return (double)*p; }
+    __device__ static void st(float* p, double v) { *p = (float)v; }
+};
+
+// absolute population value (FP64) of a stored slot
+template <typename S>
+__device__ __forceinline__ double pabs(const S* f, long long idx, int q, double rho0) {
+    double v = PSt<S>::ld(f + idx);
+    return PSt<S>::SHIFT ? v + w19(q) * rho0 : v;
+}
+template <typename S>
+__device__ __forceinline__ void pset(S* f, long long idx, int q, double v, double rho0) {
+    PSt<S>::st(f + idx, PSt<S>::SHIFT ? v - w19(q) * rho0 : v);
+}
+
+__device__ __forceinline__ double dxp(double a, double b, const PartParams& p) {
+    double d = a - b;
+    if (p.periodic_x) {
+        const double L = (double)p.nx;
+        while (d > 0.5 * L) d -= L;
+        while (d < -0.5 * L) d += L;
+    }
+    return d;
+}
+// ((x-xc)^2 + (y-yc)^2 + (z-zc)^2) <= R^2 with IEEE-rounded operations
+__device__ __forceinline__ bool inside(double x, double y, double z, const double* X, double R,
+                                       const PartParams& p) {
+    const double a = dxp(x, X[0], p), b = y - X[1], c = z - X[2];
+    double d = __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c));
+    return d <= __dmul_rn(R, R);
+}
+__device__ __forceinline__ int wrapx(int i, int nx) { return i < 0 ? i + nx : (i >= nx ? i - nx : i); }
+
+template <int NV>
+__device__ __forceinline__ void block_sum_to(double (&v)[NV], double* out, int stride) {
+    __shared__ double sh[32][NV];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; k++) sh[wid][k] = v[k];
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int k = 0; k < NV; k++) {
+            double t = 0.0;
+            for (int q = 0; q < nw; q++) t += sh[q][k];
+            out[k * stride] = t;
+        }
+    __syncthreads();
+}
+
+// ------------------------------------------------------------- bulk step --
+// compute type: FP64 for FP64 storage; FP32 (on deviations f - w rho0) for
+// FP32 storage
+template <typename S> struct PC { using C = double; };
+template <> struct PC<float> { using C = float; };
+
+template <typename S, bool FIRST>
+__global__ void __launch_bounds__(128)
+    k_pbulk(const S* __restrict__ fin, S* __restrict__ fout, const int* __restrict__ owner,
+            PartParams p, MrtCoef<typename PC<S>::C> cd, double* partials, const int* status) {
+    using C = typename PC<S>::C;
+    constexpr bool DEV = PSt<S>::SHIFT;
+    if (status[0]) return;
+    const int nx = p.nx, ny = p.ny, nz = p.nz;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y, k = blockIdx.z;
+    const long long P = (long long)nx * ny * nz;
+    double acc[2] = {0.0, 0.0};
+    const bool active = i < nx;
+    const long long cell = (long long)i + (long long)nx * (j + (long long)ny * k);
+    if (active && owner[cell] < 0) {
+        C f[Q19];
+#pragma unroll
+        for (int q = 0; q < Q19; q++) f[q] = (C)fin[q * P + cell];
+        const C rho0 = (C)p.rho0;
+        const C ax = (C)p.body_force[0], ay = (C)p.body_force[1], az = (C)p.body_force[2];
+        C rho_m, rho, ux, uy, uz;
+        if (FIRST) {  // the reference's initial fields: rho0, u = 0
+            rho = rho0;
+            rho_m = DEV ? C(0) : rho0;
+            ux = uy = uz = C(0);
+        } else {
+            C jx, jy, jz;
+            moments0(f, rho_m, jx, jy, jz);
+            rho = DEV ? rho0 + rho_m : rho_m;
+            // u = (sum f e + F/2)/rho with F = rho*a (thermal macro form)
+            ux = (jx + C(0.5) * (rho * ax)) / rho;
+            uy = (jy + C(0.5) * (rho * ay)) / rho;
+            uz = (jz + C(0.5) * (rho * az)) / rho;
+        }
+        acc[0] = (double)rho;
+        mrt_collide<C, true, false>(f, rho_m, rho, ux, uy, uz, rho * ax, rho * ay, rho * az, cd);
+        double m = DEV ? p.rho0 : 0.0;
+#pragma unroll
+        for (int q = 0; q < Q19; q++) m += (double)f[q];
+        acc[1] = m;
+        const long long sy = nx, sz = (long long)nx * ny;
+#pragma unroll
+        for (int q = 0; q < Q19; q++) {
+            const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
+            const int jj = j + dy, kk = k + dz, ir = i + dx;
+            const bool xwall = !p.periodic_x && (ir < 0 || ir >= nx);
+            if (xwall || jj < 0 || jj >= ny || kk < 0 || kk >= nz) {
+                fout[opp19(q) * P + cell] = (S)f[q];  // no-slip wall
+            } else {
+                const int ii = wrapx(ir, nx);
+                fout[q * P + ((long long)ii + sy * jj + sz * kk)] = (S)f[q];
+            }
+        }
+    }
+    const int b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    block_sum_to<2>(acc, partials + b, (int)(gridDim.x * gridDim.y * gridDim.z));
+}
+
+__global__ void k_pfinish(PartDev d, int nblocks) {
+    if (d.status[0]) return;
+    double acc[2] = {0.0, 0.0};
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+        acc[0] += d.partials[b];
+        acc[1] += d.partials[nblocks + b];
+    }
+    __shared__ double out[2];
+    block_sum_to<2>(acc, out, 1);
+    if (threadIdx.x == 0) {
+        d.rho_avg[0] = out[0] / (double)d.n_fluid[0];
+        d.rho_avg[2] = out[1];
+    }
+}
+
+// --------------------------------------------------- boundary links (IBB) --
+// post-collision value fp(q, c) of node c (coordinates as 0-based indices)
+// read from the streamed array; nodes outside the y/z walls give the
+// reference's ghost value omega*rho0
+template <typename S>
+__device__ __forceinline__ double fp_at(const S* f, int q, int i, int j, int k,
+                                        const PartParams& p) {
+    const int nx = p.nx, ny = p.ny, nz = p.nz;
+    if (j < 0 || j >= ny || k < 0 || k >= nz) return w19(q) * p.rho0;
+    if (!p.periodic_x && (i < 0 || i >= nx)) return w19(q) * p.rho0;
+    const long long P = (long long)nx * ny * nz;
+    i = wrapx(i, nx);
+    const int jj = j + ey19(q), kk = k + ez19(q), ir = i + ex19(q);
+    if (jj < 0 || jj >= ny || kk < 0 || kk >= nz || (!p.periodic_x && (ir < 0 || ir >= nx)))
+        // bounced back into slot opp(q) of c
+        return pabs<S>(f, opp19(q) * P + (i + (long long)nx * (j + (long long)ny * k)), opp19(q), p.rho0);
+    const int ii = wrapx(ir, nx);
+    return pabs<S>(f, q * P + (ii + (long long)nx * (jj + (long long)ny * kk)), q, p.rho0);
+}
+
+template <typename S>
+__global__ void __launch_bounds__(PB) k_plinks(S* __restrict__ f, PartParams p, PartDev d) {
+    if (d.status[0]) return;
+    const int c = blockIdx.x;
+    const double* X = d.xc + 3 * c;
+    const double* U = d.uc + 3 * c;
+    const double* O = d.om + 3 * c;
+    const double R = p.radius, ravg = d.rho_avg[0];
+    const int nx = p.nx, ny = p.ny, nz = p.nz;
+    const long long P = (long long)nx * ny * nz;
+    // box of nodes within R+2 of the centre (1-based coordinate = index + 1)
+    const int h = (int)ceil(R) + 2;
+    const int ci = (int)floor(X[0]) - 1, cj = (int)floor(X[1]) - 1, ck = (int)floor(X[2]) - 1;
+    const int bw = 2 * h + 2;
+    const long long nbox = (long long)bw * bw * bw;
+    double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+    for (long long t = threadIdx.x; t < nbox; t += PB) {
+        const int bi = (int)(t % bw), bj = (int)((t / bw) % bw), bk = (int)(t / ((long long)bw * bw));
+        int i = ci - h + bi;
+        const int j = cj - h + bj, k = ck - h + bk;
+        if (j < 0 || j >= ny || k < 0 || k >= nz) continue;
+        if (p.periodic_x) i = wrapx(i, nx);
+        else if (i < 0 || i >= nx) continue;
+        const long long cell = i + (long long)nx * (j + (long long)ny * k);
+        if (d.owner_cur[cell] >= 0) continue;
+#pragma unroll 1
+        for (int a = 1; a < Q19; a++) {
+            const int ea = ex19(a), eb = ey19(a), ec = ez19(a);
+            const int jn = j + eb, kn = k + ec;
+            if (jn < 0 || jn >= ny || kn < 0 || kn >= nz) continue;
+            int in = i + ea;
+            if (p.periodic_x) in = wrapx(in, nx);
+            else if (in < 0 || in >= nx) continue;
+            if (d.owner_cur[in + (long long)nx * (jn + (long long)ny * kn)] != c) continue;
+            // q: ray-sphere root from the node (calQ2, particle_bounceback.F90:144-185)
+            double x = (double)(i + 1), y = (double)(j + 1), z = (double)(k + 1);
+            if (p.periodic_x) x = X[0] + dxp(x, X[0], p);
+            const double ca = (double)(ea * ea + eb * eb + ec * ec);
+            const double cb = 2.0 * (ea * (x - X[0]) + eb * (y - X[1]) + ec * (z - X[2]));
+            const double cc = (x - X[0]) * (x - X[0]) + (y - X[1]) * (y - X[1]) + (z - X[2]) * (z - X[2]) - R * R;
+            const double delta = cb * cb - 4.0 * ca * cc;
+            if (delta < 0) { atomicCAS(d.status, 0, PS_Q_RANGE); d.status[1] = c; continue; }
+            const double q = (-cb - sqrt(delta)) / (2.0 * ca);
+            if (q > 1.0 || q < 0.0) { atomicCAS(d.status, 0, PS_Q_RANGE); d.status[1] = c; continue; }
+            const double x0 = x + q * ea, y0 = y + q * eb, z0 = z + q * ec;
+            const double rx = x0 - X[0], ry = y0 - X[1], rz = z0 - X[2];
+            const double rot0 = O[1] * rz - O[2] * ry, rot1 = O[2] * rx - O[0] * rz,
+                         rot2 = O[0] * ry - O[1] * rx;
+            const int ra = opp19(a);
+            const double eu = -ea * (U[0] + rot0) - eb * (U[1] + rot1) - ec * (U[2] + rot2);
+            const double fpa = fp_at<S>(f, a, i, j, k, p);
+            double val;
+            if (q < 0.5) {
+                const double f1 = fp_at<S>(f, a, i - ea, j - eb, k - ec, p);
+                const double f2 = fp_at<S>(f, a, i - 2 * ea, j - 2 * eb, k - 2 * ec, p);
+                val = q * (1.0 + 2.0 * q) * fpa + (1.0 - 4.0 * q * q) * f1 - q * (1.0 - 2.0 * q) * f2 +
+                      6.0 * w19(a) * ravg * eu;
+            } else {
+                const double g0 = fp_at<S>(f, ra, i, j, k, p);
+                const double g1 = fp_at<S>(f, ra, i - ea, j - eb, k - ec, p);
+                val = fpa / q / (1.0 + 2.0 * q) + g0 * (2.0 * q - 1.0) / q -
+                      g1 * (2.0 * q - 1.0) / (2.0 * q + 1.0) + 6.0 * w19(a) * ravg / q / (1.0 + 2.0 * q) * eu;
+            }
+            pset<S>(f, ra * P + cell, ra, val, p.rho0);
+            const double fnew = pabs<S>(f, ra * P + cell, ra, p.rho0);  // as stored
+            // Wen et al. 2014 Galilean-invariant momentum exchange
+            const double Fx = (ea - U[0] - rot0) * fpa - (-ea - U[0] - rot0) * fnew;
+            const double Fy = (eb - U[1] - rot1) * fpa - (-eb - U[1] - rot1) * fnew;
+            const double Fz = (ec - U[2] - rot2) * fpa - (-ec - U[2] - rot2) * fnew;
+            acc[0] += Fx;
+            acc[1] += Fy;
+            acc[2] += Fz;
+            acc[3] += ry * Fz - rz * Fy;
+            acc[4] += rz * Fx - rx * Fz;
+            acc[5] += rx * Fy - ry * Fx;
+            acc[6] += fnew - fpa;
+        }
+    }
+    __shared__ double out[7];
+    block_sum_to<7>(acc, out, 1);
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < 3; q++) {
+            d.flink[3 * c + q] = out[q];
+            d.tlink[3 * c + q] = out[3 + q];
+        }
+        d.corr[c] = out[6];
+    }
+}
+
+// ----------------------------------------------------------- update --------
+// particle_force.F90:96-190 and particle_update.F90:26-50 in 3-D
+__global__ void k_pupdate(PartParams p, PartDev d) {
+    if (d.status[0]) return;
+    const int np = p.np;
+    const double R0 = p.radius, ravg = d.rho_avg[0];
+    const double vol = 4.0 / 3.0 * p.pi * R0 * R0 * R0;
+    const double M = p.rho_solid * 4.0 / 3.0 * p.pi * R0 * R0 * R0;
+    for (int c = threadIdx.x; c < np; c += blockDim.x) {
+        const double* X = d.xc + 3 * c;
+        double fij[3] = {0.0, 0.0, 0.0}, fw[3] = {0.0, 0.0, 0.0};
+        const double Rc = R0;
+        for (int c2 = 0; c2 < np; c2++) {
+            if (c2 == c) continue;
+            const double* X2 = d.xc + 3 * c2;
+            const double d0 = dxp(X[0], X2[0], p), d1 = X[1] - X2[1], d2 = X[2] - X2[2];
+            const double dij = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+            const double thr = p.thr_part;
+            if (dij >= Rc + R0 + thr) {
+            } else if (dij >= Rc + R0) {
+                const double t = (dij - Rc - R0 - thr) / thr;
+                fij[0] = fij[0] + p.scale_part * (t * t) * d0 / dij;
+                fij[1] = fij[1] + p.scale_part * (t * t) * d1 / dij;
+                fij[2] = fij[2] + p.scale_part * (t * t) * d2 / dij;
+            } else {
+                if (atomicCAS(d.status, 0, PS_OVERLAP) == 0) {
+                    d.status[1] = c;
+                    d.status[2] = c2;
+                }
+            }
+        }
+        const double thw = p.thr_wall;
+        for (int ax = 0; ax < 3; ax++) {
+            if (ax == 0 && p.periodic_x) continue;
+            const int nax = ax == 0 ? p.nx : (ax == 1 ? p.ny : p.nz);
+            double dw = X[ax] - Rc - 1.0;
+            if (dw < 0) {
+                if (atomicCAS(d.status, 0, PS_WALL) == 0) d.status[1] = c;
+            } else if (dw < thw) {
+                fw[ax] = fw[ax] + p.scale_wall * ((dw - thw) / thw) * ((dw - thw) / thw);
+            }
+            dw = (double)nax - X[ax] - Rc;
+            if (dw < 0) {
+                if (atomicCAS(d.status, 0, PS_WALL) == 0) d.status[1] = c;
+            } else if (dw < thw) {
+                fw[ax] = fw[ax] - p.scale_wall * ((dw - thw) / thw) * ((dw - thw) / thw);
+            }
+        }
+        for (int q = 0; q < 3; q++) {
+            double tot = d.flink[3 * c + q] + (p.rho_solid - ravg) * vol * p.gravity[q] + fij[q] + fw[q];
+            tot = tot + ravg * vol * p.body_force[q];
+            d.ftot[3 * c + q] = tot;
+            d.ttot[3 * c + q] = d.tlink[3 * c + q];
+        }
+    }
+    __syncthreads();
+    if (d.status[0]) return;
+    for (int c = threadIdx.x; c < np; c += blockDim.x) {
+        const double I = 0.4 * M * R0 * R0;
+        for (int q = 0; q < 3; q++) {
+            d.xc_old[3 * c + q] = d.xc[3 * c + q];
+            d.uc_old[3 * c + q] = d.uc[3 * c + q];
+            d.om_old[3 * c + q] = d.om[3 * c + q];
+            const double a = d.ftot[3 * c + q] / M;
+            d.uc[3 * c + q] = d.uc_old[3 * c + q] + a;
+            d.om[3 * c + q] = d.om_old[3 * c + q] + d.ttot[3 * c + q] / I;
+            d.xc[3 * c + q] = d.xc_old[3 * c + q] + d.uc_old[3 * c + q] + 0.5 * a;
+        }
+        if (p.periodic_x) {
+            const double L = (double)p.nx;
+            if (d.xc[3 * c] >= L + 0.5) d.xc[3 * c] -= L;
+            if (d.xc[3 * c] < 0.5) d.xc[3 * c] += L;
+        }
+    }
+}
+
+// -------------------------------------------------------------- new mask --
+__global__ void __launch_bounds__(PB) k_pmark(int* owner, const double* xc, PartParams p,
+                                                const int* status, bool check_status) {
+    if (check_status && status[0]) return;
+    const int c = blockIdx.x;
+    const double* X = xc + 3 * c;
+    const double R = p.radius;
+    const int h = (int)ceil(R) + 1;
+    const int ci = (int)floor(X[0]) - 1, cj = (int)floor(X[1]) - 1, ck = (int)floor(X[2]) - 1;
+    const int bw = 2 * h + 2;
+    const long long nbox = (long long)bw * bw * bw;
+    for (long long t = threadIdx.x; t < nbox; t += PB) {
+        const int bi = (int)(t % bw), bj = (int)((t / bw) % bw), bk = (int)(t / ((long long)bw * bw));
+        int i = ci - h + bi;
+        const int j = cj - h + bj, k = ck - h + bk;
+        if (j < 0 || j >= p.ny || k < 0 || k >= p.nz) continue;
+        if (p.periodic_x) i = wrapx(i, p.nx);
+        else if (i < 0 || i >= p.nx) continue;
+        if (inside((double)(i + 1), (double)(j + 1), (double)(k + 1), X, R, p))
+            owner[i + (long long)p.nx * (j + (long long)p.ny * k)] = c;
+    }
+}
+
+// nodes that change phase: density bookkeeping of the average used by the refill
+template <typename S>
+__global__ void __launch_bounds__(PB) k_pprep(const S* __restrict__ f, PartParams p, PartDev d) {
+    if (d.status[0]) return;
+    const int c = blockIdx.x;
+    const long long P = (long long)p.nx * p.ny * p.nz;
+    double sum = 0.0;
+    int cnt = 0;
+    for (int pass = 0; pass < 2; pass++) {
+        const double* X = (pass == 0 ? d.xc_old : d.xc) + 3 * c;
+        const int h = (int)ceil(p.radius) + 1;
+        const int ci = (int)floor(X[0]) - 1, cj = (int)floor(X[1]) - 1, ck = (int)floor(X[2]) - 1;
+        const int bw = 2 * h + 2;
+        const long long nbox = (long long)bw * bw * bw;
+        for (long long t = threadIdx.x; t < nbox; t += PB) {
+            const int bi = (int)(t % bw), bj = (int)((t / bw) % bw), bk = (int)(t / ((long long)bw * bw));
+            int i = ci - h + bi;
+            const int j = cj - h + bj, k = ck - h + bk;
+            if (j < 0 || j >= p.ny || k < 0 || k >= p.nz) continue;
+            if (p.periodic_x) i = wrapx(i, p.nx);
+            else if (i < 0 || i >= p.nx) continue;
+            const long long cell = i + (long long)p.nx * (j + (long long)p.ny * k);
+            const int oc = d.owner_cur[cell], on = d.owner_new[cell];
+            if (pass == 0 && oc == c && on < 0) {  // leaves particle c: counted with rho_solid
+                sum += p.rho_solid;
+                cnt += 1;
+            }
+            if (pass == 1 && oc < 0 && on == c) {  // enters particle c: drop its density
+                double r = 0.0;
+                for (int q = 0; q < Q19; q++) r += pabs<S>(f, q * P + cell, q, p.rho0);
+                sum -= r;
+                cnt -= 1;
+            }
+        }
+    }
+    double acc[2] = {sum, (double)cnt};
+    __shared__ double out[2];
+    block_sum_to<2>(acc, out, 1);
+    if (threadIdx.x == 0) {
+        d.prep_sum[c] = out[0];
+        d.prep_cnt[c] = (int)llround(out[1]);
+    }
+}
+
+// D3Q19 forward moments and inverse in the reference's basis, FP64
+__device__ void moments19d(const double* f, double* m) {
+    m[0] = f[0] + f[1] + f[2] + f[3] + f[4] + f[5] + f[6] + f[7] + f[8] + f[9] + f[10] + f[11] +
+           f[12] + f[13] + f[14] + f[15] + f[16] + f[17] + f[18];
+    m[1] = -30.0 * f[0] - 11.0 * (f[1] + f[2] + f[3] + f[4] + f[5] + f[6]) +
+           8.0 * (f[7] + f[8] + f[9] + f[10] + f[11] + f[12] + f[13] + f[14] + f[15] + f[16] + f[17] + f[18]);
+    m[2] = 12.0 * f[0] - 4.0 * (f[1] + f[2] + f[3] + f[4] + f[5] + f[6]) + f[7] + f[8] + f[9] +
+           f[10] + f[11] + f[12] + f[13] + f[14] + f[15] + f[16] + f[17] + f[18];
+    m[3] = f[1] - f[2] + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14];
+    m[4] = -4.0 * (f[1] - f[2]) + f[7] - f[8] + f[9] - f[10] + f[11] - f[12] + f[13] - f[14];
+    m[5] = f[3] - f[4] + f[7] + f[8] - f[9] - f[10] + f[15] - f[16] + f[17] - f[18];
+    m[6] = -4.0 * (f[3] - f[4]) + f[7] + f[8] - f[9] - f[10] + f[15] - f[16] + f[17] - f[18];
+    m[7] = f[5] - f[6] + f[11] + f[12] - f[13] - f[14] + f[15] + f[16] - f[17] - f[18];
+    m[8] = -4.0 * (f[5] - f[6]) + f[11] + f[12] - f[13] - f[14] + f[15] + f[16] - f[17] - f[18];
+    m[9] = 2.0 * (f[1] + f[2]) - f[3] - f[4] - f[5] - f[6] + f[7] + f[8] + f[9] + f[10] + f[11] +
+           f[12] + f[13] + f[14] - 2.0 * (f[15] + f[16] + f[17] + f[18]);
+    m[10] = -4.0 * (f[1] + f[2]) + 2.0 * (f[3] + f[4] + f[5] + f[6]) + f[7] + f[8] + f[9] + f[10] +
+            f[11] + f[12] + f[13] + f[14] - 2.0 * (f[15] + f[16] + f[17] + f[18]);
+    m[11] = f[3] + f[4] - f[5] - f[6] + f[7] + f[8] + f[9] + f[10] - (f[11] + f[12] + f[13] + f[14]);
+    m[12] = -2.0 * (f[3] + f[4] - f[5] - f[6]) + (f[7] + f[8] + f[9] + f[10]) - (f[11] + f[12] + f[13] + f[14]);
+    m[13] = f[7] - f[8] - f[9] + f[10];
+    m[14] = f[15] - f[16] - f[17] + f[18];
+    m[15] = f[11] - f[12] - f[13] + f[14];
+    m[16] = f[7] - f[8] + f[9] - f[10] - f[11] + f[12] - f[13] + f[14];
+    m[17] = -f[7] - f[8] + f[9] + f[10] + f[15] - f[16] + f[17] - f[18];
+    m[18] = f[11] + f[12] - f[13] - f[14] - f[15] - f[16] + f[17] + f[18];
+}
+// f = M^-1 m with M^-1 = M^T diag(1/|M_k|^2)
+__device__ void inverse19d(const double* m, double* f) {
+    const double a0 = m[0] / 19.0, a1 = m[1] / 2394.0, a2 = m[2] / 252.0;
+    const double b3 = m[3] / 10.0, b4 = m[4] / 40.0, b5 = m[5] / 10.0, b6 = m[6] / 40.0,
+                 b7 = m[7] / 10.0, b8 = m[8] / 40.0;
+    const double c9 = m[9] / 36.0, c10 = m[10] / 72.0, c11 = m[11] / 12.0, c12 = m[12] / 24.0;
+    const double d13 = m[13] / 4.0, d14 = m[14] / 4.0, d15 = m[15] / 4.0;
+    const double e16 = m[16] / 8.0, e17 = m[17] / 8.0, e18 = m[18] / 8.0;
+    f[0] = a0 - 30.0 * a1 + 12.0 * a2;
+    const double ax = a0 - 11.0 * a1 - 4.0 * a2, ed = a0 + 8.0 * a1 + a2;
+    f[1] = ax + (b3 - 4.0 * b4) + (2.0 * c9 - 4.0 * c10);
+    f[2] = ax - (b3 - 4.0 * b4) + (2.0 * c9 - 4.0 * c10);
+    f[3] = ax + (b5 - 4.0 * b6) - c9 + 2.0 * c10 + c11 - 2.0 * c12;
+    f[4] = ax - (b5 - 4.0 * b6) - c9 + 2.0 * c10 + c11 - 2.0 * c12;
+    f[5] = ax + (b7 - 4.0 * b8) - c9 + 2.0 * c10 - c11 + 2.0 * c12;
+    f[6] = ax - (b7 - 4.0 * b8) - c9 + 2.0 * c10 - c11 + 2.0 * c12;
+    const double E = ed + c9 + c10;
+    f[7] = E + c11 + c12 + d13 + (b3 + b4 + b5 + b6) + e16 - e17;
+    f[10] = E + c11 + c12 + d13 - (b3 + b4 + b5 + b6) - e16 + e17;
+    f[9] = E + c11 + c12 - d13 + (b3 + b4 - b5 - b6) + e16 + e17;
+    f[8] = E + c11 + c12 - d13 - (b3 + b4 - b5 - b6) - e16 - e17;
+    f[11] = E - c11 - c12 + d15 + (b3 + b4 + b7 + b8) - e16 + e18;
+    f[14] = E - c11 - c12 + d15 - (b3 + b4 + b7 + b8) + e16 - e18;
+    f[13] = E - c11 - c12 - d15 + (b3 + b4 - b7 - b8) - e16 - e18;
+    f[12] = E - c11 - c12 - d15 - (b3 + b4 - b7 - b8) + e16 + e18;
+    const double Ez = ed - 2.0 * c9 - 2.0 * c10;
+    f[15] = Ez + d14 + (b5 + b6 + b7 + b8) + e17 - e18;
+    f[18] = Ez + d14 - (b5 + b6 + b7 + b8) - e17 + e18;
+    f[17] = Ez - d14 + (b5 + b6 - b7 - b8) + e17 + e18;
+    f[16] = Ez - d14 - (b5 + b6 - b7 - b8) - e17 - e18;
+}
+
+// refill (particle_update.F90:134-193 in 3-D): extrapolate along the lattice
+// direction closest to the outward normal, then reset the momentum moments to
+// rho_avg times the wall velocity.  All of a particle's refills read before
+// any of them is written.
+template <typename S>
+__global__ void __launch_bounds__(PB) k_prefill(S* __restrict__ f, PartParams p, PartDev d,
+                                                int nblocks_bulk) {
+    if (d.status[0]) return;
+    const int c = blockIdx.x;
+    const long long P = (long long)p.nx * p.ny * p.nz;
+    __shared__ double s_val[REFILL_MAX][Q19];
+    __shared__ long long s_cell[REFILL_MAX];
+    __shared__ int s_n;
+    __shared__ double s_ravg;
+    if (threadIdx.x == 0) {
+        s_n = 0;
+        // average density over the new fluid set (fixed-order sums)
+        double sum = d.rho_avg[2];
+        long long cnt = d.n_fluid[0];
+        for (int q = 0; q < p.np; q++) {
+            sum += d.corr[q];
+            sum += d.prep_sum[q];
+            cnt += d.prep_cnt[q];
+        }
+        s_ravg = sum / (double)cnt;
+        if (c == 0) {
+            d.rho_avg[1] = s_ravg;
+        }
+    }
+    __syncthreads();
+    const double* X = d.xc + 3 * c;       // new centre
+    const double* Xo = d.xc_old + 3 * c;  // old centre: the nodes it covered
+    const double* U = d.uc + 3 * c;
+    const double* O = d.om + 3 * c;
+    const int h = (int)ceil(p.radius) + 1;
+    const int ci = (int)floor(Xo[0]) - 1, cj = (int)floor(Xo[1]) - 1, ck = (int)floor(Xo[2]) - 1;
+    const int bw = 2 * h + 2;
+    const long long nbox = (long long)bw * bw * bw;
+    for (long long t = threadIdx.x; t < nbox; t += PB) {
+        const int bi = (int)(t % bw), bj = (int)((t / bw) % bw), bk = (int)(t / ((long long)bw * bw));
+        int i = ci - h + bi;
+        const int j = cj - h + bj, k = ck - h + bk;
+        if (j < 0 || j >= p.ny || k < 0 || k >= p.nz) continue;
+        if (p.periodic_x) i = wrapx(i, p.nx);
+        else if (i < 0 || i >= p.nx) continue;
+        const long long cell = i + (long long)p.nx * (j + (long long)p.ny * k);
+        if (!(d.owner_cur[cell] == c && d.owner_new[cell] < 0)) continue;
+        const double rx = dxp((double)(i + 1), X[0], p), ry = (double)(j + 1) - X[1],
+                     rz = (double)(k + 1) - X[2];
+        double out = 0.0;
+        int ec = 0;
+        const double rn = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(rx, rx), __dmul_rn(ry, ry)), __dmul_rn(rz, rz)));
+        for (int a = 1; a < Q19; a++) {
+            const double tn = __ddiv_rn(__dadd_rn(__dadd_rn(__dmul_rn(rx, (double)ex19(a)), __dmul_rn(ry, (double)ey19(a))),
+                                                  __dmul_rn(rz, (double)ez19(a))), rn);
+            if (tn > out) {
+                out = tn;
+                ec = a;
+            }
+        }
+        if (ec == 0) {
+            atomicCAS(d.status, 0, PS_NO_REFILL_DIR);
+            continue;
+        }
+        const int e0 = ex19(ec), e1 = ey19(ec), e2 = ez19(ec);
+        double fl[Q19], m[Q19];
+        for (int a = 0; a < Q19; a++) {
+            double fv[3];
+            for (int s = 1; s <= 3; s++) {
+                const int ii = p.periodic_x ? wrapx(i + s * e0, p.nx) : i + s * e0;
+                const int jj = j + s * e1, kk = k + s * e2;
+                if (ii < 0 || ii >= p.nx || jj < 0 || jj >= p.ny || kk < 0 || kk >= p.nz)
+                    fv[s - 1] = w19(a) * p.rho0;  // ghost value
+                else
+                    fv[s - 1] = pabs<S>(f, a * P + (ii + (long long)p.nx * (jj + (long long)p.ny * kk)), a, p.rho0);
+            }
+            // 3 f(x+e) - 3 f(x+2e) + f(x+3e) (particle_update.F90:157-159)
+            fl[a] = __dadd_rn(__dsub_rn(__dmul_rn(3.0, fv[0]), __dmul_rn(3.0, fv[1])), fv[2]);
+        }
+        moments19d(fl, m);
+        const double x0 = X[0] + rx, y0 = (double)(j + 1), z0 = (double)(k + 1);
+        const double qx = x0 - X[0], qy = y0 - X[1], qz = z0 - X[2];
+        m[3] = s_ravg * (U[0] + (O[1] * qz - O[2] * qy));
+        m[5] = s_ravg * (U[1] + (O[2] * qx - O[0] * qz));
+        m[7] = s_ravg * (U[2] + (O[0] * qy - O[1] * qx));
+        inverse19d(m, fl);
+        const int slot = atomicAdd(&s_n, 1);
+        if (slot >= REFILL_MAX) {
+            atomicCAS(d.status, 0, PS_REFILL_FULL);
+            continue;
+        }
+        s_cell[slot] = cell;
+        for (int a = 0; a < Q19; a++) s_val[slot][a] = fl[a];
+    }
+    __syncthreads();
+    const int n = min(s_n, REFILL_MAX);
+    for (int t = threadIdx.x; t < n * Q19; t += PB) {
+        const int slot = t / Q19, a = t % Q19;
+        pset<S>(f, a * P + s_cell[slot], a, s_val[slot][a], p.rho0);
+    }
+    if (c == 0 && threadIdx.x == 0) {
+        long long cnt = d.n_fluid[0];
+        for (int q = 0; q < p.np; q++) cnt += d.prep_cnt[q];
+        d.n_fluid[1] = cnt;  // moved into slot 0 by k_pcommit
+    }
+}
+
+__global__ void k_pcommit(PartDev d) {
+    if (d.status[0]) return;
+    d.n_fluid[0] = d.n_fluid[1];
+}
+
+// ------------------------------------------------------------ initialise --
+template <typename S>
+__global__ void k_pinit_f(S* f, const int* owner, PartParams p) {
+    const long long P = (long long)p.nx * p.ny * p.nz;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < P;
+         c += (long long)gridDim.x * blockDim.x) {
+        const bool fluid = owner[c] < 0;
+        for (int q = 0; q < Q19; q++) pset<S>(f, q * P + c, q, fluid ? w19(q) * (1.0 + 0.0) : 0.0, p.rho0);
+    }
+}
+__global__ void k_pcount(const int* owner, long long n, long long* out) {
+    long long cnt = 0;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+         c += (long long)gridDim.x * blockDim.x)
+        cnt += owner[c] < 0;
+    double acc[1] = {(double)cnt};
+    __shared__ double o[1];
+    block_sum_to<1>(acc, o, 1);
+    if (threadIdx.x == 0) out[0] = llround(o[0]);
+}
+
+template <typename S>
+__global__ void k_pmacro(const S* f, const int* owner, PartParams p, bool first, double* rho,
+                         double* u, double* v, double* w) {
+    const long long P = (long long)p.nx * p.ny * p.nz;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < P;
+         c += (long long)gridDim.x * blockDim.x) {
+        if (owner[c] >= 0) {
+            rho[c] = p.rho_solid;
+            u[c] = v[c] = w[c] = 0.0;
+            continue;
+        }
+        if (first) {
+            rho[c] = p.rho0;
+            u[c] = v[c] = w[c] = 0.0;
+            continue;
+        }
+        double fq[Q19];
+        for (int q = 0; q < Q19; q++) fq[q] = pabs<S>(f, q * P + c, q, p.rho0);
+        double r = fq[0];
+        for (int q = 1; q < Q19; q++) r += fq[q];
+        double jx = 0.0, jy = 0.0, jz = 0.0;
+        for (int q = 1; q < Q19; q++) {
+            jx += ex19(q) * fq[q];
+            jy += ey19(q) * fq[q];
+            jz += ez19(q) * fq[q];
+        }
+        rho[c] = r;
+        u[c] = (jx + 0.5 * (r * p.body_force[0])) / r;
+        v[c] = (jy + 0.5 * (r * p.body_force[1])) / r;
+        w[c] = (jz + 0.5 * (r * p.body_force[2])) / r;
+    }
+}
+
+// ---------------------------------------------------------------- launch --
+static dim3 pblock(int nx) {
+    int bx = ((nx + 31) / 32) * 32;
+    return dim3(bx > 128 ? 128 : bx, 1, 1);
+}
+int particle_bulk_blocks(const PartParams& p) {
+    dim3 b = pblock(p.nx);
+    return ((p.nx + b.x - 1) / b.x) * p.ny * p.nz;
+}
+
+template <typename S>
+static cudaError_t pstep_go(bool first, const void* fin, void* fout, const PartParams& p,
+                            const PartDev& d, cudaStream_t s) {
+    dim3 b = pblock(p.nx), g((p.nx + b.x - 1) / b.x, p.ny, p.nz);
+    MrtCoef<typename PC<S>::C> cd = cast_coef<typename PC<S>::C>(make_mrt_coef(p.snu, p.sq));
+    if (first)
+        k_pbulk<S, true><<<g, b, 0, s>>>((const S*)fin, (S*)fout, d.owner_cur, p, cd, d.partials, d.status);
+    else
+        k_pbulk<S, false><<<g, b, 0, s>>>((const S*)fin, (S*)fout, d.owner_cur, p, cd, d.partials, d.status);
+    k_pfinish<<<1, 256, 0, s>>>(d, d.nblocks);
+    if (p.np > 0) {
+        k_plinks<S><<<p.np, PB, 0, s>>>((S*)fout, p, d);
+        k_pupdate<<<1, 256, 0, s>>>(p, d);
+    }
+    cudaError_t e = cudaMemsetAsync(d.owner_new, 0xFF, sizeof(int) * (size_t)p.nx * p.ny * p.nz, s);
+    if (e != cudaSuccess) return e;
+    if (p.np > 0) {
+        k_pmark<<<p.np, PB, 0, s>>>(d.owner_new, d.xc, p, d.status, true);
+        k_pprep<S><<<p.np, PB, 0, s>>>((const S*)fout, p, d);
+        k_prefill<S><<<p.np, PB, 0, s>>>((S*)fout, p, d, d.nblocks);
+        k_pcommit<<<1, 1, 0, s>>>(d);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_particle_step(int form, bool first, const void* fin, void* fout,
+                                 const PartParams& p, const PartDev& d, cudaStream_t s) {
+    if (form == FORM_FP64) return pstep_go<double>(first, fin, fout, p, d, s);
+    if (form == FORM_FP32) return pstep_go<float>(first, fin, fout, p, d, s);
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_particle_init(int form, void* f, const PartParams& p, const PartDev& d,
+                                 cudaStream_t s) {
+    const long long n = (long long)p.nx * p.ny * p.nz;
+    cudaError_t e = cudaMemsetAsync(d.owner_cur, 0xFF, sizeof(int) * (size_t)n, s);
+    if (e != cudaSuccess) return e;
+    if (p.np > 0) k_pmark<<<p.np, PB, 0, s>>>(d.owner_cur, d.xc, p, d.status, false);
+    int gb = (int)std::min<long long>((n + 255) / 256, 152 * 16);
+    if (form == FORM_FP64) k_pinit_f<double><<<gb, 256, 0, s>>>((double*)f, d.owner_cur, p);
+    else k_pinit_f<float><<<gb, 256, 0, s>>>((float*)f, d.owner_cur, p);
+    k_pcount<<<1, 1024, 0, s>>>(d.owner_cur, n, d.n_fluid);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_particle_macro(int form, bool first, const void* f, const PartParams& p,
+                                  const PartDev& d, double* rho, double* u, double* v, double* w,
+                                  cudaStream_t s) {
+    const long long n = (long long)p.nx * p.ny * p.nz;
+    int gb = (int)std::min<long long>((n + 255) / 256, 152 * 16);
+    if (form == FORM_FP64)
+        k_pmacro<double><<<gb, 256, 0, s>>>((const double*)f, d.owner_cur, p, first, rho, u, v, w);
+    else
+        k_pmacro<float><<<gb, 256, 0, s>>>((const float*)f, d.owner_cur, p, first, rho, u, v, w);
+    return cudaGetLastError();
+}
+
+}  // namespace mglc

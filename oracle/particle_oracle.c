@@ -676,6 +676,77 @@ static int cal_force(orc_particles* s) {
     return 0;
 }
 
+
+/* 3-D refill, two phases (see update_center) */
+static int refill3(orc_particles* s) {
+    const orc_pp* p = &s->p;
+    const int np = p->np;
+    size_t cap = 1024, nref = 0;
+    size_t* cells = (size_t*)malloc(cap * sizeof(size_t));
+    double* vals = (double*)malloc(cap * 23 * sizeof(double));
+    for (int k = 1; k <= p->nz; k++)
+        for (int j = 1; j <= p->ny; j++)
+            for (int i = 1; i <= p->nx; i++) {
+                if (!(OB_(i, j, k) == 1 && ON_(i, j, k) == 0)) continue;
+                int c = -1;
+                for (int cc = 0; cc < np; cc++)
+                    if (inside(s, cc, (double)i, (double)j, (double)k, s->xc_old)) { c = cc; break; }
+                if (c < 0) { free(cells); free(vals); return 1; }
+                double rx = dxp(s, (double)i, s->xc[3 * c]);
+                double ry = (double)j - s->xc[3 * c + 1];
+                double rz = (double)k - s->xc[3 * c + 2];
+                double out = 0.0;
+                int ec = 0;
+                for (int a = 1; a < 19; a++) {
+                    double t = (rx * s->ex[a] + ry * s->ey[a] + rz * s->ez[a]) / sqrt(rx * rx + ry * ry + rz * rz);
+                    if (t > out) { out = t; ec = a; }
+                }
+                if (ec == 0) { free(cells); free(vals); return 5; }
+                const int e0 = s->ex[ec], e1 = s->ey[ec], e2 = s->ez[ec];
+                double fl[19], m[19], rot[3];
+                for (int a = 0; a < 19; a++)
+                    fl[a] = 3.0 * F_(a, i + e0, j + e1, k + e2) - 3.0 * F_(a, i + 2 * e0, j + 2 * e1, k + 2 * e2) +
+                            F_(a, i + 3 * e0, j + 3 * e1, k + 3 * e2);
+                moments19(fl, m);
+                wall_rot(s, c, s->xc[3 * c] + rx, (double)j, (double)k, rot);
+                const double ra = s->rho_avg;
+                m[3] = ra * (s->uc[3 * c] + rot[0]);
+                m[5] = ra * (s->uc[3 * c + 1] + rot[1]);
+                m[7] = ra * (s->uc[3 * c + 2] + rot[2]);
+                inverse19(m, fl);
+                if (nref == cap) {
+                    cap *= 2;
+                    cells = (size_t*)realloc(cells, cap * sizeof(size_t));
+                    vals = (double*)realloc(vals, cap * 23 * sizeof(double));
+                }
+                cells[nref] = IX(s, i, j, k);
+                double r = 0.0, jx = 0.0, jy = 0.0, jz = 0.0;
+                for (int a = 0; a < 19; a++) {
+                    vals[nref * 23 + a] = fl[a];
+                    r = r + fl[a];
+                    jx = jx + fl[a] * s->ex[a];
+                    jy = jy + fl[a] * s->ey[a];
+                    jz = jz + fl[a] * s->ez[a];
+                }
+                vals[nref * 23 + 19] = r;
+                vals[nref * 23 + 20] = (jx + 0.5 * (r * p->body_force[0])) / r;
+                vals[nref * 23 + 21] = (jy + 0.5 * (r * p->body_force[1])) / r;
+                vals[nref * 23 + 22] = (jz + 0.5 * (r * p->body_force[2])) / r;
+                nref++;
+            }
+    for (size_t q = 0; q < nref; q++) {
+        size_t ix = cells[q];
+        for (int a = 0; a < 19; a++) s->f[(size_t)19 * ix + a] = vals[q * 23 + a];
+        s->rho[ix] = vals[q * 23 + 19];
+        s->u[ix] = vals[q * 23 + 20];
+        s->v[ix] = vals[q * 23 + 21];
+        s->w[ix] = vals[q * 23 + 22];
+    }
+    free(cells);
+    free(vals);
+    return 0;
+}
+
 /* particle_update.F90:26-206 */
 static int update_center(orc_particles* s) {
     const orc_pp* p = &s->p;
@@ -729,6 +800,17 @@ static int update_center(orc_particles* s) {
                     SC_(w, i, j, k) = 0.0;
                 }
     s->rho_avg = rho_average(s, s->obst_new);
+    /* refill nodes that left a particle (:134-193).  2-D: the reference's
+     * sequential loop.  3-D: two phases -- every refilled node is computed
+     * from the populations as they were before any refill of this step, then
+     * all are written -- so the result does not depend on the sweep order;
+     * u carries the half-force shift like macro(). */
+    if (p->dim == 3) {
+        int rc3 = refill3(s);
+        if (rc3) return rc3;
+        memcpy(s->obst, s->obst_new, sizeof(int) * (size_t)s->X * s->Y * s->Z);
+        return 0;
+    }
     /* refill nodes that left a particle (:134-193) */
     for (int k = 1; k <= kmax(s); k++)
         for (int j = 1; j <= p->ny; j++)
