@@ -40,7 +40,39 @@ WORKLOADS = {
                   desc="lid-driven cavity D3Q19 MRT 64^3 Re=400 U=0.1"),
     "thermal128": dict(kind="thermal", n=128, rayleigh=1e5, prandtl=0.71, mach=0.1,
                        desc="differentially heated cavity D3Q19+D3Q7 128^3 Ra=1e5 Pr=0.71"),
+    "particles": dict(kind="particle", n=(256, 128, 128), np=200, radius=5.0, ratio=1.2,
+                      body_force=1e-6, tauf=0.65, seed=2026,
+                      desc="particle-laden channel D3Q19 256x128x128, 200 spheres R=5, "
+                           "density ratio 1.2, body force 1e-6 along x, periodic x"),
 }
+
+
+def place_spheres(nx, ny, nz, npart, R, seed):
+    """Seeded rejection sampling: centre gap >= 2R+2, wall gap >= R+2."""
+    rng = np.random.default_rng(seed)
+    out = []
+    tries = 0
+    while len(out) < npart:
+        tries += 1
+        if tries > 200000:
+            raise RuntimeError("could not place the spheres")
+        c = np.array([rng.uniform(0.5, nx + 0.5), rng.uniform(R + 2 + 1, ny - R - 2),
+                      rng.uniform(R + 2 + 1, nz - R - 2)])
+        ok = True
+        for o in out:
+            d = c - o
+            d[0] -= nx * np.round(d[0] / nx)
+            if np.dot(d, d) < (2 * R + 2) ** 2:
+                ok = False
+                break
+        if ok:
+            out.append(c)
+    return np.array(out)
+
+
+def cells_of(wl):
+    n = wl["n"]
+    return n[0] * n[1] * n[2] if isinstance(n, tuple) else n ** 3
 
 
 def load_peaks():
@@ -121,6 +153,14 @@ class ClockSampler:
 
 def make_solve(mg, wl, form):
     n = wl["n"]
+    if wl["kind"] == "particle":
+        nx, ny, nz = n
+        cen = place_spheres(nx, ny, nz, wl["np"], wl["radius"], wl["seed"])
+        return mg.ParticleFlow(nx, ny, nz, cen, wl["radius"], tauf=wl["tauf"],
+                               rho_solid=wl["ratio"], periodic_x=True,
+                               body_force=(wl["body_force"], 0.0, 0.0), threshold_wall=2.0,
+                               threshold_particle=2.0, spring_scale_wall=1.0,
+                               spring_scale_particle=1.0, precision=form)
     if wl["kind"] == "lid":
         return mg.LidDrivenCavity(n, reynolds=wl["reynolds"], u0=wl["u0"], top_layer_u0=False,
                                   precision=form)
@@ -162,8 +202,10 @@ def time_e2e(torch, mg, wl, form, steps, dist=None):
     macroscopic fields -> pinned host, residual check."""
     s = make_solve(mg, wl, form)
     n = wl["n"]
-    cells = n ** 3
+    cells = cells_of(wl)
     q_g = 7 if wl["kind"] == "thermal" else 0
+    if wl["kind"] == "particle":  # state upload is not part of the particle API: time steps + readback
+        return time_e2e_particles(torch, s, wl, steps, dist)
     f_h = torch.empty((n, n, n, 19), dtype=torch.float64, pin_memory=True).numpy()
     g_h = torch.empty((n, n, n, 7), dtype=torch.float64, pin_memory=True).numpy() if q_g else None
     fields = [torch.empty((n, n, n), dtype=torch.float64, pin_memory=True).numpy()
@@ -202,12 +244,52 @@ def time_e2e(torch, mg, wl, form, steps, dist=None):
     return dt, h2d / steps, d2h / steps, float(eu.value)
 
 
+def time_e2e_particles(torch, s, wl, steps, dist=None):
+    import ctypes
+    from mglc_gb300 import capi
+    nx, ny, nz = wl["n"]
+    cells = nx * ny * nz
+    fields = [torch.empty((nz, ny, nx), dtype=torch.float64, pin_memory=True).numpy()
+              for _ in range(4)]
+    st = [np.zeros((wl["np"], 3)) for _ in range(5)]
+    L = capi.lib()
+    ptr = lambda a: a.ctypes.data
+    s.initial()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    capi.check(s.handle, L.mglc_step(s.handle, steps))
+    capi.check(s.handle, L.mglc_get_macros(s.handle, *[ptr(a) for a in fields], None))
+    capi.check(s.handle, L.mglc_particle_state(s.handle, *[ptr(a) for a in st]))
+    dt = time.perf_counter() - t0
+    s.close()
+    return dt, 0, (8 * 4 * cells + 8 * 15 * wl["np"]) / steps, 0.0
+
+
 def cpu_sample(wl, target_s=10.0):
     """The oracle (restatement of the reference's CPU code) with OpenMP on all
     host cores, on a bounded sample of the workload."""
     from oracle import oracle as O
     threads = os.cpu_count() or 1
     n = wl["n"]
+    if wl["kind"] == "particle":
+        # the particle oracle is single-threaded: time a 64x32x32 slice with 6 spheres
+        nx, ny, nz = 64, 32, 32
+        cen = place_spheres(nx, ny, nz, 6, wl["radius"], wl["seed"])
+        o = O.ParticleOracle(cen, dim=3, nx=nx, ny=ny, nz=nz, periodic_x=1, tauf=wl["tauf"],
+                             rho_solid=wl["ratio"], radius=wl["radius"],
+                             body_force=(wl["body_force"], 0.0, 0.0), threshold_wall=2.0,
+                             threshold_particle=2.0, spring_scale_wall=1.0,
+                             spring_scale_particle=1.0, qmode=1)
+        t0 = time.perf_counter()
+        o.step(2)
+        per = max((time.perf_counter() - t0) / 2, 1e-3)
+        k = int(max(2, min(50, target_s / per)))
+        t0 = time.perf_counter()
+        o.step(k)
+        dt = time.perf_counter() - t0
+        return {"value": nx * ny * nz * k / dt / 1e6, "unit": "MLUPS", "cores": 1, "kind": "port",
+                "sample": f"64x32x32 channel with 6 spheres R={wl['radius']}: {k} steps, particle "
+                          f"oracle (3-D generalisation of the reference's case4 loop), 1 thread"}
     if wl["kind"] == "lid":
         o = O.LidOracle(n, n, n, wl["reynolds"], wl["u0"], top_layer_u0=False)
         run = lambda k: o.run(k, nthreads=threads)
@@ -235,6 +317,17 @@ def reference_arm(args, wl):
     O.build()
     threads = os.cpu_count() or 1
     n = wl["n"]
+    if wl["kind"] == "particle":
+        cb = cpu_sample(wl, target_s=60.0)
+        line = {"impl": "reference", "metric": METRIC, "value": round(cb["value"], 3), "unit": "MLUPS",
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": {"workload": wl["desc"], "form": "fp64"},
+                "cpu_baseline": cb,
+                "e2e": {"value": round(cb["value"], 3), "unit": "MLUPS", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
     # size the per-step sample so that warmup+steps finish within ~150 s
     probe_n = min(n, 128)
     if wl["kind"] == "lid":
@@ -288,9 +381,11 @@ def main():
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     wl = dict(WORKLOADS[args.workload])
-    if args.n:
+    if args.n and wl["kind"] != "particle":
         wl["desc"] = wl["desc"].replace(f"{wl['n']}^3", f"{args.n}^3")
         wl["n"] = args.n
+    if wl["kind"] == "particle" and args.form == "fp64" and "--form" not in sys.argv:
+        args.form = "fp32"  # the channel workload is specified with FP32 arithmetic
 
     if args.impl == "reference":
         return reference_arm(args, wl)
@@ -309,7 +404,7 @@ def main():
     B.build()
     mglc_gb300.lib()
 
-    cells = wl["n"] ** 3
+    cells = cells_of(wl)
     peak, peak_kind = load_peaks()
     with ClockSampler(local) as clk:
         ms, info = time_device(torch, mglc_gb300, wl, args.form, args.steps, args.warmup, dist)
@@ -347,7 +442,7 @@ def main():
                                "+ mglc_check, wall clock"}
     if rank == 0 and not args.no_forms:
         forms = {}
-        for fm in ("fp64", "fp32", "fp16", "bf16"):
+        for fm in (("fp64", "fp32") if wl["kind"] == "particle" else ("fp64", "fp32", "fp16", "bf16")):
             if fm == args.form:
                 continue
             try:

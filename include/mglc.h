@@ -170,6 +170,60 @@ int mglc_nusselt(mglc_ctx* ctx, double* nu_vol, double* re_vol, double* nu_hot, 
 int mglc_get_macros_device(mglc_ctx* ctx, double* rho, double* u, double* v, double* w,
                            double* T);
 
+/* ---- solve server: continuous batching of cavity solves ------------------- */
+/* No counterpart in the reference (each reference run is one solve).  A
+ * server keeps many lid-driven and heated-cavity solves resident in a device
+ * arena of hbm_budget_bytes, admits arriving requests as slots and memory
+ * free up, advances all active solves together in one persistent tile-queue
+ * kernel per step (K steps per CUDA-graph replay), and retires each solve when
+ * max|u - u_prev|/U over the last K steps falls below tol or at max_steps.
+ * Lid solves: U = 0.1 on the top z plane, u = 0 initially.  Heated solves:
+ * Pr = 0.71, Ma = 0.1, walls at y = 1 / ny with T = +0.5 / -0.5, U = the
+ * free-fall velocity sqrt(g beta n). */
+typedef struct mglc_server mglc_server;
+typedef struct mglc_server_params {
+    long long hbm_budget_bytes; /* device arena for resident solves */
+    int max_active;             /* solve slots (<= 256) */
+    int precision;              /* MGLC_FP16, MGLC_BF16 or MGLC_FP32 storage of f */
+    int steps_per_iteration;    /* K (even): steps between admission/retirement points */
+    double tol;                 /* convergence threshold of max|du|/U */
+    long long max_steps;        /* step cap of one solve */
+    int autotune;               /* 1: time tile shapes on the first run and keep the fastest */
+    int keep_results;           /* 1: keep rho,u,v,w(,T) of each retired solve on the host */
+} mglc_server_params;
+typedef struct mglc_request {
+    int kind;         /* MGLC_KIND_LID or MGLC_KIND_THERMAL */
+    int n;            /* cubic grid, n^3 nodes */
+    double reynolds;  /* lid: Re based on n */
+    double rayleigh;  /* heated: Ra */
+    double arrival_s; /* arrival time, seconds after the first mglc_server_run */
+} mglc_request;
+typedef struct mglc_request_result {
+    long long id;
+    int kind, n;
+    long long steps;
+    double residual;
+    double arrival_s, admit_s, finish_s; /* seconds after the first mglc_server_run */
+    int converged;
+} mglc_request_result;
+typedef struct mglc_server_stats {
+    long long iterations, steps_total, cell_updates;
+    double wall_s, busy_s;
+    int tile_threads, tile_rows, ctas_per_sm; /* the tile shape in use */
+    long long peak_device_bytes;
+    int peak_active;
+} mglc_server_stats;
+int mglc_server_create(const mglc_server_params* p, mglc_server** out);
+void mglc_server_destroy(mglc_server* s);
+const char* mglc_server_last_error(const mglc_server* s);
+int mglc_server_submit(mglc_server* s, const mglc_request* r, long long* id);
+/* Serve until every submitted request has retired (or time_limit_s passes). */
+int mglc_server_run(mglc_server* s, double time_limit_s);
+int mglc_server_results(mglc_server* s, mglc_request_result* out, int max, int* count);
+/* rho, u, v, w (and T) planes of a retired request, n^3 floats each. */
+int mglc_server_get_field(mglc_server* s, long long id, float* out);
+int mglc_server_get_stats(mglc_server* s, mglc_server_stats* out);
+
 /* ---- no-allocation variant ----------------------------------------------- */
 /* No counterpart in the reference.  The residual of check() (errorU, and errorT
  * when T and Tp are given) over caller-owned DEVICE arrays of n cells, for

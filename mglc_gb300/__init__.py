@@ -6,5 +6,6 @@ Python host API that mirrors the reference's routines.
 """
 from .capi import FORMS, MglcError, lib  # noqa: F401
 from .cavity import BuoyancyCavity, LidDrivenCavity, ParticleFlow  # noqa: F401
+from .serve import SolveServer  # noqa: F401
 
-__all__ = ["LidDrivenCavity", "BuoyancyCavity", "ParticleFlow", "MglcError", "FORMS", "lib"]
+__all__ = ["LidDrivenCavity", "BuoyancyCavity", "ParticleFlow", "SolveServer", "MglcError", "FORMS", "lib"]

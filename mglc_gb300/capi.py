@@ -49,6 +49,27 @@ class Info(ctypes.Structure):
                 ("bytes_per_cell_step", _D), ("device_bytes", _LL)]
 
 
+class ServerParams(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", _LL), ("max_active", _I), ("precision", _I),
+                ("steps_per_iteration", _I), ("tol", _D), ("max_steps", _LL), ("autotune", _I),
+                ("keep_results", _I)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("kind", _I), ("n", _I), ("reynolds", _D), ("rayleigh", _D), ("arrival_s", _D)]
+
+
+class RequestResult(ctypes.Structure):
+    _fields_ = [("id", _LL), ("kind", _I), ("n", _I), ("steps", _LL), ("residual", _D),
+                ("arrival_s", _D), ("admit_s", _D), ("finish_s", _D), ("converged", _I)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("iterations", _LL), ("steps_total", _LL), ("cell_updates", _LL), ("wall_s", _D),
+                ("busy_s", _D), ("tile_threads", _I), ("tile_rows", _I), ("ctas_per_sm", _I),
+                ("peak_device_bytes", _LL), ("peak_active", _I)]
+
+
 # (name, argtypes, restype) of every exported symbol; tests check that the
 # library exports all of them
 SIGNATURES = {
@@ -70,6 +91,14 @@ SIGNATURES = {
     "mglc_check": ([_VP, _DP, _DP], _I),
     "mglc_totals": ([_VP, _DP, _DP, _DP], _I),
     "mglc_nusselt": ([_VP, _DP, _DP, _DP, _DP], _I),
+    "mglc_server_create": ([ctypes.POINTER(ServerParams), ctypes.POINTER(_VP)], _I),
+    "mglc_server_destroy": ([_VP], None),
+    "mglc_server_last_error": ([_VP], ctypes.c_char_p),
+    "mglc_server_submit": ([_VP, ctypes.POINTER(Request), ctypes.POINTER(_LL)], _I),
+    "mglc_server_run": ([_VP, _D], _I),
+    "mglc_server_results": ([_VP, _VP, _I, ctypes.POINTER(_I)], _I),
+    "mglc_server_get_field": ([_VP, _LL, _VP], _I),
+    "mglc_server_get_stats": ([_VP, ctypes.POINTER(ServerStats)], _I),
     "mglc_residual_noalloc": ([_LL, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _I, _VP, _DP, _DP,
                                ctypes.c_char_p, _I], _I),
 }

@@ -1,0 +1,199 @@
+// k_serve.cu -- kernels of the solve server.
+//
+// k_serve_step is a persistent kernel: a grid sized to the SM count pulls
+// tiles (rows_per_tile x-rows of one solve) from a queue shared by every
+// resident solve, through one atomic counter per step, and runs the fused
+// step of that solve on the tile's cells.  Small and large grids, lid and
+// heated cavities are mixed in one launch, so small solves no longer leave
+// the GPU idle.  The per-cell arithmetic is exactly that of the one-solve
+// kernels (step_cell.cuh), so a solve's result does not depend on which
+// other solves share the launch.
+#include "serve.cuh"
+
+namespace mglc {
+
+// solve that owns queue tile t (binary search over tile0)
+__device__ __forceinline__ int find_solve(const ServeTable* tab, int t) {
+    int lo = 0, hi = tab->n_active - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tab->s[mid].tile0 <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// grab the next tile for the whole CTA
+__device__ __forceinline__ int next_tile(unsigned* counter) {
+    __shared__ int s_tile;
+    __syncthreads();
+    if (threadIdx.x == 0) s_tile = (int)atomicAdd(counter, 1u);
+    __syncthreads();
+    return s_tile;
+}
+
+template <typename S>
+__global__ void k_serve_step(const ServeTable* __restrict__ tab, int parity, unsigned* counter) {
+    const int total = tab->total_tiles;
+    const int R = tab->rows_per_tile;
+    for (;;) {
+        const int t = next_tile(counter);
+        if (t >= total) break;
+        const ServeSolve& sv = tab->s[find_solve(tab, t)];
+        const int nx = sv.nx, ny = sv.ny, nz = sv.nz;
+        const int r0 = (t - sv.tile0) * R;
+        const int r1 = min(r0 + R, ny * nz);
+        const int ncell = (r1 - r0) * nx;
+        const S* fin = (const S*)sv.f[parity];
+        S* fout = (S*)sv.f[parity ^ 1];
+        for (int idx = threadIdx.x; idx < ncell; idx += blockDim.x) {
+            const int i = idx % nx, r = r0 + idx / nx;
+            const int j = r % ny, k = r / ny;
+            if (sv.kind == 1)
+                lid_cell<S, false, unsigned>(i, j, k, fin, fout, sv.K, sv.plane, nullptr, nullptr,
+                                             nullptr, nullptr);
+            else
+                thermal_cell<S, false, false, unsigned>(i, j, k, fin, fout, sv.g[parity],
+                                                        sv.g[parity ^ 1], sv.F, sv.K, sv.plane,
+                                                        nullptr, nullptr, nullptr, nullptr,
+                                                        nullptr, 0u);
+        }
+    }
+}
+
+// max |u - uprev| / uref per solve; uprev <- u
+template <typename S>
+__global__ void k_serve_resid(const ServeTable* __restrict__ tab, unsigned* counter,
+                              unsigned* resid) {
+    const int total = tab->total_tiles;
+    const int R = tab->rows_per_tile;
+    __shared__ float s_max[32];
+    for (;;) {
+        const int t = next_tile(counter);
+        if (t >= total) break;
+        const int si = find_solve(tab, t);
+        const ServeSolve& sv = tab->s[si];
+        const int nx = sv.nx, ny = sv.ny, nz = sv.nz;
+        const unsigned P = sv.plane;
+        const int r0 = (t - sv.tile0) * R;
+        const int r1 = min(r0 + R, ny * nz);
+        const int ncell = (r1 - r0) * nx;
+        const S* f = (const S*)sv.f[0];  // residual runs after an even number of steps
+        float m = 0.0f;
+        for (int idx = threadIdx.x; idx < ncell; idx += blockDim.x) {
+            const unsigned cell = (unsigned)(r0 * nx + idx);
+            float fq[Q19];
+#pragma unroll
+            for (int q = 0; q < Q19; q++) fq[q] = St<S>::ld(f + (q * P + cell), sv.K.inv_scale);
+            float rho_m, jx, jy, jz;
+            moments0(fq, rho_m, jx, jy, jz);
+            const float rho = 1.0f + rho_m;
+            if (sv.kind == 2) jz += 0.5f * sv.F[cell];
+            const float ux = jx / rho, uy = jy / rho, uz = jz / rho;
+            float d = fmaxf(fabsf(ux - sv.uprev[cell]),
+                            fmaxf(fabsf(uy - sv.uprev[P + cell]), fabsf(uz - sv.uprev[2 * P + cell])));
+            d = d / sv.uref;
+            if (!(d == d)) d = __int_as_float(0x7f800000);  // NaN -> inf: never converges
+            m = fmaxf(m, d);
+            sv.uprev[cell] = ux;
+            sv.uprev[P + cell] = uy;
+            sv.uprev[2 * P + cell] = uz;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+        if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = m;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float b = 0.0f;
+            for (int w = 0; w < (int)(blockDim.x + 31) / 32; w++) b = fmaxf(b, s_max[w]);
+            atomicMax(resid + si, __float_as_uint(b));
+        }
+    }
+}
+
+template <typename S>
+__global__ void k_serve_init(ServeSolve sv, float t_hot, float t_cold) {
+    const unsigned P = sv.plane;
+    for (unsigned c = blockIdx.x * blockDim.x + threadIdx.x; c < P; c += gridDim.x * blockDim.x) {
+        S* f = (S*)sv.f[0];
+#pragma unroll
+        for (int q = 0; q < Q19; q++) St<S>::st(f + (q * P + c), 0.0f, 1.0f);  // f = w (rho = 1, u = 0)
+        sv.uprev[c] = 0.0f;
+        sv.uprev[P + c] = 0.0f;
+        sv.uprev[2 * P + c] = 0.0f;
+        if (sv.kind == 2) {
+            const int j = (int)((c / sv.nx) % sv.ny);
+            const float T = j == 0 ? t_hot : (j == sv.ny - 1 ? t_cold : 0.0f);
+            const float a = sv.K.para_a;
+            const float w0 = (1.0f - a) / 7.0f, wi = (a + 6.0f) / 42.0f;
+            float* g = sv.g[0];
+            g[c] = w0 * T;
+#pragma unroll
+            for (int q = 1; q < Q7; q++) g[q * P + c] = wi * T;
+            sv.F[c] = 0.0f;
+        }
+    }
+}
+
+template <typename S>
+__global__ void k_serve_fields(ServeSolve sv, float* out) {
+    const unsigned P = sv.plane;
+    for (unsigned c = blockIdx.x * blockDim.x + threadIdx.x; c < P; c += gridDim.x * blockDim.x) {
+        const S* f = (const S*)sv.f[0];
+        float fq[Q19];
+#pragma unroll
+        for (int q = 0; q < Q19; q++) fq[q] = St<S>::ld(f + (q * P + c), sv.K.inv_scale);
+        float rho_m, jx, jy, jz;
+        moments0(fq, rho_m, jx, jy, jz);
+        const float rho = 1.0f + rho_m;
+        if (sv.kind == 2) jz += 0.5f * sv.F[c];
+        out[c] = rho;
+        out[P + c] = jx / rho;
+        out[2 * P + c] = jy / rho;
+        out[3 * P + c] = jz / rho;
+        if (sv.kind == 2) {
+            const float* g = sv.g[0];
+            out[4 * P + c] = ((g[c] + g[P + c]) + (g[2 * P + c] + g[3 * P + c])) +
+                             ((g[4 * P + c] + g[5 * P + c]) + g[6 * P + c]);
+        }
+    }
+}
+
+cudaError_t launch_serve_step(int form, const ServeTable* tab, int parity, unsigned* counter,
+                              int grid, int block, cudaStream_t st) {
+    if (form == FORM_FP16) k_serve_step<__half><<<grid, block, 0, st>>>(tab, parity, counter);
+    else if (form == FORM_FP32) k_serve_step<float><<<grid, block, 0, st>>>(tab, parity, counter);
+    else if (form == FORM_BF16) k_serve_step<__nv_bfloat16><<<grid, block, 0, st>>>(tab, parity, counter);
+    else return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_serve_resid(int form, const ServeTable* tab, unsigned* counter,
+                               unsigned* resid, int grid, int block, cudaStream_t st) {
+    if (form == FORM_FP16) k_serve_resid<__half><<<grid, block, 0, st>>>(tab, counter, resid);
+    else if (form == FORM_FP32) k_serve_resid<float><<<grid, block, 0, st>>>(tab, counter, resid);
+    else if (form == FORM_BF16) k_serve_resid<__nv_bfloat16><<<grid, block, 0, st>>>(tab, counter, resid);
+    else return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_serve_init(int form, const ServeSolve& s, double t_hot, double t_cold,
+                              cudaStream_t st) {
+    const int grid = (int)std::min<unsigned>((s.plane + 255) / 256, 152 * 8);
+    if (form == FORM_FP16) k_serve_init<__half><<<grid, 256, 0, st>>>(s, (float)t_hot, (float)t_cold);
+    else if (form == FORM_FP32) k_serve_init<float><<<grid, 256, 0, st>>>(s, (float)t_hot, (float)t_cold);
+    else if (form == FORM_BF16) k_serve_init<__nv_bfloat16><<<grid, 256, 0, st>>>(s, (float)t_hot, (float)t_cold);
+    else return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_serve_fields(int form, const ServeSolve& s, float* out, cudaStream_t st) {
+    const int grid = (int)std::min<unsigned>((s.plane + 255) / 256, 152 * 8);
+    if (form == FORM_FP16) k_serve_fields<__half><<<grid, 256, 0, st>>>(s, out);
+    else if (form == FORM_FP32) k_serve_fields<float><<<grid, 256, 0, st>>>(s, out);
+    else if (form == FORM_BF16) k_serve_fields<__nv_bfloat16><<<grid, 256, 0, st>>>(s, out);
+    else return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
+}  // namespace mglc

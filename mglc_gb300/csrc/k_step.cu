@@ -14,258 +14,32 @@
 //   thermal: bouyancy3d_mpi.F90 collision :641-864, streaming :867-892,
 //            bounceback :895-983, collisionT :1014-1070, streamingT :1073-1098,
 //            bouncebackT :1101-1210, macro :986-1010, macroT :1215-1231
-#include <cuda_bf16.h>
-#include <cuda_fp16.h>
-
-#include "kernels.cuh"
+#include "step_cell.cuh"
 
 namespace mglc {
 
-// ---------------------------------------------------------------- storage --
-template <typename S>
-struct St;
-template <>
-struct St<double> {
-    using C = double;
-    static constexpr bool SHIFT = false;
-    __device__ static C ld(const double* p, float) { return __ldg(p); }
-    __device__ static void st(double* p, C v, float) { *p = v; }
-};
-template <>
-struct St<float> {
-    using C = float;
-    static constexpr bool SHIFT = true;
-    __device__ static C ld(const float* p, float) { return __ldg(p); }
-    __device__ static void st(float* p, C v, float) { *p = v; }
-};
-template <>
-struct St<__half> {
-    using C = float;
-    static constexpr bool SHIFT = true;
-    __device__ static C ld(const __half* p, float inv) { return __half2float(__ldg(p)) * inv; }
-    __device__ static void st(__half* p, C v, float sc) { *p = __float2half_rn(v * sc); }
-};
-template <>
-struct St<__nv_bfloat16> {
-    using C = float;
-    static constexpr bool SHIFT = true;
-    __device__ static C ld(const __nv_bfloat16* p, float inv) {
-        return __bfloat162float(__ldg(p)) * inv;
-    }
-    __device__ static void st(__nv_bfloat16* p, C v, float sc) { *p = __float2bfloat16_rn(v * sc); }
-};
-
-// Reciprocal of the density (rho is within a few percent of 1 in every
-// cavity flow).  FP32: the hardware reciprocal.  FP64: Newton-Raphson
-// refinement r <- r + r(1 - x r) of a single-precision seed; two steps take
-// the 2^-23 seed error below 2^-52 with four FP64 FMAs, about half the FP64
-// work of an IEEE division.
-__device__ __forceinline__ float recip(float x) { return __frcp_rn(x); }
-__device__ __forceinline__ double recip(double x) {
-    double r = (double)__frcp_rn((float)x);
-    double e = fma(-x, r, 1.0);
-    r = fma(r, e, r);
-    e = fma(-x, r, 1.0);
-    return fma(r, e, r);
-}
-
-// Scalar constants converted once on the host to the arithmetic type.
-template <typename C>
-struct StepK {
-    int nx, ny, nz;
-    C u0, rho0;
-    float scale, inv_scale;
-    MrtCoef<C> c;
-    // thermal
-    C gbeta, omega_rot, t_ref, para_a, qd, qnu, chot, ccold;
-    int bc_y, bc_z;
-};
-
-template <typename C>
-static StepK<C> make_k(const Geom& g, const MrtCoef<double>& cd, double u0, double rho0,
-                       float scale, float inv_scale) {
-    StepK<C> k{};
-    k.nx = g.nx; k.ny = g.ny; k.nz = g.nz;
-    k.u0 = (C)u0; k.rho0 = (C)rho0;
-    k.scale = scale; k.inv_scale = inv_scale;
-    k.c = cast_coef<C>(cd);
-    return k;
-}
-
-// Face mask of a cell: bit 0/1 = low/high x face, 2/3 = y, 4/5 = z.
-__device__ __forceinline__ unsigned face_mask(int i, int j, int k, int nx, int ny, int nz) {
-    return (unsigned)(i == 0) | ((unsigned)(i == nx - 1) << 1) | ((unsigned)(j == 0) << 2) |
-           ((unsigned)(j == ny - 1) << 3) | ((unsigned)(k == 0) << 4) |
-           ((unsigned)(k == nz - 1) << 5);
-}
-// does direction (dx,dy,dz) leave the domain from a cell with face mask m
-__host__ __device__ constexpr unsigned leave_bits(int dx, int dy, int dz) {
-    return (dx < 0 ? 1u : 0u) | (dx > 0 ? 2u : 0u) | (dy < 0 ? 4u : 0u) | (dy > 0 ? 8u : 0u) |
-           (dz < 0 ? 16u : 0u) | (dz > 0 ? 32u : 0u);
-}
-
-// ------------------------------------------------------------ lid kernel --
-// IDX: 32-bit element indices when Q*cells < 2^31, 64-bit otherwise.
 template <typename S, bool FIRST, typename IDX>
 __global__ void __launch_bounds__(128)
     k_lid_step(const S* __restrict__ fin, S* __restrict__ fout, StepK<typename St<S>::C> K,
                IDX P, const double* __restrict__ mrho, const double* __restrict__ mu,
                const double* __restrict__ mv, const double* __restrict__ mw) {
-    using C = typename St<S>::C;
-    const int nx = K.nx, ny = K.ny, nz = K.nz;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y, k = blockIdx.z;
-    if (i >= nx) return;
-    const IDX cell = (IDX)i + (IDX)nx * ((IDX)j + (IDX)ny * (IDX)k);
-    C f[Q19];
-#pragma unroll
-    for (int q = 0; q < Q19; q++) f[q] = St<S>::ld(fin + ((IDX)q * P + cell), K.inv_scale);
-    C rho_m, rho, ux, uy, uz;
-    if (FIRST) {
-        rho = (C)mrho[cell];
-        ux = (C)mu[cell];
-        uy = (C)mv[cell];
-        uz = (C)mw[cell];
-        rho_m = St<S>::SHIFT ? rho - K.rho0 : rho;
-    } else {
-        C jx, jy, jz;
-        moments0(f, rho_m, jx, jy, jz);
-        rho = St<S>::SHIFT ? K.rho0 + rho_m : rho_m;
-        const C inv = recip(rho);
-        ux = jx * inv;
-        uy = jy * inv;
-        uz = jz * inv;
-    }
-    mrt_collide<C, false, true>(f, rho_m, rho, ux, uy, uz, C(0), C(0), C(0), K.c);
-    const IDX sy = (IDX)nx, sz = (IDX)nx * (IDX)ny;
-    const unsigned bm = face_mask(i, j, k, nx, ny, nz);
-    if (bm == 0) {  // interior cell: every population streams
-#pragma unroll
-        for (int q = 0; q < Q19; q++) {
-            const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
-            St<S>::st(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), f[q],
-                      K.scale);
-        }
-        return;
-    }
-    // moving lid: f(14) = f_post(11) - rho/6*U0, f(13) = f_post(12) + rho/6*U0
-    // (bounce_back.f90:77-78); the lid face is written last, so it wins on edges
-    C lid = C(0);
-    if (k == nz - 1) lid = rho / C(6) * K.u0;
-#pragma unroll
-    for (int q = 0; q < Q19; q++) {
-        const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
-        if ((bm & leave_bits(dx, dy, dz)) == 0) {
-            St<S>::st(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), f[q],
-                      K.scale);
-        } else {
-            C val = f[q];
-            if (dz > 0 && dx != 0) val = val - C(dx) * lid;
-            St<S>::st(fout + ((IDX)opp19(q) * P + cell), val, K.scale);
-        }
-    }
+    if (i >= K.nx) return;
+    lid_cell<S, FIRST, IDX>(i, blockIdx.y, blockIdx.z, fin, fout, K, P, mrho, mu, mv, mw);
 }
 
-// -------------------------------------------------------- thermal kernel --
-// Temperature populations are kept in the arithmetic type (FP64, or FP32 for
-// the reduced forms): g_0 ~ 0.7 T has a 16-bit ulp (~2e-4) far above the
-// per-step diffusive increments, so 16-bit g would stagnate.
 template <typename S, bool FIRST, bool ROT, typename IDX>
 __global__ void __launch_bounds__(128)
     k_thermal_step(const S* __restrict__ fin, S* __restrict__ fout,
                    const typename St<S>::C* __restrict__ gin, typename St<S>::C* __restrict__ gout,
-                   typename St<S>::C* __restrict__ F,
-                   StepK<typename St<S>::C> K, IDX P, const double* __restrict__ mrho,
-                   const double* __restrict__ mu, const double* __restrict__ mv,
-                   const double* __restrict__ mw, const double* __restrict__ mT) {
-    using C = typename St<S>::C;
-    const int nx = K.nx, ny = K.ny, nz = K.nz;
+                   typename St<S>::C* __restrict__ F, StepK<typename St<S>::C> K, IDX P,
+                   const double* __restrict__ mrho, const double* __restrict__ mu,
+                   const double* __restrict__ mv, const double* __restrict__ mw,
+                   const double* __restrict__ mT) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y, k = blockIdx.z;
-    if (i >= nx) return;
-    const IDX cell = (IDX)i + (IDX)nx * ((IDX)j + (IDX)ny * (IDX)k);
-    C f[Q19], g[Q7];
-#pragma unroll
-    for (int q = 0; q < Q19; q++) f[q] = St<S>::ld(fin + ((IDX)q * P + cell), K.inv_scale);
-#pragma unroll
-    for (int q = 0; q < Q7; q++) g[q] = gin[(IDX)q * P + cell];
-    C rho_m, rho, ux, uy, uz, temp;
-    if (FIRST) {
-        rho = (C)mrho[cell];
-        ux = (C)mu[cell];
-        uy = (C)mv[cell];
-        uz = (C)mw[cell];
-        temp = (C)mT[cell];
-        rho_m = St<S>::SHIFT ? rho - K.rho0 : rho;
-    } else {
-        C jx, jy, jz;
-        moments0(f, rho_m, jx, jy, jz);
-        rho = St<S>::SHIFT ? K.rho0 + rho_m : rho_m;
-        const C inv = recip(rho);
-        // u^n = (sum f e + F^n/2)/rho^n with the force carried from the previous step
-        C fxp = C(0), fyp = C(0);
-        if (ROT) {
-            fxp = F[cell];
-            fyp = F[P + cell];
-        }
-        const C fzp = F[(IDX)2 * P + cell];
-        ux = (jx + C(0.5) * fxp) * inv;
-        uy = (jy + C(0.5) * fyp) * inv;
-        uz = (jz + C(0.5) * fzp) * inv;
-        temp = ((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + g[6]);
-    }
-    // body force from (rho,u,T) of the previous macro (bouyancy3d_mpi.F90:743-745)
-    C fx = C(0), fy = C(0);
-    if (ROT) {
-        fx = C(-2) * rho * uy * K.omega_rot;
-        fy = C(2) * rho * ux * K.omega_rot;
-        F[cell] = fx;
-        F[P + cell] = fy;
-    }
-    const C fz = rho * K.gbeta * (temp - K.t_ref);
-    F[(IDX)2 * P + cell] = fz;
-    mrt_collide<C, true, false>(f, rho_m, rho, ux, uy, uz, fx, fy, fz, K.c);
-    mrt_collide_t<C>(g, temp, ux, uy, uz, K.para_a, K.qd, K.qnu);
-
-    const IDX sy = (IDX)nx, sz = (IDX)nx * (IDX)ny;
-    const unsigned bm = face_mask(i, j, k, nx, ny, nz);
-    if (bm == 0) {
-#pragma unroll
-        for (int q = 0; q < Q19; q++) {
-            const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
-            St<S>::st(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), f[q],
-                      K.scale);
-        }
-#pragma unroll
-        for (int q = 0; q < Q7; q++) {
-            const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
-            gout[(IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz] = g[q];
-        }
-        return;
-    }
-#pragma unroll
-    for (int q = 0; q < Q19; q++) {
-        const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
-        if ((bm & leave_bits(dx, dy, dz)) == 0)
-            St<S>::st(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), f[q],
-                      K.scale);
-        else
-            St<S>::st(fout + ((IDX)opp19(q) * P + cell), f[q], K.scale);
-    }
-    // D3Q7: adiabatic walls reflect, constant-T walls anti-bounce-back
-    // g_in = -g_out + (6+paraA)/21 * T_wall (bouyancy3d_mpi.F90:1101-1210)
-#pragma unroll
-    for (int q = 0; q < Q7; q++) {
-        const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
-        if ((bm & leave_bits(dx, dy, dz)) == 0) {
-            gout[(IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz] = g[q];
-        } else {
-            C val = g[q];
-            if (dy != 0 && K.bc_y) val = -val + (dy < 0 ? K.chot : K.ccold);
-            if (dz != 0 && K.bc_z) val = -val + (dz < 0 ? K.chot : K.ccold);
-            gout[(IDX)opp19(q) * P + cell] = val;
-        }
-    }
+    if (i >= K.nx) return;
+    thermal_cell<S, FIRST, ROT, IDX>(i, blockIdx.y, blockIdx.z, fin, fout, gin, gout, F, K, P,
+                                     mrho, mu, mv, mw, mT, (IDX)2 * P);
 }
 
 // --------------------------------------------------------------- launch --
