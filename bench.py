@@ -265,6 +265,66 @@ def time_e2e_particles(torch, s, wl, steps, dist=None):
     return dt, 0, (8 * 4 * cells + 8 * 15 * wl["np"]) / steps, 0.0
 
 
+def serve_bench(torch, mg, n_req=24, rate=50.0, seed=1234, max_steps=2000, tol=1e-6, K=100,
+                precision="fp16"):
+    """Batched serving stream: Poisson arrivals of lid-driven and heated-cavity
+    solves (grids from {32,48,64,96,128}, Re ~ U[100,1000] or Ra log-uniform in
+    [1e3,1e5]), each run to max|du|/U < tol or max_steps, through the solve
+    server; then the same requests run one at a time with the FP64 plain
+    context (and with the FP16 context) for the same step counts."""
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
+    arrivals -= arrivals[0]
+    sizes = rng.choice([32, 48, 64, 96, 128], n_req)
+    lid = rng.random(n_req) < 0.5
+    re = rng.uniform(100.0, 1000.0, n_req)
+    ra = 10.0 ** rng.uniform(3.0, 5.0, n_req)
+    with mg.SolveServer(hbm_budget_gb=32.0, max_active=64, precision=precision,
+                        steps_per_iteration=K, tol=tol, max_steps=max_steps, autotune=True,
+                        keep_results=False) as srv:
+        ids = [srv.submit("lid" if lid[q] else "thermal", int(sizes[q]), reynolds=float(re[q]),
+                          rayleigh=float(ra[q]), arrival_s=float(arrivals[q])) for q in range(n_req)]
+        srv.run()
+        res = {r["id"]: r for r in srv.results()}
+        st = srv.stats()
+    lat = np.array([(res[i]["finish_s"] - res[i]["arrival_s"]) * 1e3 for i in ids])
+    span = max(r["finish_s"] for r in res.values()) - float(arrivals[0])
+    cells_done = st["cell_updates"]
+
+    def serial(form):
+        tot = 0.0
+        for q, i in enumerate(ids):
+            n = int(sizes[q])
+            c = (mg.LidDrivenCavity(n, reynolds=float(re[q]), u0=0.1, top_layer_u0=False,
+                                    precision=form) if lid[q] else
+                 mg.BuoyancyCavity(n, rayleigh=float(ra[q]), t_hot=0.5, t_cold=-0.5, precision=form))
+            c.initial()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            c.step(int(res[i]["steps"]))
+            torch.cuda.synchronize()
+            tot += time.perf_counter() - t0
+            c.close()
+        return tot
+
+    t_plain = serial("fp64")
+    t_fp16 = serial("fp16")
+    agg = cells_done / span / 1e6
+    return {"requests": n_req, "rate_per_s": rate, "seed": seed, "max_steps": max_steps,
+            "tol": tol, "steps_per_iteration": K, "precision": precision,
+            "converged": int(sum(r["converged"] for r in res.values())),
+            "p50_ms": round(float(np.percentile(lat, 50)), 2),
+            "p99_ms": round(float(np.percentile(lat, 99)), 2),
+            "aggregate_mlups": round(agg, 1),
+            "busy_mlups": round(cells_done / st["busy_s"] / 1e6, 1),
+            "serial_plain_fp64_mlups": round(cells_done / t_plain / 1e6, 1),
+            "serial_fp16_mlups": round(cells_done / t_fp16 / 1e6, 1),
+            "speedup_vs_serial_plain": round(agg / (cells_done / t_plain / 1e6), 2),
+            "peak_active": st["peak_active"], "peak_device_bytes": st["peak_device_bytes"],
+            "tile": {"threads": st["tile_threads"], "rows": st["tile_rows"],
+                     "ctas_per_sm": st["ctas_per_sm"]}}
+
+
 def cpu_sample(wl, target_s=10.0):
     """The oracle (restatement of the reference's CPU code) with OpenMP on all
     host cores, on a bounded sample of the workload."""
@@ -378,6 +438,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--n", type=int, default=0, help="override the cube size (profiling runs)")
+    ap.add_argument("--no-serve", action="store_true", help="skip the batched-serving stream")
+    ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--serve-max-steps", type=int, default=2000)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     wl = dict(WORKLOADS[args.workload])
@@ -455,6 +518,9 @@ def main():
             except Exception as e:  # report, never hide
                 forms[fm] = {"error": str(e)}
         line["forms"] = forms
+    if rank == 0 and not args.no_serve and wl["kind"] == "lid":
+        line["serve"] = serve_bench(torch, mglc_gb300, n_req=args.serve_requests,
+                                    max_steps=args.serve_max_steps)
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_sample(wl)
     if rank == 0:

@@ -31,15 +31,16 @@ def lid_ref(mg):
         return np.stack(c.macro()[1:4])
 
 
-@pytest.mark.parametrize("form,tol", [("fp32", 1e-6), ("fp16", 1e-3), ("bf16", 5e-2)])
-def test_lid_forms_velocity_error(mg, lid_ref, form, tol):
+@pytest.mark.parametrize("form,tol,tmass", [("fp32", 1e-6, 1e-6), ("fp16", 1e-3, 1e-4),
+                                            ("bf16", 5e-2, 1e-3)])
+def test_lid_forms_velocity_error(mg, lid_ref, form, tol, tmass):
     with mg.LidDrivenCavity(64, reynolds=400.0, u0=0.1, top_layer_u0=False, precision=form) as c:
         c.initial()
         c.step(2000)
         U = np.stack(c.macro()[1:4])
         m, _, _ = c.totals()
     assert rel_l2(U, lid_ref) <= tol
-    assert abs(m / 64 ** 3 - 1.0) < 1e-4  # mass kept by the deviation storage
+    assert abs(m / 64 ** 3 - 1.0) < tmass  # mass drift from rounding the stored deviations
 
 
 @pytest.fixture(scope="module")
