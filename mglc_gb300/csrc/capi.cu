@@ -716,14 +716,18 @@ int mglc_particle_create(const mglc_particle_params* p, const double* centers, i
     if ((rc = dalloc(c, (void**)&d.owner_cur, n * sizeof(int), "owner mask"))) return rc;
     if ((rc = dalloc(c, (void**)&d.owner_new, n * sizeof(int), "owner mask"))) return rc;
     const size_t v3 = sizeof(double) * 3 * (size_t)(np > 0 ? np : 1);
-    double** p3[] = {&d.xc, &d.uc, &d.om, &d.xc_old, &d.uc_old, &d.om_old, &d.flink, &d.tlink, &d.ftot, &d.ttot};
+    double** p3[] = {&d.xc, &d.uc, &d.om, &d.xc_old, &d.uc_old, &d.om_old, &d.ftot, &d.ttot};
     for (double** a : p3)
         if ((rc = dalloc(c, (void**)a, v3, "particle state"))) return rc;
-    if ((rc = dalloc(c, (void**)&d.corr, v3 / 3, "particle sums"))) return rc;
+    // per-particle, per-slab partial sums of the boundary-link kernel
+    if ((rc = dalloc(c, (void**)&d.flink, PART_NSLAB * v3, "link sums"))) return rc;
+    if ((rc = dalloc(c, (void**)&d.tlink, PART_NSLAB * v3, "link sums"))) return rc;
+    if ((rc = dalloc(c, (void**)&d.corr, PART_NSLAB * v3 / 3, "link sums"))) return rc;
     if ((rc = dalloc(c, (void**)&d.prep_sum, v3 / 3, "particle sums"))) return rc;
     if ((rc = dalloc(c, (void**)&d.prep_cnt, sizeof(int) * (size_t)(np > 0 ? np : 1), "particle sums"))) return rc;
     d.nblocks = particle_bulk_blocks(pp);
-    if ((rc = dalloc(c, (void**)&d.partials, sizeof(double) * 2 * (size_t)d.nblocks, "bulk partials"))) return rc;
+    // bulk partials (2 per block) and the 2 x 32 stage-two sums of the finish kernel
+    if ((rc = dalloc(c, (void**)&d.partials, sizeof(double) * (2 * (size_t)d.nblocks + 64), "bulk partials"))) return rc;
     if ((rc = dalloc(c, (void**)&d.n_fluid, 2 * sizeof(long long), "fluid count"))) return rc;
     if ((rc = dalloc(c, (void**)&d.rho_avg, 4 * sizeof(double), "average density"))) return rc;
     if ((rc = dalloc(c, (void**)&d.status, 3 * sizeof(int), "particle status"))) return rc;

@@ -8,7 +8,7 @@
 //               solid cells do nothing.  Block partials of sum rho and of
 //               the post-collision mass feed the average density.
 //   k_pfinish   fixed-order sums -> rho_avg (particle_bounceback.F90:15-35)
-//   k_plinks    one CTA per particle: every fluid node x with a neighbour
+//   k_plinks    PART_NSLAB CTAs per particle: every fluid node x with a neighbour
 //               x+e inside the particle is a boundary link.  The
 //               post-collision values the quadratic interpolated bounce-back
 //               needs (particle_bounceback.F90:65-75) are read from the
@@ -16,8 +16,9 @@
 //               (including solid destination cells, which only fluid pushes
 //               write).  Writes f(abar,x) and accumulates the Wen 2014
 //               momentum exchange (particle_force.F90:59-66) in FP64.
-//   k_pupdate   one CTA: springs, gravity, body force, explicit update
-//               (particle_force.F90:96-190, particle_update.F90:26-50).
+//   k_pforce    one warp per particle: springs, gravity, body force
+//               (particle_force.F90:96-190)
+//   k_pmove     explicit update (particle_update.F90:26-50)
 //   k_pmark     new owner mask from the new centres (particle_update.F90:80-93)
 //   k_pprep     density bookkeeping of nodes that change phase
 //   k_prefill   refill of nodes that left a particle (:134-193), two phases
@@ -34,6 +35,7 @@
 namespace mglc {
 
 constexpr int PB = 256;             // threads of the per-particle kernels
+constexpr int NSLAB = PART_NSLAB;   // CTAs per particle in k_plinks
 constexpr int REFILL_MAX = 256;     // refilled nodes one particle may produce per step
 
 template <typename S>
@@ -118,7 +120,7 @@ __global__ void __launch_bounds__(128)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y, k = blockIdx.z;
     const long long P = (long long)nx * ny * nz;
-    double acc[2] = {0.0, 0.0};
+    C cacc[2] = {C(0), C(0)};  // per-cell sums in the arithmetic type, widened per warp
     const bool active = i < nx;
     const long long cell = (long long)i + (long long)nx * (j + (long long)ny * k);
     if (active && owner[cell] < 0) {
@@ -141,12 +143,13 @@ __global__ void __launch_bounds__(128)
             uy = (jy + C(0.5) * (rho * ay)) / rho;
             uz = (jz + C(0.5) * (rho * az)) / rho;
         }
-        acc[0] = (double)rho;
+        // deviation storage sums deviations (rho0 added back per warp)
+        cacc[0] = DEV ? rho_m : rho;
         mrt_collide<C, true, false>(f, rho_m, rho, ux, uy, uz, rho * ax, rho * ay, rho * az, cd);
-        double m = DEV ? p.rho0 : 0.0;
+        C m = C(0);
 #pragma unroll
-        for (int q = 0; q < Q19; q++) m += (double)f[q];
-        acc[1] = m;
+        for (int q = 0; q < Q19; q++) m += f[q];
+        cacc[1] = m;
         const long long sy = nx, sz = (long long)nx * ny;
 #pragma unroll
         for (int q = 0; q < Q19; q++) {
@@ -161,49 +164,129 @@ __global__ void __launch_bounds__(128)
             }
         }
     }
-    const int b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-    block_sum_to<2>(acc, partials + b, (int)(gridDim.x * gridDim.y * gridDim.z));
+#pragma unroll
+    for (int q = 0; q < 2; q++)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) cacc[q] += __shfl_down_sync(0xffffffffu, cacc[q], o);
+    // fluid cells of this warp (deviation storage adds rho0 for each of them)
+    const unsigned fl = __ballot_sync(0xffffffffu, active && owner[active ? cell : 0] < 0);
+    // FP64 only for the warp leaders: one value per warp, then thread 0 adds the warps
+    __shared__ double s_w[2][4];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) {
+        const double nf = DEV ? (double)__popc(fl) * p.rho0 : 0.0;
+        s_w[0][wid] = (double)cacc[0] + nf;
+        s_w[1][wid] = (double)cacc[1] + nf;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+        const int nb = gridDim.x * gridDim.y * gridDim.z, nw = (blockDim.x + 31) >> 5;
+        double a0 = 0.0, a1 = 0.0;
+        for (int q = 0; q < nw; q++) {
+            a0 += s_w[0][q];
+            a1 += s_w[1][q];
+        }
+        partials[b] = a0;
+        partials[nb + b] = a1;
+    }
 }
 
+constexpr int FINISH_BLOCKS = 32;
+
+// stage 1: FINISH_BLOCKS contiguous ranges of the bulk partials
 __global__ void k_pfinish(PartDev d, int nblocks) {
     if (d.status[0]) return;
+    const int per = (nblocks + FINISH_BLOCKS - 1) / FINISH_BLOCKS;
+    const int b0 = blockIdx.x * per, b1 = min(nblocks, b0 + per);
     double acc[2] = {0.0, 0.0};
-    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+    for (int b = b0 + threadIdx.x; b < b1; b += blockDim.x) {
         acc[0] += d.partials[b];
         acc[1] += d.partials[nblocks + b];
     }
     __shared__ double out[2];
     block_sum_to<2>(acc, out, 1);
     if (threadIdx.x == 0) {
-        d.rho_avg[0] = out[0] / (double)d.n_fluid[0];
-        d.rho_avg[2] = out[1];
+        d.partials[2 * nblocks + blockIdx.x] = out[0];
+        d.partials[2 * nblocks + FINISH_BLOCKS + blockIdx.x] = out[1];
+    }
+}
+// stage 2 (one warp): rho_avg at bounce-back and the post-collision mass
+__global__ void k_pfinish2(PartDev d, int nblocks) {
+    if (d.status[0]) return;
+    const int lane = threadIdx.x;
+    double a0 = d.partials[2 * nblocks + lane], a1 = d.partials[2 * nblocks + FINISH_BLOCKS + lane];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a0 += __shfl_down_sync(0xffffffffu, a0, o);
+        a1 += __shfl_down_sync(0xffffffffu, a1, o);
+    }
+    if (lane == 0) {
+        d.rho_avg[0] = a0 / (double)d.n_fluid[0];
+        d.rho_avg[2] = a1;
+    }
+}
+// average density over the new fluid set, used by the refill (one warp,
+// fixed order): (mass after bounce-back + link corrections + phase changes)
+// / (fluid count + its change)
+__global__ void k_prefill_avg(PartParams p, PartDev d) {
+    if (d.status[0]) return;
+    const int lane = threadIdx.x;
+    double sum = 0.0;
+    long long cnt = 0;
+    for (int q = lane; q < p.np; q += 32) {
+        for (int sl = 0; sl < NSLAB; sl++) sum += d.corr[q * NSLAB + sl];
+        sum += d.prep_sum[q];
+        cnt += d.prep_cnt[q];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        sum += __shfl_down_sync(0xffffffffu, sum, o);
+        cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    }
+    if (lane == 0) {
+        const long long n1 = d.n_fluid[0] + cnt;
+        d.rho_avg[1] = (d.rho_avg[2] + sum) / (double)n1;
+        d.n_fluid[1] = n1;  // moved into slot 0 by k_pcommit
     }
 }
 
 // --------------------------------------------------- boundary links (IBB) --
-// post-collision value fp(q, c) of node c (coordinates as 0-based indices)
-// read from the streamed array; nodes outside the y/z walls give the
-// reference's ghost value omega*rho0
-template <typename S>
-__device__ __forceinline__ double fp_at(const S* f, int q, int i, int j, int k,
-                                        const PartParams& p) {
+// Deviation f - w rho0 of the post-collision value fp(q, c) of node c
+// (coordinates as 0-based indices), read from the streamed array; nodes
+// outside the walls hold the reference's ghost value omega*rho0 (deviation 0).
+// L: arithmetic type of the population work (FP64 for FP64 storage, FP32 for
+// FP32 storage).
+template <typename S, typename L>
+__device__ __forceinline__ L fp_dev(const S* f, int q, int i, int j, int k, const PartParams& p) {
     const int nx = p.nx, ny = p.ny, nz = p.nz;
-    if (j < 0 || j >= ny || k < 0 || k >= nz) return w19(q) * p.rho0;
-    if (!p.periodic_x && (i < 0 || i >= nx)) return w19(q) * p.rho0;
+    if (j < 0 || j >= ny || k < 0 || k >= nz) return L(0);
+    if (!p.periodic_x && (i < 0 || i >= nx)) return L(0);
     const long long P = (long long)nx * ny * nz;
     i = wrapx(i, nx);
     const int jj = j + ey19(q), kk = k + ez19(q), ir = i + ex19(q);
-    if (jj < 0 || jj >= ny || kk < 0 || kk >= nz || (!p.periodic_x && (ir < 0 || ir >= nx)))
-        // bounced back into slot opp(q) of c
-        return pabs<S>(f, opp19(q) * P + (i + (long long)nx * (j + (long long)ny * k)), opp19(q), p.rho0);
-    const int ii = wrapx(ir, nx);
-    return pabs<S>(f, q * P + (ii + (long long)nx * (jj + (long long)ny * kk)), q, p.rho0);
+    long long idx;
+    int qq = q;
+    if (jj < 0 || jj >= ny || kk < 0 || kk >= nz || (!p.periodic_x && (ir < 0 || ir >= nx))) {
+        qq = opp19(q);  // bounced back into slot opp(q) of c (w_q = w_opp(q))
+        idx = qq * P + (i + (long long)nx * (j + (long long)ny * k));
+    } else {
+        idx = q * P + (wrapx(ir, nx) + (long long)nx * (jj + (long long)ny * kk));
+    }
+    if (PSt<S>::SHIFT) return (L)f[idx];
+    return (L)((double)f[idx] - w19(qq) * p.rho0);
 }
 
+// The interpolation weights of the quadratic bounce-back sum to one, so it is
+// applied to deviations directly.  The momentum exchange
+//   (e - u_w) fp - (-e - u_w) f_new = 2 e w rho0 + (e - u_w) dfp + (e + u_w) df_new
+// adds its constant part 2 e w rho0 exactly in FP64; geometry (q, the wall
+// point, the wall velocity) is FP64 in both forms.
 template <typename S>
 __global__ void __launch_bounds__(PB) k_plinks(S* __restrict__ f, PartParams p, PartDev d) {
+    using L = typename PC<S>::C;
     if (d.status[0]) return;
-    const int c = blockIdx.x;
+    const int c = blockIdx.x, slab = blockIdx.y;
     const double* X = d.xc + 3 * c;
     const double* U = d.uc + 3 * c;
     const double* O = d.om + 3 * c;
@@ -214,154 +297,241 @@ __global__ void __launch_bounds__(PB) k_plinks(S* __restrict__ f, PartParams p, 
     const int h = (int)ceil(R) + 2;
     const int ci = (int)floor(X[0]) - 1, cj = (int)floor(X[1]) - 1, ck = (int)floor(X[2]) - 1;
     const int bw = 2 * h + 2;
-    const long long nbox = (long long)bw * bw * bw;
+    const int kz0 = slab * bw / NSLAB, kz1 = (slab + 1) * bw / NSLAB;
+    const long long nbox = (long long)bw * bw * (kz1 - kz0);
+    const double reach2 = (R + 1.8) * (R + 1.8);  // |x - X| <= R + sqrt(2) for a link
     double acc[7] = {0, 0, 0, 0, 0, 0, 0};
-    for (long long t = threadIdx.x; t < nbox; t += PB) {
-        const int bi = (int)(t % bw), bj = (int)((t / bw) % bw), bk = (int)(t / ((long long)bw * bw));
-        int i = ci - h + bi;
-        const int j = cj - h + bj, k = ck - h + bk;
-        if (j < 0 || j >= ny || k < 0 || k >= nz) continue;
-        if (p.periodic_x) i = wrapx(i, nx);
-        else if (i < 0 || i >= nx) continue;
-        const long long cell = i + (long long)nx * (j + (long long)ny * k);
-        if (d.owner_cur[cell] >= 0) continue;
-#pragma unroll 1
-        for (int a = 1; a < Q19; a++) {
+    // Links are first listed per round of PB box nodes (cell, direction) and
+    // then processed one per thread, so that the heavy link arithmetic runs
+    // with full warps instead of once per direction with a few lanes.
+    __shared__ long long s_cell[PB * 18];
+    __shared__ unsigned char s_dir[PB * 18];
+    __shared__ int s_n;
+    __shared__ int s_wsum[PB / 32];
+    for (long long t0 = 0; t0 < nbox; t0 += PB) {
+        unsigned my_dirs = 0;  // bit a: direction a is a boundary link of my node
+        long long my_cell = 0;
+        const long long t = t0 + threadIdx.x;
+        if (t < nbox) {
+            const int bi = (int)(t % bw), bj = (int)((t / bw) % bw), bk = kz0 + (int)(t / ((long long)bw * bw));
+            int i = ci - h + bi;
+            const int j = cj - h + bj, k = ck - h + bk;
+            bool ok = !(j < 0 || j >= ny || k < 0 || k >= nz);
+            if (ok) {
+                const double ox = dxp((double)(i + 1), X[0], p), oy = (double)(j + 1) - X[1],
+                             oz = (double)(k + 1) - X[2];
+                ok = ox * ox + oy * oy + oz * oz <= reach2;
+            }
+            if (ok) {
+                if (p.periodic_x) i = wrapx(i, nx);
+                else ok = i >= 0 && i < nx;
+            }
+            const long long cell = i + (long long)nx * (j + (long long)ny * k);
+            if (ok && d.owner_cur[cell] < 0) {
+                for (int a = 1; a < Q19; a++) {
+                    const int jn = j + ey19(a), kn = k + ez19(a);
+                    if (jn < 0 || jn >= ny || kn < 0 || kn >= nz) continue;
+                    int in = i + ex19(a);
+                    if (p.periodic_x) in = wrapx(in, nx);
+                    else if (in < 0 || in >= nx) continue;
+                    if (d.owner_cur[in + (long long)nx * (jn + (long long)ny * kn)] != c) continue;
+                    my_dirs |= 1u << a;
+                }
+                my_cell = cell;
+            }
+        }
+        // deterministic slots: exclusive prefix sum of the per-thread link counts
+        const int cnt = __popc(my_dirs);
+        int incl = cnt;
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (lane == 31) s_wsum[wid] = incl;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int run = 0;
+            for (int q = 0; q < PB / 32; q++) {
+                const int v = s_wsum[q];
+                s_wsum[q] = run;
+                run += v;
+            }
+            s_n = run;
+        }
+        __syncthreads();
+        int slot = s_wsum[wid] + incl - cnt;
+        for (unsigned m = my_dirs; m; m &= m - 1) {
+            s_cell[slot] = my_cell;
+            s_dir[slot] = (unsigned char)(__ffs(m) - 1);
+            slot++;
+        }
+        __syncthreads();
+        const int nl = s_n;
+        for (int e = threadIdx.x; e < nl; e += PB) {
+            const long long cell = s_cell[e];
+            const int a = s_dir[e];
+            const int i = (int)(cell % nx), j = (int)((cell / nx) % ny), k = (int)(cell / ((long long)nx * ny));
+            const double ox = dxp((double)(i + 1), X[0], p), oy = (double)(j + 1) - X[1],
+                         oz = (double)(k + 1) - X[2];
             const int ea = ex19(a), eb = ey19(a), ec = ez19(a);
-            const int jn = j + eb, kn = k + ec;
-            if (jn < 0 || jn >= ny || kn < 0 || kn >= nz) continue;
-            int in = i + ea;
-            if (p.periodic_x) in = wrapx(in, nx);
-            else if (in < 0 || in >= nx) continue;
-            if (d.owner_cur[in + (long long)nx * (jn + (long long)ny * kn)] != c) continue;
             // q: ray-sphere root from the node (calQ2, particle_bounceback.F90:144-185)
-            double x = (double)(i + 1), y = (double)(j + 1), z = (double)(k + 1);
-            if (p.periodic_x) x = X[0] + dxp(x, X[0], p);
             const double ca = (double)(ea * ea + eb * eb + ec * ec);
-            const double cb = 2.0 * (ea * (x - X[0]) + eb * (y - X[1]) + ec * (z - X[2]));
-            const double cc = (x - X[0]) * (x - X[0]) + (y - X[1]) * (y - X[1]) + (z - X[2]) * (z - X[2]) - R * R;
+            const double cb = 2.0 * (ea * ox + eb * oy + ec * oz);
+            const double cc = ox * ox + oy * oy + oz * oz - R * R;
             const double delta = cb * cb - 4.0 * ca * cc;
             if (delta < 0) { atomicCAS(d.status, 0, PS_Q_RANGE); d.status[1] = c; continue; }
-            const double q = (-cb - sqrt(delta)) / (2.0 * ca);
+            const double q = (-cb - sqrt(delta)) * (ca == 1.0 ? 0.5 : 0.25);  // /(2 ca), exact
             if (q > 1.0 || q < 0.0) { atomicCAS(d.status, 0, PS_Q_RANGE); d.status[1] = c; continue; }
-            const double x0 = x + q * ea, y0 = y + q * eb, z0 = z + q * ec;
-            const double rx = x0 - X[0], ry = y0 - X[1], rz = z0 - X[2];
-            const double rot0 = O[1] * rz - O[2] * ry, rot1 = O[2] * rx - O[0] * rz,
-                         rot2 = O[0] * ry - O[1] * rx;
+            // wall point relative to the centre and its velocity U + Omega x r
+            const double rx = ox + q * ea, ry = oy + q * eb, rz = oz + q * ec;
+            const double uw0 = U[0] + (O[1] * rz - O[2] * ry);
+            const double uw1 = U[1] + (O[2] * rx - O[0] * rz);
+            const double uw2 = U[2] + (O[0] * ry - O[1] * rx);
             const int ra = opp19(a);
-            const double eu = -ea * (U[0] + rot0) - eb * (U[1] + rot1) - ec * (U[2] + rot2);
-            const double fpa = fp_at<S>(f, a, i, j, k, p);
-            double val;
+            const double w = w19(a);
+            const L mv = (L)(6.0 * w * ravg * (-ea * uw0 - eb * uw1 - ec * uw2));  // moving-wall term
+            const L dpa = fp_dev<S, L>(f, a, i, j, k, p);
+            L dn;
             if (q < 0.5) {
-                const double f1 = fp_at<S>(f, a, i - ea, j - eb, k - ec, p);
-                const double f2 = fp_at<S>(f, a, i - 2 * ea, j - 2 * eb, k - 2 * ec, p);
-                val = q * (1.0 + 2.0 * q) * fpa + (1.0 - 4.0 * q * q) * f1 - q * (1.0 - 2.0 * q) * f2 +
-                      6.0 * w19(a) * ravg * eu;
+                const L c0 = (L)(q * (1.0 + 2.0 * q)), c1 = (L)(1.0 - 4.0 * q * q),
+                        c2 = (L)(q * (1.0 - 2.0 * q));
+                const L d1 = fp_dev<S, L>(f, a, i - ea, j - eb, k - ec, p);
+                const L d2 = fp_dev<S, L>(f, a, i - 2 * ea, j - 2 * eb, k - 2 * ec, p);
+                dn = c0 * dpa + c1 * d1 - c2 * d2 + mv;
             } else {
-                const double g0 = fp_at<S>(f, ra, i, j, k, p);
-                const double g1 = fp_at<S>(f, ra, i - ea, j - eb, k - ec, p);
-                val = fpa / q / (1.0 + 2.0 * q) + g0 * (2.0 * q - 1.0) / q -
-                      g1 * (2.0 * q - 1.0) / (2.0 * q + 1.0) + 6.0 * w19(a) * ravg / q / (1.0 + 2.0 * q) * eu;
+                const double iq = 1.0 / q, i2 = 1.0 / (1.0 + 2.0 * q), a2 = 2.0 * q - 1.0;
+                const L g0 = fp_dev<S, L>(f, ra, i, j, k, p);
+                const L g1 = fp_dev<S, L>(f, ra, i - ea, j - eb, k - ec, p);
+                dn = (L)(iq * i2) * dpa + (L)(a2 * iq) * g0 - (L)(a2 * i2) * g1 + (L)(iq * i2) * mv;
             }
-            pset<S>(f, ra * P + cell, ra, val, p.rho0);
-            const double fnew = pabs<S>(f, ra * P + cell, ra, p.rho0);  // as stored
+            const long long slot = ra * P + cell;
+            if (PSt<S>::SHIFT) {
+                f[slot] = (S)dn;
+                dn = (L)f[slot];  // as stored
+            } else {
+                f[slot] = (S)((double)dn + w * p.rho0);
+                dn = (L)((double)f[slot] - w * p.rho0);
+            }
             // Wen et al. 2014 Galilean-invariant momentum exchange
-            const double Fx = (ea - U[0] - rot0) * fpa - (-ea - U[0] - rot0) * fnew;
-            const double Fy = (eb - U[1] - rot1) * fpa - (-eb - U[1] - rot1) * fnew;
-            const double Fz = (ec - U[2] - rot2) * fpa - (-ec - U[2] - rot2) * fnew;
-            acc[0] += Fx;
-            acc[1] += Fy;
-            acc[2] += Fz;
-            acc[3] += ry * Fz - rz * Fy;
-            acc[4] += rz * Fx - rx * Fz;
-            acc[5] += rx * Fy - ry * Fx;
-            acc[6] += fnew - fpa;
+            const double F0 = 2.0 * ea * w * p.rho0 + (double)((ea - (L)uw0) * dpa + (ea + (L)uw0) * dn);
+            const double F1 = 2.0 * eb * w * p.rho0 + (double)((eb - (L)uw1) * dpa + (eb + (L)uw1) * dn);
+            const double F2 = 2.0 * ec * w * p.rho0 + (double)((ec - (L)uw2) * dpa + (ec + (L)uw2) * dn);
+            acc[0] += F0;
+            acc[1] += F1;
+            acc[2] += F2;
+            acc[3] += ry * F2 - rz * F1;
+            acc[4] += rz * F0 - rx * F2;
+            acc[5] += rx * F1 - ry * F0;
+            acc[6] += (double)(dn - dpa);
         }
+        __syncthreads();
     }
     __shared__ double out[7];
     block_sum_to<7>(acc, out, 1);
     if (threadIdx.x == 0) {
+        const int sl = c * NSLAB + slab;  // per-slab partials, summed in slab order by readers
         for (int q = 0; q < 3; q++) {
-            d.flink[3 * c + q] = out[q];
-            d.tlink[3 * c + q] = out[3 + q];
+            d.flink[3 * sl + q] = out[q];
+            d.tlink[3 * sl + q] = out[3 + q];
         }
-        d.corr[c] = out[6];
+        d.corr[sl] = out[6];
     }
 }
 
 // ----------------------------------------------------------- update --------
-// particle_force.F90:96-190 and particle_update.F90:26-50 in 3-D
-__global__ void k_pupdate(PartParams p, PartDev d) {
+// particle_force.F90:96-190 in 3-D: one warp per particle; the lanes split the
+// pair loop and a fixed shuffle tree adds their spring forces.
+__global__ void k_pforce(PartParams p, PartDev d) {
     if (d.status[0]) return;
     const int np = p.np;
+    const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (c >= np) return;
     const double R0 = p.radius, ravg = d.rho_avg[0];
     const double vol = 4.0 / 3.0 * p.pi * R0 * R0 * R0;
-    const double M = p.rho_solid * 4.0 / 3.0 * p.pi * R0 * R0 * R0;
-    for (int c = threadIdx.x; c < np; c += blockDim.x) {
-        const double* X = d.xc + 3 * c;
-        double fij[3] = {0.0, 0.0, 0.0}, fw[3] = {0.0, 0.0, 0.0};
-        const double Rc = R0;
-        for (int c2 = 0; c2 < np; c2++) {
-            if (c2 == c) continue;
-            const double* X2 = d.xc + 3 * c2;
-            const double d0 = dxp(X[0], X2[0], p), d1 = X[1] - X2[1], d2 = X[2] - X2[2];
-            const double dij = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
-            const double thr = p.thr_part;
-            if (dij >= Rc + R0 + thr) {
-            } else if (dij >= Rc + R0) {
-                const double t = (dij - Rc - R0 - thr) / thr;
-                fij[0] = fij[0] + p.scale_part * (t * t) * d0 / dij;
-                fij[1] = fij[1] + p.scale_part * (t * t) * d1 / dij;
-                fij[2] = fij[2] + p.scale_part * (t * t) * d2 / dij;
-            } else {
-                if (atomicCAS(d.status, 0, PS_OVERLAP) == 0) {
-                    d.status[1] = c;
-                    d.status[2] = c2;
-                }
+    const double* X = d.xc + 3 * c;
+    double fij[3] = {0.0, 0.0, 0.0};
+    const double Rc = R0;
+    for (int c2 = lane; c2 < np; c2 += 32) {
+        if (c2 == c) continue;
+        const double* X2 = d.xc + 3 * c2;
+        const double d0 = dxp(X[0], X2[0], p), d1 = X[1] - X2[1], d2 = X[2] - X2[2];
+        const double thr = p.thr_part;
+        const double reach = Rc + R0 + thr;
+        if (fabs(d0) >= reach || fabs(d1) >= reach || fabs(d2) >= reach) continue;  // out of range
+        const double dij = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+        if (dij >= Rc + R0 + thr) {
+        } else if (dij >= Rc + R0) {
+            const double t = (dij - Rc - R0 - thr) / thr;
+            fij[0] = fij[0] + p.scale_part * (t * t) * d0 / dij;
+            fij[1] = fij[1] + p.scale_part * (t * t) * d1 / dij;
+            fij[2] = fij[2] + p.scale_part * (t * t) * d2 / dij;
+        } else {
+            if (atomicCAS(d.status, 0, PS_OVERLAP) == 0) {
+                d.status[1] = c;
+                d.status[2] = c2;
             }
-        }
-        const double thw = p.thr_wall;
-        for (int ax = 0; ax < 3; ax++) {
-            if (ax == 0 && p.periodic_x) continue;
-            const int nax = ax == 0 ? p.nx : (ax == 1 ? p.ny : p.nz);
-            double dw = X[ax] - Rc - 1.0;
-            if (dw < 0) {
-                if (atomicCAS(d.status, 0, PS_WALL) == 0) d.status[1] = c;
-            } else if (dw < thw) {
-                fw[ax] = fw[ax] + p.scale_wall * ((dw - thw) / thw) * ((dw - thw) / thw);
-            }
-            dw = (double)nax - X[ax] - Rc;
-            if (dw < 0) {
-                if (atomicCAS(d.status, 0, PS_WALL) == 0) d.status[1] = c;
-            } else if (dw < thw) {
-                fw[ax] = fw[ax] - p.scale_wall * ((dw - thw) / thw) * ((dw - thw) / thw);
-            }
-        }
-        for (int q = 0; q < 3; q++) {
-            double tot = d.flink[3 * c + q] + (p.rho_solid - ravg) * vol * p.gravity[q] + fij[q] + fw[q];
-            tot = tot + ravg * vol * p.body_force[q];
-            d.ftot[3 * c + q] = tot;
-            d.ttot[3 * c + q] = d.tlink[3 * c + q];
         }
     }
-    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 3; q++)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) fij[q] += __shfl_down_sync(0xffffffffu, fij[q], o);
+    if (lane != 0) return;
+    double fw[3] = {0.0, 0.0, 0.0};
+    const double thw = p.thr_wall;
+    for (int ax = 0; ax < 3; ax++) {
+        if (ax == 0 && p.periodic_x) continue;
+        const int nax = ax == 0 ? p.nx : (ax == 1 ? p.ny : p.nz);
+        double dw = X[ax] - Rc - 1.0;
+        if (dw < 0) {
+            if (atomicCAS(d.status, 0, PS_WALL) == 0) d.status[1] = c;
+        } else if (dw < thw) {
+            fw[ax] = fw[ax] + p.scale_wall * ((dw - thw) / thw) * ((dw - thw) / thw);
+        }
+        dw = (double)nax - X[ax] - Rc;
+        if (dw < 0) {
+            if (atomicCAS(d.status, 0, PS_WALL) == 0) d.status[1] = c;
+        } else if (dw < thw) {
+            fw[ax] = fw[ax] - p.scale_wall * ((dw - thw) / thw) * ((dw - thw) / thw);
+        }
+    }
+    for (int q = 0; q < 3; q++) {
+        double fl = 0.0, tl = 0.0;
+        for (int sl = 0; sl < NSLAB; sl++) {
+            fl += d.flink[3 * (c * NSLAB + sl) + q];
+            tl += d.tlink[3 * (c * NSLAB + sl) + q];
+        }
+        double tot = fl + (p.rho_solid - ravg) * vol * p.gravity[q] + fij[q] + fw[q];
+        tot = tot + ravg * vol * p.body_force[q];
+        d.ftot[3 * c + q] = tot;
+        d.ttot[3 * c + q] = tl;
+    }
+}
+
+// particle_update.F90:26-50 in 3-D, one thread per particle
+__global__ void k_pmove(PartParams p, PartDev d) {
     if (d.status[0]) return;
-    for (int c = threadIdx.x; c < np; c += blockDim.x) {
-        const double I = 0.4 * M * R0 * R0;
-        for (int q = 0; q < 3; q++) {
-            d.xc_old[3 * c + q] = d.xc[3 * c + q];
-            d.uc_old[3 * c + q] = d.uc[3 * c + q];
-            d.om_old[3 * c + q] = d.om[3 * c + q];
-            const double a = d.ftot[3 * c + q] / M;
-            d.uc[3 * c + q] = d.uc_old[3 * c + q] + a;
-            d.om[3 * c + q] = d.om_old[3 * c + q] + d.ttot[3 * c + q] / I;
-            d.xc[3 * c + q] = d.xc_old[3 * c + q] + d.uc_old[3 * c + q] + 0.5 * a;
-        }
-        if (p.periodic_x) {
-            const double L = (double)p.nx;
-            if (d.xc[3 * c] >= L + 0.5) d.xc[3 * c] -= L;
-            if (d.xc[3 * c] < 0.5) d.xc[3 * c] += L;
-        }
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= p.np) return;
+    const double R0 = p.radius;
+    const double M = p.rho_solid * 4.0 / 3.0 * p.pi * R0 * R0 * R0;
+    const double I = 0.4 * M * R0 * R0;
+    for (int q = 0; q < 3; q++) {
+        d.xc_old[3 * c + q] = d.xc[3 * c + q];
+        d.uc_old[3 * c + q] = d.uc[3 * c + q];
+        d.om_old[3 * c + q] = d.om[3 * c + q];
+        const double a = d.ftot[3 * c + q] / M;
+        d.uc[3 * c + q] = d.uc_old[3 * c + q] + a;
+        d.om[3 * c + q] = d.om_old[3 * c + q] + d.ttot[3 * c + q] / I;
+        d.xc[3 * c + q] = d.xc_old[3 * c + q] + d.uc_old[3 * c + q] + 0.5 * a;
+    }
+    if (p.periodic_x) {
+        const double L = (double)p.nx;
+        if (d.xc[3 * c] >= L + 0.5) d.xc[3 * c] -= L;
+        if (d.xc[3 * c] < 0.5) d.xc[3 * c] += L;
     }
 }
 
@@ -383,8 +553,15 @@ __global__ void __launch_bounds__(PB) k_pmark(int* owner, const double* xc, Part
         if (j < 0 || j >= p.ny || k < 0 || k >= p.nz) continue;
         if (p.periodic_x) i = wrapx(i, p.nx);
         else if (i < 0 || i >= p.nx) continue;
-        if (inside((double)(i + 1), (double)(j + 1), (double)(k + 1), X, R, p))
-            owner[i + (long long)p.nx * (j + (long long)p.ny * k)] = c;
+        // FP32 decides far from the surface; nodes within 1e-3 R^2 of it use
+        // the IEEE-rounded FP64 test
+        const float fx = (float)dxp((double)(i + 1), X[0], p), fy = (float)((double)(j + 1) - X[1]),
+                    fz = (float)((double)(k + 1) - X[2]);
+        const float d2 = fx * fx + fy * fy + fz * fz, r2 = (float)(R * R);
+        bool in;
+        if (fabsf(d2 - r2) > 1e-3f * r2) in = d2 < r2;
+        else in = inside((double)(i + 1), (double)(j + 1), (double)(k + 1), X, R, p);
+        if (in) owner[i + (long long)p.nx * (j + (long long)p.ny * k)] = c;
     }
 }
 
@@ -507,18 +684,7 @@ __global__ void __launch_bounds__(PB) k_prefill(S* __restrict__ f, PartParams p,
     __shared__ double s_ravg;
     if (threadIdx.x == 0) {
         s_n = 0;
-        // average density over the new fluid set (fixed-order sums)
-        double sum = d.rho_avg[2];
-        long long cnt = d.n_fluid[0];
-        for (int q = 0; q < p.np; q++) {
-            sum += d.corr[q];
-            sum += d.prep_sum[q];
-            cnt += d.prep_cnt[q];
-        }
-        s_ravg = sum / (double)cnt;
-        if (c == 0) {
-            d.rho_avg[1] = s_ravg;
-        }
+        s_ravg = d.rho_avg[1];
     }
     __syncthreads();
     const double* X = d.xc + 3 * c;       // new centre
@@ -590,11 +756,6 @@ __global__ void __launch_bounds__(PB) k_prefill(S* __restrict__ f, PartParams p,
     for (int t = threadIdx.x; t < n * Q19; t += PB) {
         const int slot = t / Q19, a = t % Q19;
         pset<S>(f, a * P + s_cell[slot], a, s_val[slot][a], p.rho0);
-    }
-    if (c == 0 && threadIdx.x == 0) {
-        long long cnt = d.n_fluid[0];
-        for (int q = 0; q < p.np; q++) cnt += d.prep_cnt[q];
-        d.n_fluid[1] = cnt;  // moved into slot 0 by k_pcommit
     }
 }
 
@@ -676,16 +837,19 @@ static cudaError_t pstep_go(bool first, const void* fin, void* fout, const PartP
         k_pbulk<S, true><<<g, b, 0, s>>>((const S*)fin, (S*)fout, d.owner_cur, p, cd, d.partials, d.status);
     else
         k_pbulk<S, false><<<g, b, 0, s>>>((const S*)fin, (S*)fout, d.owner_cur, p, cd, d.partials, d.status);
-    k_pfinish<<<1, 256, 0, s>>>(d, d.nblocks);
+    k_pfinish<<<FINISH_BLOCKS, 256, 0, s>>>(d, d.nblocks);
+    k_pfinish2<<<1, 32, 0, s>>>(d, d.nblocks);
     if (p.np > 0) {
-        k_plinks<S><<<p.np, PB, 0, s>>>((S*)fout, p, d);
-        k_pupdate<<<1, 256, 0, s>>>(p, d);
+        k_plinks<S><<<dim3(p.np, NSLAB), PB, 0, s>>>((S*)fout, p, d);
+        k_pforce<<<(p.np + 7) / 8, 256, 0, s>>>(p, d);
+        k_pmove<<<(p.np + 127) / 128, 128, 0, s>>>(p, d);
     }
     cudaError_t e = cudaMemsetAsync(d.owner_new, 0xFF, sizeof(int) * (size_t)p.nx * p.ny * p.nz, s);
     if (e != cudaSuccess) return e;
     if (p.np > 0) {
         k_pmark<<<p.np, PB, 0, s>>>(d.owner_new, d.xc, p, d.status, true);
         k_pprep<S><<<p.np, PB, 0, s>>>((const S*)fout, p, d);
+        k_prefill_avg<<<1, 32, 0, s>>>(p, d);
         k_prefill<S><<<p.np, PB, 0, s>>>((S*)fout, p, d, d.nblocks);
         k_pcommit<<<1, 1, 0, s>>>(d);
     }

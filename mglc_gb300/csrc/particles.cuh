@@ -7,6 +7,10 @@
 
 namespace mglc {
 
+// CTAs per particle in the boundary-link kernel (z slabs of the node box);
+// the link sums are kept per (particle, slab) and added in slab order
+constexpr int PART_NSLAB = 4;
+
 // Status codes written by the particle kernels (mirrors orc_pt_step's codes).
 enum PartStatus {
     PS_OK = 0,
@@ -31,7 +35,7 @@ struct PartDev {
     int* owner_new;
     double *xc, *uc, *om;              // np*3, current
     double *xc_old, *uc_old, *om_old;  // np*3
-    double *flink, *tlink, *corr;      // np*3, np*3, np: momentum exchange sums per particle
+    double *flink, *tlink, *corr;      // np*PART_NSLAB*3 (x2), np*PART_NSLAB: link sums per slab
     double *ftot, *ttot;               // np*3: total force and torque of the last step
     double* prep_sum;                  // np: refill bookkeeping (density)
     int* prep_cnt;                     // np: refill bookkeeping (fluid count change)
