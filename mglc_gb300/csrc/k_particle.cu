@@ -151,16 +151,23 @@ __global__ void __launch_bounds__(128)
         for (int q = 0; q < Q19; q++) m += f[q];
         cacc[1] = m;
         const long long sy = nx, sz = (long long)nx * ny;
+        if (i > 0 && i < nx - 1 && j > 0 && j < ny - 1 && k > 0 && k < nz - 1) {
+            // interior node: every population streams, no wrap
 #pragma unroll
-        for (int q = 0; q < Q19; q++) {
-            const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
-            const int jj = j + dy, kk = k + dz, ir = i + dx;
-            const bool xwall = !p.periodic_x && (ir < 0 || ir >= nx);
-            if (xwall || jj < 0 || jj >= ny || kk < 0 || kk >= nz) {
-                fout[opp19(q) * P + cell] = (S)f[q];  // no-slip wall
-            } else {
-                const int ii = wrapx(ir, nx);
-                fout[q * P + ((long long)ii + sy * jj + sz * kk)] = (S)f[q];
+            for (int q = 0; q < Q19; q++)
+                fout[q * P + cell + ex19(q) + ey19(q) * sy + ez19(q) * sz] = (S)f[q];
+        } else {
+#pragma unroll
+            for (int q = 0; q < Q19; q++) {
+                const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
+                const int jj = j + dy, kk = k + dz, ir = i + dx;
+                const bool xwall = !p.periodic_x && (ir < 0 || ir >= nx);
+                if (xwall || jj < 0 || jj >= ny || kk < 0 || kk >= nz) {
+                    fout[opp19(q) * P + cell] = (S)f[q];  // no-slip wall
+                } else {
+                    const int ii = wrapx(ir, nx);
+                    fout[q * P + ((long long)ii + sy * jj + sz * kk)] = (S)f[q];
+                }
             }
         }
     }

@@ -1,9 +1,11 @@
 // k_serve.cu -- kernels of the solve server.
 //
-// k_serve_step is a persistent kernel: a grid sized to the SM count pulls
-// tiles (rows_per_tile x-rows of one solve) from a queue shared by every
-// resident solve, through one atomic counter per step, and runs the fused
-// step of that solve on the tile's cells.  Small and large grids, lid and
+// k_serve_step is a persistent kernel: every warp of a grid sized to the SM
+// count pulls tiles (rows_per_tile x-rows of one solve) from a queue shared by
+// the resident solves of one kind, through one atomic counter per step, and
+// runs the fused step of that solve on the tile's cells.  Lid and heated
+// solves have separate kernels (each with its own register budget) that run
+// concurrently.  Small and large grids, lid and
 // heated cavities are mixed in one launch, so small solves no longer leave
 // the GPU idle.  The per-cell arithmetic is exactly that of the one-solve
 // kernels (step_cell.cuh), so a solve's result does not depend on which
@@ -23,22 +25,26 @@ __device__ __forceinline__ int find_solve(const ServeTable* tab, int t) {
     return lo;
 }
 
-// grab the next tile for the whole CTA
-__device__ __forceinline__ int next_tile(unsigned* counter) {
-    __shared__ int s_tile;
-    __syncthreads();
-    if (threadIdx.x == 0) s_tile = (int)atomicAdd(counter, 1u);
-    __syncthreads();
-    return s_tile;
+// Each warp pulls its own tiles (no block-wide barriers): lane 0 takes the
+// next index from the step's counter and broadcasts it.
+__device__ __forceinline__ int next_tile_warp(unsigned* counter) {
+    int t = 0;
+    if ((threadIdx.x & 31) == 0) t = (int)atomicAdd(counter, 1u);
+    return __shfl_sync(0xffffffffu, t, 0);
 }
 
-template <typename S>
-__global__ void k_serve_step(const ServeTable* __restrict__ tab, int parity, unsigned* counter) {
-    const int total = tab->total_tiles;
+// lid tiles: [0, lid_tiles); heated tiles: [lid_tiles, total_tiles)
+template <typename S, bool THERMAL>
+__global__ void __launch_bounds__(256, THERMAL ? 2 : 3)
+    k_serve_step(const ServeTable* __restrict__ tab, int parity, unsigned* counter) {
+    const int base = THERMAL ? tab->lid_tiles : 0;
+    const int ntiles = (THERMAL ? tab->total_tiles : tab->lid_tiles) - base;
     const int R = tab->rows_per_tile;
+    const int lane = threadIdx.x & 31;
     for (;;) {
-        const int t = next_tile(counter);
-        if (t >= total) break;
+        const int tl = next_tile_warp(counter);
+        if (tl >= ntiles) break;
+        const int t = base + tl;
         const ServeSolve& sv = tab->s[find_solve(tab, t)];
         const int nx = sv.nx, ny = sv.ny, nz = sv.nz;
         const int r0 = (t - sv.tile0) * R;
@@ -46,10 +52,10 @@ __global__ void k_serve_step(const ServeTable* __restrict__ tab, int parity, uns
         const int ncell = (r1 - r0) * nx;
         const S* fin = (const S*)sv.f[parity];
         S* fout = (S*)sv.f[parity ^ 1];
-        for (int idx = threadIdx.x; idx < ncell; idx += blockDim.x) {
+        for (int idx = lane; idx < ncell; idx += 32) {
             const int i = idx % nx, r = r0 + idx / nx;
             const int j = r % ny, k = r / ny;
-            if (sv.kind == 1)
+            if (!THERMAL)
                 lid_cell<S, false, unsigned>(i, j, k, fin, fout, sv.K, sv.plane, nullptr, nullptr,
                                              nullptr, nullptr);
             else
@@ -61,15 +67,15 @@ __global__ void k_serve_step(const ServeTable* __restrict__ tab, int parity, uns
     }
 }
 
-// max |u - uprev| / uref per solve; uprev <- u
+// max |u - uprev| / uref per solve; uprev <- u (all solves, warp tiles)
 template <typename S>
 __global__ void k_serve_resid(const ServeTable* __restrict__ tab, unsigned* counter,
                               unsigned* resid) {
     const int total = tab->total_tiles;
     const int R = tab->rows_per_tile;
-    __shared__ float s_max[32];
+    const int lane = threadIdx.x & 31;
     for (;;) {
-        const int t = next_tile(counter);
+        const int t = next_tile_warp(counter);
         if (t >= total) break;
         const int si = find_solve(tab, t);
         const ServeSolve& sv = tab->s[si];
@@ -80,7 +86,7 @@ __global__ void k_serve_resid(const ServeTable* __restrict__ tab, unsigned* coun
         const int ncell = (r1 - r0) * nx;
         const S* f = (const S*)sv.f[0];  // residual runs after an even number of steps
         float m = 0.0f;
-        for (int idx = threadIdx.x; idx < ncell; idx += blockDim.x) {
+        for (int idx = lane; idx < ncell; idx += 32) {
             const unsigned cell = (unsigned)(r0 * nx + idx);
             float fq[Q19];
 #pragma unroll
@@ -101,13 +107,7 @@ __global__ void k_serve_resid(const ServeTable* __restrict__ tab, unsigned* coun
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
-        if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = m;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            float b = 0.0f;
-            for (int w = 0; w < (int)(blockDim.x + 31) / 32; w++) b = fmaxf(b, s_max[w]);
-            atomicMax(resid + si, __float_as_uint(b));
-        }
+        if (lane == 0) atomicMax(resid + si, __float_as_uint(m));
     }
 }
 
@@ -159,11 +159,18 @@ __global__ void k_serve_fields(ServeSolve sv, float* out) {
     }
 }
 
-cudaError_t launch_serve_step(int form, const ServeTable* tab, int parity, unsigned* counter,
-                              int grid, int block, cudaStream_t st) {
-    if (form == FORM_FP16) k_serve_step<__half><<<grid, block, 0, st>>>(tab, parity, counter);
-    else if (form == FORM_FP32) k_serve_step<float><<<grid, block, 0, st>>>(tab, parity, counter);
-    else if (form == FORM_BF16) k_serve_step<__nv_bfloat16><<<grid, block, 0, st>>>(tab, parity, counter);
+template <typename S>
+static void serve_go(int thermal, const ServeTable* tab, int parity, unsigned* counter, int grid,
+                     int block, cudaStream_t st) {
+    if (thermal) k_serve_step<S, true><<<grid, block, 0, st>>>(tab, parity, counter);
+    else k_serve_step<S, false><<<grid, block, 0, st>>>(tab, parity, counter);
+}
+
+cudaError_t launch_serve_step(int form, int thermal, const ServeTable* tab, int parity,
+                              unsigned* counter, int grid, int block, cudaStream_t st) {
+    if (form == FORM_FP16) serve_go<__half>(thermal, tab, parity, counter, grid, block, st);
+    else if (form == FORM_FP32) serve_go<float>(thermal, tab, parity, counter, grid, block, st);
+    else if (form == FORM_BF16) serve_go<__nv_bfloat16>(thermal, tab, parity, counter, grid, block, st);
     else return cudaErrorInvalidValue;
     return cudaGetLastError();
 }

@@ -116,6 +116,8 @@ struct mglc_server {
     size_t fields_bytes = 0;
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t done = nullptr;
+    cudaStream_t side = nullptr;        // heated-solve branch of the captured step
+    cudaEvent_t fork = nullptr, join = nullptr;
     int block = 256, rows = 2, ctas_per_sm = 4, nsm = 152;
     bool tuned = false;
     std::vector<Req> reqs;
@@ -215,18 +217,23 @@ void place(mglc_server* s, Req& q) {
 
 int tiles_of(const mglc_server* s, const ServeSolve& sv) { return (sv.ny * sv.nz + s->rows - 1) / s->rows; }
 
-// rebuild the host table from the active list and upload it
+// rebuild the host table from the active list (lid solves first) and upload it
 int upload_table(mglc_server* s) {
     ServeTable* t = s->tab_host;
+    std::stable_sort(s->active.begin(), s->active.end(), [&](int a, int b) {
+        return s->reqs[a].r.kind < s->reqs[b].r.kind;  // MGLC_KIND_LID (1) before THERMAL (2)
+    });
     t->n_active = (int)s->active.size();
     t->rows_per_tile = s->rows;
     int tile = 0;
+    t->lid_tiles = 0;
     for (int a = 0; a < t->n_active; a++) {
         Req& q = s->reqs[s->active[a]];
         q.slot = a;
         q.sv.tile0 = tile;
         q.sv.ntiles = tiles_of(s, q.sv);
         tile += q.sv.ntiles;
+        if (q.r.kind == MGLC_KIND_LID) t->lid_tiles = tile;
         t->s[a] = q.sv;
     }
     t->total_tiles = tile;
@@ -244,12 +251,22 @@ int build_graph(mglc_server* s) {
     const int grid = s->nsm * s->ctas_per_sm;
     cudaGraph_t g;
     SCK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
-    cudaError_t e = cudaMemsetAsync(s->counters, 0, sizeof(unsigned) * (K + 1), s->stream);
+    // counters: [0, K) lid steps, [K, 2K) heated steps, 2K residual
+    cudaError_t e = cudaMemsetAsync(s->counters, 0, sizeof(unsigned) * (2 * K + 1), s->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(s->resid_dev, 0, sizeof(unsigned) * SERVE_MAX_ACTIVE, s->stream);
-    for (int k = 0; k < K && e == cudaSuccess; k++)
-        e = launch_serve_step(s->p.precision, s->tab_dev, k & 1, s->counters + k, grid, s->block, s->stream);
+    for (int k = 0; k < K && e == cudaSuccess; k++) {
+        // the heated branch runs beside the lid branch: fork and join per step
+        e = cudaEventRecord(s->fork, s->stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s->side, s->fork, 0);
+        if (e == cudaSuccess)
+            e = launch_serve_step(s->p.precision, 1, s->tab_dev, k & 1, s->counters + K + k, grid, s->block, s->side);
+        if (e == cudaSuccess)
+            e = launch_serve_step(s->p.precision, 0, s->tab_dev, k & 1, s->counters + k, grid, s->block, s->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(s->join, s->side);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s->stream, s->join, 0);
+    }
     if (e == cudaSuccess)
-        e = launch_serve_resid(s->p.precision, s->tab_dev, s->counters + K, s->resid_dev, grid, s->block, s->stream);
+        e = launch_serve_resid(s->p.precision, s->tab_dev, s->counters + 2 * K, s->resid_dev, grid, s->block, s->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(s->resid_host, s->resid_dev, sizeof(unsigned) * SERVE_MAX_ACTIVE,
                             cudaMemcpyDeviceToHost, s->stream);
@@ -313,11 +330,14 @@ int autotune(mglc_server* s) {
                 if (upload_table(s)) break;
                 cudaStreamSynchronize(s->stream);  // the pinned table is rewritten next round
                 const int grid = s->nsm * cp;
-                cudaMemsetAsync(s->counters, 0, sizeof(unsigned) * 8, s->stream);
-                launch_serve_step(s->p.precision, s->tab_dev, 0, s->counters, grid, blk, s->stream);
+                cudaMemsetAsync(s->counters, 0, sizeof(unsigned) * 10, s->stream);
+                launch_serve_step(s->p.precision, 0, s->tab_dev, 0, s->counters, grid, blk, s->stream);
+                launch_serve_step(s->p.precision, 1, s->tab_dev, 0, s->counters + 5, grid, blk, s->stream);
                 cudaEventRecord(a, s->stream);
-                for (int k = 0; k < 4; k++)
-                    launch_serve_step(s->p.precision, s->tab_dev, (k + 1) & 1, s->counters + 1 + k, grid, blk, s->stream);
+                for (int k = 0; k < 4; k++) {
+                    launch_serve_step(s->p.precision, 0, s->tab_dev, (k + 1) & 1, s->counters + 1 + k, grid, blk, s->stream);
+                    launch_serve_step(s->p.precision, 1, s->tab_dev, (k + 1) & 1, s->counters + 6 + k, grid, blk, s->stream);
+                }
                 cudaEventRecord(b, s->stream);
                 cudaEventSynchronize(b);
                 float ms = 0;
@@ -392,10 +412,13 @@ int mglc_server_create(const mglc_server_params* p, mglc_server** out) {
     SCK(cudaMallocHost((void**)&s->tab_host, sizeof(ServeTable)), "pinned table");
     std::memset(s->tab_host, 0, sizeof(ServeTable));
     SCK(cudaMalloc((void**)&s->tab_dev, sizeof(ServeTable)), "device table");
-    SCK(cudaMalloc((void**)&s->counters, sizeof(unsigned) * (p->steps_per_iteration + 8)), "counters");
+    SCK(cudaMalloc((void**)&s->counters, sizeof(unsigned) * (2 * p->steps_per_iteration + 8)), "counters");
     SCK(cudaMalloc((void**)&s->resid_dev, sizeof(unsigned) * SERVE_MAX_ACTIVE), "residuals");
     SCK(cudaMallocHost((void**)&s->resid_host, sizeof(unsigned) * SERVE_MAX_ACTIVE), "pinned residuals");
     SCK(cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming), "event");
+    SCK(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking), "side stream");
+    SCK(cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming), "fork event");
+    SCK(cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming), "join event");
     return MGLC_OK;
 }
 
@@ -404,6 +427,9 @@ void mglc_server_destroy(mglc_server* s) {
     if (s->stream) cudaStreamSynchronize(s->stream);
     if (s->graph) cudaGraphExecDestroy(s->graph);
     if (s->done) cudaEventDestroy(s->done);
+    if (s->fork) cudaEventDestroy(s->fork);
+    if (s->join) cudaEventDestroy(s->join);
+    if (s->side) cudaStreamDestroy(s->side);
     if (s->arena_mem) cudaFree(s->arena_mem);
     if (s->tab_dev) cudaFree(s->tab_dev);
     if (s->counters) cudaFree(s->counters);

@@ -25,16 +25,20 @@ struct ServeSolve {
     StepK<float> K;
 };
 
+// Active solves, lid-driven ones first: tiles [0, lid_tiles) belong to lid
+// solves, tiles [lid_tiles, total_tiles) to heated ones.
 struct ServeTable {
     int n_active;
     int total_tiles;
+    int lid_tiles;
     int rows_per_tile;
     ServeSolve s[SERVE_MAX_ACTIVE];
 };
 
-// One time step of every active solve (parity selects the ping-pong buffer).
-cudaError_t launch_serve_step(int form, const ServeTable* tab, int parity, unsigned* counter,
-                              int grid, int block, cudaStream_t st);
+// One time step of every active solve of one kind (parity selects the
+// ping-pong buffer); thermal = 0 runs the lid tiles, 1 the heated ones.
+cudaError_t launch_serve_step(int form, int thermal, const ServeTable* tab, int parity,
+                              unsigned* counter, int grid, int block, cudaStream_t st);
 // resid[s] = max over cells of |u - uprev| / uref (as float bits); uprev <- u
 cudaError_t launch_serve_resid(int form, const ServeTable* tab, unsigned* counter,
                                unsigned* resid, int grid, int block, cudaStream_t st);
