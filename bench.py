@@ -5,12 +5,13 @@ Re=1000, U=0.1, FP64 plain method (the drop-in).  A "step" is one fused time
 step over the whole lattice.  ``value`` is MLUPS with the state resident in
 HBM; ``e2e`` is the same metric through the C-ABI with host buffers (initial
 state uploaded from pinned host memory, K steps, macroscopic fields read back)
-inside the timed region.  The other storage forms (FP32 / FP16 / BF16
-deviations, FP32 arithmetic) are timed on the same workload and reported under
-``forms``.
+inside the timed region.  The other forms (FX64: FP64 storage with the
+fixed-point collision; FP32 / FP16 / BF16 deviations with FP32 arithmetic) are
+timed on the same workload and reported under ``forms``.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mglc|reference]
-                    [--workload lid384|lid64|thermal128] [--form fp64|fp32|fp16|bf16]
+                    [--workload lid384|lid64|thermal128|particles]
+                    [--form fp64|fx64|fp32|fp16|bf16]
 
 Multi-GPU: replicas only (one independent cavity per GPU, no inter-GPU
 traffic); launched by torchrun, rank 0 prints max-over-ranks timing.
@@ -443,7 +444,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="mglc", choices=["mglc", "reference"])
     ap.add_argument("--workload", default="lid384", choices=sorted(WORKLOADS))
-    ap.add_argument("--form", default="fp64", choices=["fp64", "fp32", "fp16", "bf16"])
+    ap.add_argument("--form", default="fp64", choices=["fp64", "fx64", "fp32", "fp16", "bf16"])
     ap.add_argument("--no-forms", action="store_true", help="skip timing the other storage forms")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
@@ -495,7 +496,7 @@ def main():
         "metric": METRIC, "value": round(value, 3), "unit": "MLUPS", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if args.form == "fp64" else "f32",
+        "dtype": {"fp64": "f64", "fx64": "i64 Q55 fixed point (f64 storage)"}.get(args.form, "f32"),
         "data": wl.get("data", "synthetic (analytic cavity initial state, no dataset)"),
         "config": {"workload": wl["desc"], "form": args.form, "cells": cells,
                    "parallelism": f"replicas{world}" if world > 1 else "single",
@@ -515,7 +516,9 @@ def main():
                                "+ mglc_check, wall clock"}
     if rank == 0 and not args.no_forms:
         forms = {}
-        for fm in (("fp64", "fp32") if wl["kind"] == "particle" else ("fp64", "fp32", "fp16", "bf16")):
+        fms = {"particle": ("fp64", "fp32"), "thermal": ("fp64", "fp32", "fp16", "bf16"),
+               "lid": ("fp64", "fx64", "fp32", "fp16", "bf16")}[wl["kind"]]
+        for fm in fms:
             if fm == args.form:
                 continue
             try:

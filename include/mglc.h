@@ -40,8 +40,11 @@ extern "C" {
 /* Storage / arithmetic form of the populations.
  *  FP64: FP64 storage and FP64 arithmetic -- the drop-in for the reference.
  *  FP32/FP16/BF16: populations stored as deviations f_i - w_i*rho0 in that
- *  type, FP32 arithmetic; FP64 kept for reductions (residual, totals). */
-enum { MGLC_FP64 = 0, MGLC_FP32 = 1, MGLC_FP16 = 2, MGLC_BF16 = 3 };
+ *  type, FP32 arithmetic; FP64 kept for reductions (residual, totals).
+ *  FX64 (lid-driven cavity only): FP64 storage; the collision runs in 64-bit
+ *  fixed point with 55 fractional bits (exact moment transforms, one rounding
+ *  to FP64 per stored population), everything else as FP64. */
+enum { MGLC_FP64 = 0, MGLC_FP32 = 1, MGLC_FP16 = 2, MGLC_BF16 = 3, MGLC_FX64 = 4 };
 
 enum { MGLC_KIND_LID = 1, MGLC_KIND_THERMAL = 2, MGLC_KIND_PARTICLE = 3 };
 
@@ -55,7 +58,7 @@ typedef struct mglc_lid_params {
     double rho0;                      /* initial density (1.0) */
     double u0;                        /* lid velocity (lattice units) */
     int top_layer_u0; /* 1: initial u = u0 on the top layer (initial.f90:55-61); 0: u = 0 */
-    int precision;    /* MGLC_FP64 ... MGLC_BF16 */
+    int precision;    /* MGLC_FP64 ... MGLC_FX64 */
 } mglc_lid_params;
 
 /* Buoyancy-driven cavity parameters:

@@ -22,6 +22,7 @@ using namespace mglc;
 
 struct mglc_ctx {
     int kind = 0, form = FORM_FP64;
+    bool fx64 = false;  // MGLC_FX64: FP64 storage (form FP64), Q55 fixed-point lid collision
     Geom geom{};
     long long n = 0;
     cudaStream_t stream = nullptr;
@@ -246,14 +247,16 @@ int mglc_lid_create(const mglc_lid_params* p, mglc_ctx** out) {
     *out = nullptr;
     mglc_ctx* c = new mglc_ctx();
     int rc = check_geom(c, p->total_nx, p->total_ny, p->total_nz);
-    if (!rc && !valid_form(p->precision)) rc = fail(c, MGLC_ERR_INVALID, "unknown precision %d", p->precision);
+    if (!rc && !valid_form(p->precision) && p->precision != MGLC_FX64)
+        rc = fail(c, MGLC_ERR_INVALID, "unknown precision %d", p->precision);
     if (!rc && !(p->reynolds > 0.0)) rc = fail(c, MGLC_ERR_INVALID, "reynolds must be positive");
     if (rc) {
         *out = c;  // caller reads the message, then destroys
         return rc;
     }
     c->kind = MGLC_KIND_LID;
-    c->form = p->precision;
+    c->fx64 = p->precision == MGLC_FX64;
+    c->form = c->fx64 ? FORM_FP64 : p->precision;
     c->geom = {p->total_nx, p->total_ny, p->total_nz,
                (long long)p->total_nx * p->total_ny * p->total_nz};
     c->n = c->geom.plane;
@@ -281,6 +284,8 @@ int mglc_thermal_create(const mglc_thermal_params* p, mglc_ctx** out) {
     *out = nullptr;
     mglc_ctx* c = new mglc_ctx();
     int rc = check_geom(c, p->total_nx, p->total_ny, p->total_nz);
+    if (!rc && p->precision == MGLC_FX64)
+        rc = fail(c, MGLC_ERR_UNSUPPORTED, "MGLC_FX64 is implemented for the lid-driven cavity only");
     if (!rc && !valid_form(p->precision)) rc = fail(c, MGLC_ERR_INVALID, "unknown precision %d", p->precision);
     if (!rc && !(p->rayleigh > 0.0 && p->prandtl > 0.0 && p->mach > 0.0))
         rc = fail(c, MGLC_ERR_INVALID, "rayleigh, prandtl and mach must be positive");
@@ -348,7 +353,7 @@ int mglc_get_info(const mglc_ctx* c, mglc_info* o) {
     if (!c || !o) return MGLC_ERR_INVALID;
     std::memset(o, 0, sizeof *o);
     o->kind = c->kind;
-    o->precision = c->form;
+    o->precision = c->fx64 ? MGLC_FX64 : c->form;
     o->nx = c->geom.nx;
     o->ny = c->geom.ny;
     o->nz = c->geom.nz;
@@ -532,7 +537,8 @@ int mglc_step(mglc_ctx* c, int nsteps) {
             a.scale = c->scale;
             a.inv_scale = c->inv_scale;
             a.rho = c->rho; a.u = c->u; a.v = c->v; a.w = c->w;
-            e = launch_lid_step(c->form, c->first_pending, c->f[c->cur], c->f[nxt], a, c->stream);
+            e = launch_lid_step(c->fx64 ? FORM_FX64 : c->form, c->first_pending, c->f[c->cur],
+                                c->f[nxt], a, c->stream);
         } else {
             ThermalStepArgs a;
             a.g = c->geom;
@@ -726,7 +732,7 @@ int mglc_particle_create(const mglc_particle_params* p, const double* centers, i
     if ((rc = dalloc(c, (void**)&d.prep_sum, v3 / 3, "particle sums"))) return rc;
     if ((rc = dalloc(c, (void**)&d.prep_cnt, sizeof(int) * (size_t)(np > 0 ? np : 1), "particle sums"))) return rc;
     d.nblocks = particle_bulk_blocks(pp);
-    // bulk partials (2 per block) and the 2 x 32 stage-two sums of the finish kernel
+    // bulk partials (2 per warp) and the 2 x 32 stage-two sums of the finish kernel
     if ((rc = dalloc(c, (void**)&d.partials, sizeof(double) * (2 * (size_t)d.nblocks + 64), "bulk partials"))) return rc;
     if ((rc = dalloc(c, (void**)&d.n_fluid, 2 * sizeof(long long), "fluid count"))) return rc;
     if ((rc = dalloc(c, (void**)&d.rho_avg, 4 * sizeof(double), "average density"))) return rc;

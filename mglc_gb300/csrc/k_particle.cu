@@ -109,26 +109,39 @@ __device__ __forceinline__ void block_sum_to(double (&v)[NV], double* out, int s
 template <typename S> struct PC { using C = double; };
 template <> struct PC<float> { using C = float; };
 
-template <typename S, bool FIRST>
-__global__ void __launch_bounds__(128)
+// per-step constants of the bulk kernel in its arithmetic type (converted
+// once on the host: double -> float conversions are slow on the device)
+template <typename C> struct PBulkK {
+    C rho0, ax, ay, az;
+};
+
+// One thread per node of an x-row segment.  Fluid nodes collide and push
+// their populations (walls at y, z and, unless periodic, x bounce them back in
+// place); solid nodes do nothing.  Each warp writes its partial sums of the
+// fluid density before collision and of the post-collision mass to its own
+// slot, so no block barrier is needed and the totals are added in a fixed
+// order by k_pfinish.
+template <typename S, bool FIRST, typename IDX>
+__global__ void __launch_bounds__(128, (sizeof(S) == 4 ? 6 : 4))
     k_pbulk(const S* __restrict__ fin, S* __restrict__ fout, const int* __restrict__ owner,
-            PartParams p, MrtCoef<typename PC<S>::C> cd, double* partials, const int* status) {
+            PartParams p, MrtCoef<typename PC<S>::C> cd, PBulkK<typename PC<S>::C> bk,
+            double* partials, const int* status) {
     using C = typename PC<S>::C;
     constexpr bool DEV = PSt<S>::SHIFT;
     if (status[0]) return;
     const int nx = p.nx, ny = p.ny, nz = p.nz;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y, k = blockIdx.z;
-    const long long P = (long long)nx * ny * nz;
+    const IDX P = (IDX)nx * ny * nz;
     C cacc[2] = {C(0), C(0)};  // per-cell sums in the arithmetic type, widened per warp
     const bool active = i < nx;
-    const long long cell = (long long)i + (long long)nx * (j + (long long)ny * k);
-    if (active && owner[cell] < 0) {
+    const IDX cell = (IDX)i + (IDX)nx * ((IDX)j + (IDX)ny * k);
+    const bool fluid = active && owner[cell] < 0;
+    if (fluid) {
         C f[Q19];
 #pragma unroll
         for (int q = 0; q < Q19; q++) f[q] = (C)fin[q * P + cell];
-        const C rho0 = (C)p.rho0;
-        const C ax = (C)p.body_force[0], ay = (C)p.body_force[1], az = (C)p.body_force[2];
+        const C rho0 = bk.rho0, ax = bk.ax, ay = bk.ay, az = bk.az;
         C rho_m, rho, ux, uy, uz;
         if (FIRST) {  // the reference's initial fields: rho0, u = 0
             rho = rho0;
@@ -150,12 +163,12 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
         for (int q = 0; q < Q19; q++) m += f[q];
         cacc[1] = m;
-        const long long sy = nx, sz = (long long)nx * ny;
+        const IDX sy = nx, sz = (IDX)nx * ny;
         if (i > 0 && i < nx - 1 && j > 0 && j < ny - 1 && k > 0 && k < nz - 1) {
             // interior node: every population streams, no wrap
 #pragma unroll
             for (int q = 0; q < Q19; q++)
-                fout[q * P + cell + ex19(q) + ey19(q) * sy + ez19(q) * sz] = (S)f[q];
+                fout[q * P + cell + (IDX)ex19(q) + (IDX)ey19(q) * sy + (IDX)ez19(q) * sz] = (S)f[q];
         } else {
 #pragma unroll
             for (int q = 0; q < Q19; q++) {
@@ -166,7 +179,7 @@ __global__ void __launch_bounds__(128)
                     fout[opp19(q) * P + cell] = (S)f[q];  // no-slip wall
                 } else {
                     const int ii = wrapx(ir, nx);
-                    fout[q * P + ((long long)ii + sy * jj + sz * kk)] = (S)f[q];
+                    fout[q * P + ((IDX)ii + sy * jj + sz * kk)] = (S)f[q];
                 }
             }
         }
@@ -176,26 +189,15 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) cacc[q] += __shfl_down_sync(0xffffffffu, cacc[q], o);
     // fluid cells of this warp (deviation storage adds rho0 for each of them)
-    const unsigned fl = __ballot_sync(0xffffffffu, active && owner[active ? cell : 0] < 0);
-    // FP64 only for the warp leaders: one value per warp, then thread 0 adds the warps
-    __shared__ double s_w[2][4];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) {
-        const double nf = DEV ? (double)__popc(fl) * p.rho0 : 0.0;
-        s_w[0][wid] = (double)cacc[0] + nf;
-        s_w[1][wid] = (double)cacc[1] + nf;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
+    const unsigned fl = __ballot_sync(0xffffffffu, fluid);
+    if ((threadIdx.x & 31) == 0) {  // FP64 only for the warp leaders
+        const int nw = blockDim.x >> 5;
         const int b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-        const int nb = gridDim.x * gridDim.y * gridDim.z, nw = (blockDim.x + 31) >> 5;
-        double a0 = 0.0, a1 = 0.0;
-        for (int q = 0; q < nw; q++) {
-            a0 += s_w[0][q];
-            a1 += s_w[1][q];
-        }
-        partials[b] = a0;
-        partials[nb + b] = a1;
+        const int slot = b * nw + (threadIdx.x >> 5);
+        const int nslot = gridDim.x * gridDim.y * gridDim.z * nw;
+        const double nf = DEV ? (double)__popc(fl) * p.rho0 : 0.0;
+        partials[slot] = (double)cacc[0] + nf;
+        partials[nslot + slot] = (double)cacc[1] + nf;
     }
 }
 
@@ -284,57 +286,98 @@ __device__ __forceinline__ L fp_dev(const S* f, int q, int i, int j, int k, cons
     return (L)((double)f[idx] - w19(qq) * p.rho0);
 }
 
+// Direction components for a direction index held in a register: 2-bit
+// fields (component + 1) of one 64-bit constant per axis, so no compare chain.
+__host__ __device__ constexpr unsigned long long pack_e(int axis) {
+    unsigned long long v = 0;
+    for (int a = 0; a < Q19; a++) {
+        const int e = axis == 0 ? ex19(a) : (axis == 1 ? ey19(a) : ez19(a));
+        v |= (unsigned long long)(e + 1) << (2 * a);
+    }
+    return v;
+}
+__device__ __forceinline__ int e_rt(unsigned long long pack, int a) {
+    return (int)((pack >> (2 * a)) & 3ull) - 1;
+}
+constexpr unsigned long long EX_PACK = pack_e(0), EY_PACK = pack_e(1), EZ_PACK = pack_e(2);
+__host__ __device__ constexpr int opp_rt(int a) {
+    // 1<->2, 3<->4, 5<->6; 7<->10, 8<->9, 11<->14, 12<->13, 15<->18, 16<->17
+    return a <= 6 ? (a & 1 ? a + 1 : a - 1) : ((a - 7) & 3) == 0 ? a + 3 : ((a - 7) & 3) == 3 ? a - 3
+                                            : ((a - 7) & 3) == 1 ? a + 1 : a - 1;
+}
+
+constexpr bool opp_rt_ok() {
+    for (int a = 1; a < Q19; a++)
+        if (opp_rt(a) != opp19(a)) return false;
+    return true;
+}
+static_assert(opp_rt_ok(), "opp_rt must match opp19");
+
+// Link-list capacity of k_plinks: one scan round adds at most PB * 18 links,
+// so the list is processed as soon as fewer than that many slots are free.
+constexpr int LINK_CAP = PB * 27;
+
 // The interpolation weights of the quadratic bounce-back sum to one, so it is
-// applied to deviations directly.  The momentum exchange
-//   (e - u_w) fp - (-e - u_w) f_new = 2 e w rho0 + (e - u_w) dfp + (e + u_w) df_new
-// adds its constant part 2 e w rho0 exactly in FP64; geometry (q, the wall
-// point, the wall velocity) is FP64 in both forms.
+// applied to deviations directly.  The momentum exchange of a link,
+//   (e - u_w) fp - (-e - u_w) f_new = 2 e w rho0 + (e - u_w) dfp + (e + u_w) df_new,
+// splits into a constant part and a small variable part.  The constant parts
+// are summed exactly as integers: with m = 2 (axis links, w = 1/18) or 1
+// (diagonal links, w = 1/36),
+//   sum 2 e w rho0        = rho0/18 * sum m e
+//   sum r x (2 e w rho0)  = rho0/18 * (sum m n x e - X x sum m e)
+// because r = o + q e gives r x e = o x e, and o = n - X with n the node's
+// (unwrapped) coordinates.  The variable parts use the population arithmetic
+// type; q (calQ2) is computed in FP64 in both forms.
 template <typename S>
 __global__ void __launch_bounds__(PB) k_plinks(S* __restrict__ f, PartParams p, PartDev d) {
     using L = typename PC<S>::C;
     if (d.status[0]) return;
     const int c = blockIdx.x, slab = blockIdx.y;
-    const double* X = d.xc + 3 * c;
-    const double* U = d.uc + 3 * c;
-    const double* O = d.om + 3 * c;
-    const double R = p.radius, ravg = d.rho_avg[0];
+    const double X0 = d.xc[3 * c], X1 = d.xc[3 * c + 1], X2 = d.xc[3 * c + 2];
+    const L Ux = (L)d.uc[3 * c], Uy = (L)d.uc[3 * c + 1], Uz = (L)d.uc[3 * c + 2];
+    const L Ox = (L)d.om[3 * c], Oy = (L)d.om[3 * c + 1], Oz = (L)d.om[3 * c + 2];
+    const double R = p.radius;
+    const L ravg = (L)d.rho_avg[0];
     const int nx = p.nx, ny = p.ny, nz = p.nz;
     const long long P = (long long)nx * ny * nz;
     // box of nodes within R+2 of the centre (1-based coordinate = index + 1)
     const int h = (int)ceil(R) + 2;
-    const int ci = (int)floor(X[0]) - 1, cj = (int)floor(X[1]) - 1, ck = (int)floor(X[2]) - 1;
+    const int ci = (int)floor(X0) - 1, cj = (int)floor(X1) - 1, ck = (int)floor(X2) - 1;
     const int bw = 2 * h + 2;
     const int kz0 = slab * bw / NSLAB, kz1 = (slab + 1) * bw / NSLAB;
-    const long long nbox = (long long)bw * bw * (kz1 - kz0);
+    const int nbox = bw * bw * (kz1 - kz0);
     const double reach2 = (R + 1.8) * (R + 1.8);  // |x - X| <= R + sqrt(2) for a link
-    double acc[7] = {0, 0, 0, 0, 0, 0, 0};
-    // Links are first listed per round of PB box nodes (cell, direction) and
-    // then processed one per thread, so that the heavy link arithmetic runs
-    // with full warps instead of once per direction with a few lanes.
-    __shared__ long long s_cell[PB * 18];
-    __shared__ unsigned char s_dir[PB * 18];
+    int nf[3] = {0, 0, 0};  // sum m e
+    int nt[3] = {0, 0, 0};  // sum m (n x e)
+    L av[7] = {L(0), L(0), L(0), L(0), L(0), L(0), L(0)};  // variable force, torque, mass change
+    // Links are listed (box index, direction) over the scan rounds of PB box
+    // nodes, in a deterministic order, and processed one per thread once the
+    // list is nearly full or the box is done.
+    __shared__ int s_t[LINK_CAP];
+    __shared__ unsigned char s_dir[LINK_CAP];
     __shared__ int s_n;
     __shared__ int s_wsum[PB / 32];
-    for (long long t0 = 0; t0 < nbox; t0 += PB) {
+    if (threadIdx.x == 0) s_n = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int t0 = 0; t0 < nbox; t0 += PB) {
         unsigned my_dirs = 0;  // bit a: direction a is a boundary link of my node
-        long long my_cell = 0;
-        const long long t = t0 + threadIdx.x;
+        const int t = t0 + threadIdx.x;
         if (t < nbox) {
-            const int bi = (int)(t % bw), bj = (int)((t / bw) % bw), bk = kz0 + (int)(t / ((long long)bw * bw));
+            const int bi = t % bw, bj = (t / bw) % bw, bk = kz0 + t / (bw * bw);
             int i = ci - h + bi;
             const int j = cj - h + bj, k = ck - h + bk;
             bool ok = !(j < 0 || j >= ny || k < 0 || k >= nz);
             if (ok) {
-                const double ox = dxp((double)(i + 1), X[0], p), oy = (double)(j + 1) - X[1],
-                             oz = (double)(k + 1) - X[2];
+                const double ox = dxp((double)(i + 1), X0, p), oy = (double)(j + 1) - X1,
+                             oz = (double)(k + 1) - X2;
                 ok = ox * ox + oy * oy + oz * oz <= reach2;
             }
             if (ok) {
                 if (p.periodic_x) i = wrapx(i, nx);
                 else ok = i >= 0 && i < nx;
             }
-            const long long cell = i + (long long)nx * (j + (long long)ny * k);
-            if (ok && d.owner_cur[cell] < 0) {
+            if (ok && d.owner_cur[i + (long long)nx * (j + (long long)ny * k)] < 0) {
                 for (int a = 1; a < Q19; a++) {
                     const int jn = j + ey19(a), kn = k + ez19(a);
                     if (jn < 0 || jn >= ny || kn < 0 || kn >= nz) continue;
@@ -344,13 +387,11 @@ __global__ void __launch_bounds__(PB) k_plinks(S* __restrict__ f, PartParams p, 
                     if (d.owner_cur[in + (long long)nx * (jn + (long long)ny * kn)] != c) continue;
                     my_dirs |= 1u << a;
                 }
-                my_cell = cell;
             }
         }
         // deterministic slots: exclusive prefix sum of the per-thread link counts
         const int cnt = __popc(my_dirs);
         int incl = cnt;
-        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const int v = __shfl_up_sync(0xffffffffu, incl, o);
@@ -359,7 +400,7 @@ __global__ void __launch_bounds__(PB) k_plinks(S* __restrict__ f, PartParams p, 
         if (lane == 31) s_wsum[wid] = incl;
         __syncthreads();
         if (threadIdx.x == 0) {
-            int run = 0;
+            int run = s_n;
             for (int q = 0; q < PB / 32; q++) {
                 const int v = s_wsum[q];
                 s_wsum[q] = run;
@@ -370,78 +411,109 @@ __global__ void __launch_bounds__(PB) k_plinks(S* __restrict__ f, PartParams p, 
         __syncthreads();
         int slot = s_wsum[wid] + incl - cnt;
         for (unsigned m = my_dirs; m; m &= m - 1) {
-            s_cell[slot] = my_cell;
+            s_t[slot] = t;
             s_dir[slot] = (unsigned char)(__ffs(m) - 1);
             slot++;
         }
-        __syncthreads();
         const int nl = s_n;
+        if (nl <= LINK_CAP - PB * 18 && t0 + PB < nbox) continue;  // uniform over the block
+        __syncthreads();
         for (int e = threadIdx.x; e < nl; e += PB) {
-            const long long cell = s_cell[e];
-            const int a = s_dir[e];
-            const int i = (int)(cell % nx), j = (int)((cell / nx) % ny), k = (int)(cell / ((long long)nx * ny));
-            const double ox = dxp((double)(i + 1), X[0], p), oy = (double)(j + 1) - X[1],
-                         oz = (double)(k + 1) - X[2];
-            const int ea = ex19(a), eb = ey19(a), ec = ez19(a);
+            const int tt = s_t[e], a = s_dir[e];
+            const int bi = tt % bw, bj = (tt / bw) % bw, bk = kz0 + tt / (bw * bw);
+            const int iu = ci - h + bi, j = cj - h + bj, k = ck - h + bk;  // iu: unwrapped
+            const int i = p.periodic_x ? wrapx(iu, nx) : iu;
+            const int ea = e_rt(EX_PACK, a), eb = e_rt(EY_PACK, a), ec = e_rt(EZ_PACK, a);
+            const int m = a <= 6 ? 2 : 1;
+            // the node lies within R + 1.8 < nx / 2 of the centre: the unwrapped
+            // difference is the periodic minimum image
+            const double ox = (double)(iu + 1) - X0, oy = (double)(j + 1) - X1,
+                         oz = (double)(k + 1) - X2;
             // q: ray-sphere root from the node (calQ2, particle_bounceback.F90:144-185)
-            const double ca = (double)(ea * ea + eb * eb + ec * ec);
-            const double cb = 2.0 * (ea * ox + eb * oy + ec * oz);
+            const double sx = ea > 0 ? ox : (ea < 0 ? -ox : 0.0);
+            const double sy = eb > 0 ? oy : (eb < 0 ? -oy : 0.0);
+            const double sz = ec > 0 ? oz : (ec < 0 ? -oz : 0.0);
+            const double cb = 2.0 * (sx + sy + sz);
             const double cc = ox * ox + oy * oy + oz * oz - R * R;
-            const double delta = cb * cb - 4.0 * ca * cc;
+            const double delta = cb * cb - (a <= 6 ? 4.0 : 8.0) * cc;
             if (delta < 0) { atomicCAS(d.status, 0, PS_Q_RANGE); d.status[1] = c; continue; }
-            const double q = (-cb - sqrt(delta)) * (ca == 1.0 ? 0.5 : 0.25);  // /(2 ca), exact
-            if (q > 1.0 || q < 0.0) { atomicCAS(d.status, 0, PS_Q_RANGE); d.status[1] = c; continue; }
+            const double qd = (-cb - sqrt(delta)) * (a <= 6 ? 0.5 : 0.25);  // /(2 |e|^2), exact
+            if (qd > 1.0 || qd < 0.0) { atomicCAS(d.status, 0, PS_Q_RANGE); d.status[1] = c; continue; }
+            // constant parts (integers)
+            const int n0 = iu + 1, n1 = j + 1, n2 = k + 1;
+            nf[0] += m * ea;
+            nf[1] += m * eb;
+            nf[2] += m * ec;
+            nt[0] += m * (n1 * ec - n2 * eb);
+            nt[1] += m * (n2 * ea - n0 * ec);
+            nt[2] += m * (n0 * eb - n1 * ea);
             // wall point relative to the centre and its velocity U + Omega x r
-            const double rx = ox + q * ea, ry = oy + q * eb, rz = oz + q * ec;
-            const double uw0 = U[0] + (O[1] * rz - O[2] * ry);
-            const double uw1 = U[1] + (O[2] * rx - O[0] * rz);
-            const double uw2 = U[2] + (O[0] * ry - O[1] * rx);
-            const int ra = opp19(a);
-            const double w = w19(a);
-            const L mv = (L)(6.0 * w * ravg * (-ea * uw0 - eb * uw1 - ec * uw2));  // moving-wall term
+            const L q = (L)qd;
+            const L rx = (L)ox + q * (L)ea, ry = (L)oy + q * (L)eb, rz = (L)oz + q * (L)ec;
+            const L uw0 = Ux + (Oy * rz - Oz * ry);
+            const L uw1 = Uy + (Oz * rx - Ox * rz);
+            const L uw2 = Uz + (Ox * ry - Oy * rx);
+            const int ra = opp_rt(a);
+            const L w = a <= 6 ? L(1.0 / 18.0) : L(1.0 / 36.0);
+            const L mv = L(6) * w * ravg * (-(L)ea * uw0 - (L)eb * uw1 - (L)ec * uw2);  // moving wall
             const L dpa = fp_dev<S, L>(f, a, i, j, k, p);
             L dn;
-            if (q < 0.5) {
-                const L c0 = (L)(q * (1.0 + 2.0 * q)), c1 = (L)(1.0 - 4.0 * q * q),
-                        c2 = (L)(q * (1.0 - 2.0 * q));
+            if (q < L(0.5)) {
+                const L c0 = q * (L(1) + L(2) * q), c1 = L(1) - L(4) * q * q, c2 = q * (L(1) - L(2) * q);
                 const L d1 = fp_dev<S, L>(f, a, i - ea, j - eb, k - ec, p);
                 const L d2 = fp_dev<S, L>(f, a, i - 2 * ea, j - 2 * eb, k - 2 * ec, p);
                 dn = c0 * dpa + c1 * d1 - c2 * d2 + mv;
             } else {
-                const double iq = 1.0 / q, i2 = 1.0 / (1.0 + 2.0 * q), a2 = 2.0 * q - 1.0;
+                const L iq = L(1) / q, i2 = L(1) / (L(1) + L(2) * q), a2 = L(2) * q - L(1);
                 const L g0 = fp_dev<S, L>(f, ra, i, j, k, p);
                 const L g1 = fp_dev<S, L>(f, ra, i - ea, j - eb, k - ec, p);
-                dn = (L)(iq * i2) * dpa + (L)(a2 * iq) * g0 - (L)(a2 * i2) * g1 + (L)(iq * i2) * mv;
+                dn = (iq * i2) * dpa + (a2 * iq) * g0 - (a2 * i2) * g1 + (iq * i2) * mv;
             }
-            const long long slot = ra * P + cell;
+            const long long fslot = ra * P + (i + (long long)nx * (j + (long long)ny * k));
             if (PSt<S>::SHIFT) {
-                f[slot] = (S)dn;
-                dn = (L)f[slot];  // as stored
+                f[fslot] = (S)dn;
+                dn = (L)f[fslot];  // as stored
             } else {
-                f[slot] = (S)((double)dn + w * p.rho0);
-                dn = (L)((double)f[slot] - w * p.rho0);
+                const double wd = a <= 6 ? 1.0 / 18.0 : 1.0 / 36.0;
+                f[fslot] = (S)((double)dn + wd * p.rho0);
+                dn = (L)((double)f[fslot] - wd * p.rho0);
             }
-            // Wen et al. 2014 Galilean-invariant momentum exchange
-            const double F0 = 2.0 * ea * w * p.rho0 + (double)((ea - (L)uw0) * dpa + (ea + (L)uw0) * dn);
-            const double F1 = 2.0 * eb * w * p.rho0 + (double)((eb - (L)uw1) * dpa + (eb + (L)uw1) * dn);
-            const double F2 = 2.0 * ec * w * p.rho0 + (double)((ec - (L)uw2) * dpa + (ec + (L)uw2) * dn);
-            acc[0] += F0;
-            acc[1] += F1;
-            acc[2] += F2;
-            acc[3] += ry * F2 - rz * F1;
-            acc[4] += rz * F0 - rx * F2;
-            acc[5] += rx * F1 - ry * F0;
-            acc[6] += (double)(dn - dpa);
+            // Wen et al. 2014 Galilean-invariant momentum exchange, variable part
+            const L F0 = ((L)ea - uw0) * dpa + ((L)ea + uw0) * dn;
+            const L F1 = ((L)eb - uw1) * dpa + ((L)eb + uw1) * dn;
+            const L F2 = ((L)ec - uw2) * dpa + ((L)ec + uw2) * dn;
+            av[0] += F0;
+            av[1] += F1;
+            av[2] += F2;
+            av[3] += ry * F2 - rz * F1;
+            av[4] += rz * F0 - rx * F2;
+            av[5] += rx * F1 - ry * F0;
+            av[6] += dn - dpa;
         }
         __syncthreads();
+        if (threadIdx.x == 0) s_n = 0;
     }
-    __shared__ double out[7];
-    block_sum_to<7>(acc, out, 1);
+    double acc[13];
+#pragma unroll
+    for (int q = 0; q < 7; q++) acc[q] = (double)av[q];
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        acc[7 + q] = (double)nf[q];  // integers: the block sums are exact
+        acc[10 + q] = (double)nt[q];
+    }
+    __shared__ double out[13];
+    block_sum_to<13>(acc, out, 1);
     if (threadIdx.x == 0) {
+        const double k0 = p.rho0 / 18.0;
+        const double NF0 = out[7], NF1 = out[8], NF2 = out[9];
+        const double fc[3] = {k0 * NF0, k0 * NF1, k0 * NF2};
+        const double tc[3] = {k0 * (out[10] - (X1 * NF2 - X2 * NF1)),
+                              k0 * (out[11] - (X2 * NF0 - X0 * NF2)),
+                              k0 * (out[12] - (X0 * NF1 - X1 * NF0))};
         const int sl = c * NSLAB + slab;  // per-slab partials, summed in slab order by readers
         for (int q = 0; q < 3; q++) {
-            d.flink[3 * sl + q] = out[q];
-            d.tlink[3 * sl + q] = out[3 + q];
+            d.flink[3 * sl + q] = fc[q] + out[q];
+            d.tlink[3 * sl + q] = tc[q] + out[3 + q];
         }
         d.corr[sl] = out[6];
     }
@@ -830,20 +902,28 @@ static dim3 pblock(int nx) {
     int bx = ((nx + 31) / 32) * 32;
     return dim3(bx > 128 ? 128 : bx, 1, 1);
 }
+// number of per-warp partial slots of the bulk kernel
 int particle_bulk_blocks(const PartParams& p) {
     dim3 b = pblock(p.nx);
-    return ((p.nx + b.x - 1) / b.x) * p.ny * p.nz;
+    return ((p.nx + b.x - 1) / b.x) * p.ny * p.nz * (int)(b.x / 32);
 }
 
 template <typename S>
 static cudaError_t pstep_go(bool first, const void* fin, void* fout, const PartParams& p,
                             const PartDev& d, cudaStream_t s) {
+    using C = typename PC<S>::C;
     dim3 b = pblock(p.nx), g((p.nx + b.x - 1) / b.x, p.ny, p.nz);
-    MrtCoef<typename PC<S>::C> cd = cast_coef<typename PC<S>::C>(make_mrt_coef(p.snu, p.sq));
-    if (first)
-        k_pbulk<S, true><<<g, b, 0, s>>>((const S*)fin, (S*)fout, d.owner_cur, p, cd, d.partials, d.status);
-    else
-        k_pbulk<S, false><<<g, b, 0, s>>>((const S*)fin, (S*)fout, d.owner_cur, p, cd, d.partials, d.status);
+    MrtCoef<C> cd = cast_coef<C>(make_mrt_coef(p.snu, p.sq));
+    const PBulkK<C> bk = {(C)p.rho0, (C)p.body_force[0], (C)p.body_force[1], (C)p.body_force[2]};
+    // 32-bit indices while every population index (and the +-1 neighbour
+    // offsets) fits in int
+    const bool i32 = (long long)p.nx * p.ny * p.nz * (Q19 + 1) < (1LL << 31);
+    const S* fi = (const S*)fin;
+    S* fo = (S*)fout;
+    if (first && i32) k_pbulk<S, true, int><<<g, b, 0, s>>>(fi, fo, d.owner_cur, p, cd, bk, d.partials, d.status);
+    else if (first) k_pbulk<S, true, long long><<<g, b, 0, s>>>(fi, fo, d.owner_cur, p, cd, bk, d.partials, d.status);
+    else if (i32) k_pbulk<S, false, int><<<g, b, 0, s>>>(fi, fo, d.owner_cur, p, cd, bk, d.partials, d.status);
+    else k_pbulk<S, false, long long><<<g, b, 0, s>>>(fi, fo, d.owner_cur, p, cd, bk, d.partials, d.status);
     k_pfinish<<<FINISH_BLOCKS, 256, 0, s>>>(d, d.nblocks);
     k_pfinish2<<<1, 32, 0, s>>>(d, d.nblocks);
     if (p.np > 0) {

@@ -28,6 +28,16 @@ __global__ void __launch_bounds__(128)
     lid_cell<S, FIRST, IDX>(i, blockIdx.y, blockIdx.z, fin, fout, K, P, mrho, mu, mv, mw);
 }
 
+template <bool FIRST, typename IDX>
+__global__ void __launch_bounds__(128)
+    k_lid_step_fx(const double* __restrict__ fin, double* __restrict__ fout, FxK K, IDX P,
+                  const double* __restrict__ mrho, const double* __restrict__ mu,
+                  const double* __restrict__ mv, const double* __restrict__ mw) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= K.nx) return;
+    lid_cell_fx<FIRST, IDX>(i, blockIdx.y, blockIdx.z, fin, fout, K, P, mrho, mu, mv, mw);
+}
+
 template <typename S, bool FIRST, bool ROT, typename IDX>
 __global__ void __launch_bounds__(128)
     k_thermal_step(const S* __restrict__ fin, S* __restrict__ fout,
@@ -71,9 +81,30 @@ static cudaError_t lid_go(bool first, const void* fin, void* fout, const LidStep
     return cudaGetLastError();
 }
 
+static cudaError_t lid_go_fx(bool first, const void* fin, void* fout, const LidStepArgs& a,
+                             cudaStream_t s) {
+    FxK K;
+    K.nx = a.g.nx; K.ny = a.g.ny; K.nz = a.g.nz;
+    K.c = make_fx_coef(a.cd, a.u0);
+    dim3 b = step_block(a.g.nx), gr = step_grid(a.g, b);
+    const bool small = (long long)Q19 * a.g.plane < (1ll << 31);
+    const double* fi = (const double*)fin;
+    double* fo = (double*)fout;
+#define FX_LAUNCH(FI, IT) \
+    k_lid_step_fx<FI, IT><<<gr, b, 0, s>>>(fi, fo, K, (IT)a.g.plane, a.rho, a.u, a.v, a.w)
+    if (small) {
+        if (first) FX_LAUNCH(true, unsigned); else FX_LAUNCH(false, unsigned);
+    } else {
+        if (first) FX_LAUNCH(true, long long); else FX_LAUNCH(false, long long);
+    }
+#undef FX_LAUNCH
+    return cudaGetLastError();
+}
+
 cudaError_t launch_lid_step(int form, bool first, const void* fin, void* fout,
                             const LidStepArgs& a, cudaStream_t s) {
     switch (form) {
+        case FORM_FX64: return lid_go_fx(first, fin, fout, a, s);
         case FORM_FP64: return lid_go<double>(first, fin, fout, a, s);
         case FORM_FP32: return lid_go<float>(first, fin, fout, a, s);
         case FORM_FP16: return lid_go<__half>(first, fin, fout, a, s);

@@ -9,7 +9,9 @@
 namespace mglc {
 
 // Storage forms of the populations (mirrors MGLC_FP64 ... in mglc.h).
-enum Form { FORM_FP64 = 0, FORM_FP32 = 1, FORM_FP16 = 2, FORM_BF16 = 3 };
+// FORM_FX64: FP64 storage (the FP64 layout everywhere) with the Q55
+// fixed-point lid collision of fixed64.cuh
+enum Form { FORM_FP64 = 0, FORM_FP32 = 1, FORM_FP16 = 2, FORM_BF16 = 3, FORM_FX64 = 4 };
 
 inline size_t form_bytes(int form) { return form == FORM_FP64 ? 8 : form == FORM_FP32 ? 4 : 2; }
 

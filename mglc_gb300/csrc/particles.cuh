@@ -40,7 +40,7 @@ struct PartDev {
     double* prep_sum;                  // np: refill bookkeeping (density)
     int* prep_cnt;                     // np: refill bookkeeping (fluid count change)
     double* partials;                  // bulk-kernel block partials, 2 per block
-    int nblocks;                       // number of bulk-kernel blocks
+    int nblocks;                       // number of bulk-kernel partial slots (one per warp)
     long long* n_fluid;                // device scalar
     double* rho_avg;                   // device scalars: [0] at bounce-back, [1] after update
     int* status;                       // device: [0] code, [1] particle, [2] other particle
@@ -60,6 +60,6 @@ cudaError_t launch_particle_init(int form, void* f, const PartParams& p, const P
 cudaError_t launch_particle_macro(int form, bool first, const void* f, const PartParams& p,
                                   const PartDev& d, double* rho, double* u, double* v, double* w,
                                   cudaStream_t s);
-int particle_bulk_blocks(const PartParams& p);
+int particle_bulk_blocks(const PartParams& p);  // per-warp partial slots
 
 }  // namespace mglc

@@ -5,6 +5,7 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include "fixed64.cuh"
 #include "kernels.cuh"
 
 namespace mglc {
@@ -149,6 +150,76 @@ __device__ __forceinline__ void lid_cell(int i, int j, int k, const S* __restric
             C val = f[q];
             if (dz > 0 && dx != 0) val = val - C(dx) * lid;
             St<S>::st(fout + ((IDX)opp19(q) * P + cell), val, K.scale);
+        }
+    }
+}
+
+// ------------------------------------------------------ lid kernel, FX64 --
+// FP64 storage, Q55 fixed-point collision (fixed64.cuh); the same streaming,
+// halfway bounce-back and lid term as lid_cell.
+struct FxK {
+    int nx, ny, nz;
+    FxCoef c;
+};
+
+template <bool FIRST, typename IDX>
+__device__ __forceinline__ void lid_cell_fx(int i, int j, int k, const double* __restrict__ fin,
+                                            double* __restrict__ fout, const FxK& K, IDX P,
+                                            const double* __restrict__ mrho,
+                                            const double* __restrict__ mu,
+                                            const double* __restrict__ mv,
+                                            const double* __restrict__ mw) {
+    const int nx = K.nx, ny = K.ny, nz = K.nz;
+    const IDX cell = (IDX)i + (IDX)nx * ((IDX)j + (IDX)ny * (IDX)k);
+    long long f[Q19];
+    {
+        // all loads issued before any conversion
+        double raw[Q19];
+#pragma unroll
+        for (int q = 0; q < Q19; q++) raw[q] = __ldg(fin + ((IDX)q * P + cell));
+#pragma unroll
+        for (int q = 0; q < Q19; q++) f[q] = __double_as_longlong(raw[q]);
+    }
+    bool bad = false;
+#pragma unroll
+    for (int q = 0; q < Q19; q++) {
+        bad |= fx_bad(__longlong_as_double(f[q]));
+        f[q] = d2q(__longlong_as_double(f[q]));
+    }
+    long long rin = 0, uin = 0, vin = 0, win = 0;
+    if (FIRST) {
+        const double r = mrho[cell], a = mu[cell], b = mv[cell], c = mw[cell];
+        bad |= ((unsigned)(__double_as_longlong(r) >> 52) & 0x7FFu) >= 1024u;  // rho >= 2
+        bad |= fx_bad(a) || fx_bad(b) || fx_bad(c);
+        rin = d2q(r);
+        uin = d2q(a);
+        vin = d2q(b);
+        win = d2q(c);
+    }
+    long long rho;
+    bad |= !mrt_collide_fx<FIRST>(f, rin, uin, vin, win, K.c, rho);
+    const double nan = __longlong_as_double(0x7ff8000000000000LL);
+    const IDX sy = (IDX)nx, sz = (IDX)nx * (IDX)ny;
+    const unsigned bm = face_mask(i, j, k, nx, ny, nz);
+    if (bm == 0) {
+#pragma unroll
+        for (int q = 0; q < Q19; q++) {
+            const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
+            fout[(IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz] = bad ? nan : q2d(f[q]);
+        }
+        return;
+    }
+    // moving lid: f(14) = f_post(11) - rho/6*U0, f(13) = f_post(12) + rho/6*U0
+    const long long lid = k == nz - 1 ? qmulc(rho, K.c.u0_6) : 0LL;
+#pragma unroll
+    for (int q = 0; q < Q19; q++) {
+        const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
+        if ((bm & leave_bits(dx, dy, dz)) == 0) {
+            fout[(IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz] = bad ? nan : q2d(f[q]);
+        } else {
+            long long val = f[q];
+            if (dz > 0 && dx != 0) val -= dx * lid;
+            fout[(IDX)opp19(q) * P + cell] = bad ? nan : q2d(val);
         }
     }
 }
