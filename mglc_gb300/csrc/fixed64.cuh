@@ -71,6 +71,20 @@ __device__ __forceinline__ double q2d(long long v) {
     return __longlong_as_double((long long)(bits | ((unsigned long long)sg << 63)));
 }
 
+// The same two conversions on the FP64 unit, which the fixed-point collision
+// otherwise leaves idle: scaling by 2^+-55 is an exact integer add on the
+// exponent field, the conversion itself is one cvt instruction.
+// q2d_cvt(v) == q2d(v) for every v; d2q_cvt rounds ties to even (d2q: away
+// from zero), which differs only for inputs below 1/8 that end in exactly
+// half a unit of 2^-55.
+__device__ __forceinline__ double q2d_cvt(long long v) {
+    const long long b = __double_as_longlong((double)v);  // round to nearest even
+    return __longlong_as_double(v ? b - ((long long)FXQ << 52) : 0LL);
+}
+__device__ __forceinline__ long long d2q_cvt(double x) {
+    return __double2ll_rn(__longlong_as_double(__double_as_longlong(x) + ((long long)FXQ << 52)));
+}
+
 // (a * b) >> 55 for signed Q55 values (floor of the exact product)
 __device__ __forceinline__ long long qmul(long long a, long long b) {
     const long long hi = __mul64hi(a, b);

@@ -161,6 +161,14 @@ struct FxK {
     int nx, ny, nz;
     FxCoef c;
 };
+// populations converted on the FP64 unit (the rest with integer bit
+// operations), balancing that unit against the integer pipe
+#ifndef FX_CVT_IN
+#define FX_CVT_IN 17
+#endif
+#ifndef FX_CVT_OUT
+#define FX_CVT_OUT 17
+#endif
 
 template <bool FIRST, typename IDX>
 __device__ __forceinline__ void lid_cell_fx(int i, int j, int k, const double* __restrict__ fin,
@@ -184,7 +192,7 @@ __device__ __forceinline__ void lid_cell_fx(int i, int j, int k, const double* _
 #pragma unroll
     for (int q = 0; q < Q19; q++) {
         bad |= fx_bad(__longlong_as_double(f[q]));
-        f[q] = d2q(__longlong_as_double(f[q]));
+        f[q] = q < FX_CVT_IN ? d2q_cvt(__longlong_as_double(f[q])) : d2q(__longlong_as_double(f[q]));
     }
     long long rin = 0, uin = 0, vin = 0, win = 0;
     if (FIRST) {
@@ -198,29 +206,36 @@ __device__ __forceinline__ void lid_cell_fx(int i, int j, int k, const double* _
     }
     long long rho;
     bad |= !mrt_collide_fx<FIRST>(f, rin, uin, vin, win, K.c, rho);
+    // moving lid: f(14) = f_post(11) - rho/6*U0, f(13) = f_post(12) + rho/6*U0
+    // (bounce_back.f90:77-78); on the top layer populations 11 and 12 always
+    // leave through the lid, so the term is applied to them before rounding
+    if (k == nz - 1) {
+        const long long lid = qmulc(rho, K.c.u0_6);
+        f[11] -= lid;
+        f[12] += lid;
+    }
+    // one rounding per population; the store pattern below moves doubles only
+    double o[Q19];
     const double nan = __longlong_as_double(0x7ff8000000000000LL);
+#pragma unroll
+    for (int q = 0; q < Q19; q++) o[q] = bad ? nan : (q < FX_CVT_OUT ? q2d_cvt(f[q]) : q2d(f[q]));
     const IDX sy = (IDX)nx, sz = (IDX)nx * (IDX)ny;
     const unsigned bm = face_mask(i, j, k, nx, ny, nz);
     if (bm == 0) {
 #pragma unroll
         for (int q = 0; q < Q19; q++) {
             const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
-            fout[(IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz] = bad ? nan : q2d(f[q]);
+            fout[(IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz] = o[q];
         }
         return;
     }
-    // moving lid: f(14) = f_post(11) - rho/6*U0, f(13) = f_post(12) + rho/6*U0
-    const long long lid = k == nz - 1 ? qmulc(rho, K.c.u0_6) : 0LL;
 #pragma unroll
     for (int q = 0; q < Q19; q++) {
         const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
-        if ((bm & leave_bits(dx, dy, dz)) == 0) {
-            fout[(IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz] = bad ? nan : q2d(f[q]);
-        } else {
-            long long val = f[q];
-            if (dz > 0 && dx != 0) val -= dx * lid;
-            fout[(IDX)opp19(q) * P + cell] = bad ? nan : q2d(val);
-        }
+        if ((bm & leave_bits(dx, dy, dz)) == 0)
+            fout[(IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz] = o[q];
+        else
+            fout[(IDX)opp19(q) * P + cell] = o[q];
     }
 }
 
