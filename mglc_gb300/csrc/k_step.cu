@@ -28,11 +28,8 @@ __global__ void __launch_bounds__(128)
     lid_cell<S, FIRST, IDX>(i, blockIdx.y, blockIdx.z, fin, fout, K, P, mrho, mu, mv, mw);
 }
 
-#ifndef FX_MINB
-#define FX_MINB 1
-#endif
 template <bool FIRST, typename IDX>
-__global__ void __launch_bounds__(128, FX_MINB)
+__global__ void __launch_bounds__(128)
     k_lid_step_fx(const double* __restrict__ fin, double* __restrict__ fout, FxK K, IDX P,
                   const double* __restrict__ mrho, const double* __restrict__ mu,
                   const double* __restrict__ mv, const double* __restrict__ mw) {

@@ -18,6 +18,8 @@ struct St<double> {
     using C = double;
     static constexpr bool SHIFT = false;
     __device__ static C ld(const double* p, float) { return __ldg(p); }
+    __device__ static double raw(const double* p) { return __ldg(p); }
+    __device__ static C cvt(double v, float) { return v; }
     __device__ static void st(double* p, C v, float) { *p = v; }
 };
 template <>
@@ -25,6 +27,8 @@ struct St<float> {
     using C = float;
     static constexpr bool SHIFT = true;
     __device__ static C ld(const float* p, float) { return __ldg(p); }
+    __device__ static float raw(const float* p) { return __ldg(p); }
+    __device__ static C cvt(float v, float) { return v; }
     __device__ static void st(float* p, C v, float) { *p = v; }
 };
 template <>
@@ -32,6 +36,8 @@ struct St<__half> {
     using C = float;
     static constexpr bool SHIFT = true;
     __device__ static C ld(const __half* p, float inv) { return __half2float(__ldg(p)) * inv; }
+    __device__ static __half raw(const __half* p) { return __ldg(p); }
+    __device__ static C cvt(__half v, float inv) { return __half2float(v) * inv; }
     __device__ static void st(__half* p, C v, float sc) { *p = __float2half_rn(v * sc); }
 };
 template <>
@@ -41,6 +47,8 @@ struct St<__nv_bfloat16> {
     __device__ static C ld(const __nv_bfloat16* p, float inv) {
         return __bfloat162float(__ldg(p)) * inv;
     }
+    __device__ static __nv_bfloat16 raw(const __nv_bfloat16* p) { return __ldg(p); }
+    __device__ static C cvt(__nv_bfloat16 v, float inv) { return __bfloat162float(v) * inv; }
     __device__ static void st(__nv_bfloat16* p, C v, float sc) { *p = __float2bfloat16_rn(v * sc); }
 };
 
@@ -106,8 +114,14 @@ __device__ __forceinline__ void lid_cell(int i, int j, int k, const S* __restric
     const int nx = K.nx, ny = K.ny, nz = K.nz;
     const IDX cell = (IDX)i + (IDX)nx * ((IDX)j + (IDX)ny * (IDX)k);
     C f[Q19];
+    {
+        // every load is issued before the first conversion
+        S raw[Q19];
 #pragma unroll
-    for (int q = 0; q < Q19; q++) f[q] = St<S>::ld(fin + ((IDX)q * P + cell), K.inv_scale);
+        for (int q = 0; q < Q19; q++) raw[q] = St<S>::raw(fin + ((IDX)q * P + cell));
+#pragma unroll
+        for (int q = 0; q < Q19; q++) f[q] = St<S>::cvt(raw[q], K.inv_scale);
+    }
     C rho_m, rho, ux, uy, uz;
     if (FIRST) {
         rho = (C)mrho[cell];
