@@ -11,7 +11,8 @@ module mglc_iface
     implicit none
 
     integer(c_int), parameter :: MGLC_OK = 0
-    integer(c_int), parameter :: MGLC_FP64 = 0, MGLC_FP32 = 1, MGLC_FP16 = 2, MGLC_BF16 = 3
+    integer(c_int), parameter :: MGLC_FP64 = 0, MGLC_FP32 = 1, MGLC_FP16 = 2, MGLC_BF16 = 3, &
+                                  MGLC_FX64 = 4
 
     type, bind(C) :: mglc_lid_params
         integer(c_int) :: total_nx, total_ny, total_nz
