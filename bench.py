@@ -179,6 +179,15 @@ def l2_note(resident_bytes):
     return f"state fits in L2 ({mb:.0f} MB): parity-size workload, not a headline number"
 
 
+def max_over_ranks(torch, dist, x, device="cuda"):
+    """The slowest rank's time (replicas: the job finishes with its last rank)."""
+    if not dist:
+        return x
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def time_device(torch, mg, wl, form, steps, warmup, dist=None):
     """Device-resident MLUPS: state in HBM, K fused steps between CUDA events."""
     s = make_solve(mg, wl, form)
@@ -199,10 +208,7 @@ def time_device(torch, mg, wl, form, steps, warmup, dist=None):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     s.set_stream(None)
-    if dist:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(torch, dist, ms)
     info = s.info()
     s.close()
     return ms, info
@@ -245,10 +251,7 @@ def time_e2e(torch, mg, wl, form, steps, dist=None):
     capi.check(s.handle, L.mglc_check(s.handle, ctypes.byref(eu), None))
     t1 = time.perf_counter()
     dt = t1 - t0
-    if dist:
-        t = torch.tensor([dt], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dt = float(t.item())
+    dt = max_over_ranks(torch, dist, dt)
     s.close()
     h2d = 8 * (19 + q_g) * cells
     d2h = 8 * len(fields) * cells + 8
@@ -267,11 +270,13 @@ def time_e2e_particles(torch, s, wl, steps, dist=None):
     ptr = lambda a: a.ctypes.data
     s.initial()
     torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
     t0 = time.perf_counter()
     capi.check(s.handle, L.mglc_step(s.handle, steps))
     capi.check(s.handle, L.mglc_get_macros(s.handle, *[ptr(a) for a in fields], None))
     capi.check(s.handle, L.mglc_particle_state(s.handle, *[ptr(a) for a in st]))
-    dt = time.perf_counter() - t0
+    dt = max_over_ranks(torch, dist, time.perf_counter() - t0)
     s.close()
     return dt, 0, (8 * 4 * cells + 8 * 15 * wl["np"]) / steps, 0.0
 
@@ -508,7 +513,7 @@ def main():
         "clocks": clocks,
         "gpu_launches": args.steps * wl.get("launches_per_step", 1),
     }
-    if rank == 0 and not args.no_e2e:
+    if not args.no_e2e:  # every rank runs its replica end to end; the slowest one counts
         dt, h2d, d2h, eu = time_e2e(torch, mglc_gb300, wl, args.form, args.steps, dist)
         line["e2e"] = {"value": round(world * cells * args.steps / dt / 1e6, 3), "unit": "MLUPS",
                        "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),

@@ -317,6 +317,18 @@ static_assert(opp_rt_ok(), "opp_rt must match opp19");
 // so the list is processed as soon as fewer than that many slots are free.
 constexpr int LINK_CAP = PB * 27;
 
+// Is node (i, j, k) (0-based, x unwrapped) a fluid node, or a ghost beyond a
+// wall?  Only those have a post-collision value of this step.
+__device__ __forceinline__ bool node_avail(int i, int j, int k, const PartParams& p,
+                                           const int* __restrict__ owner) {
+    if (j < 0 || j >= p.ny || k < 0 || k >= p.nz) return true;
+    if (i < 0 || i >= p.nx) {
+        if (!p.periodic_x) return true;
+        i = wrapx(i, p.nx);
+    }
+    return owner[i + (long long)p.nx * (j + (long long)p.ny * k)] < 0;
+}
+
 // The interpolation weights of the quadratic bounce-back sum to one, so it is
 // applied to deviations directly.  The momentum exchange of a link,
 //   (e - u_w) fp - (-e - u_w) f_new = 2 e w rho0 + (e - u_w) dfp + (e + u_w) df_new,
@@ -457,17 +469,34 @@ __global__ void __launch_bounds__(PB) k_plinks(S* __restrict__ f, PartParams p, 
             const L w = a <= 6 ? L(1.0 / 18.0) : L(1.0 / 36.0);
             const L mv = L(6) * w * ravg * (-(L)ea * uw0 - (L)eb * uw1 - (L)ec * uw2);  // moving wall
             const L dpa = fp_dev<S, L>(f, a, i, j, k, p);
+            // interpolation nodes inside a solid have no post-collision value
+            // of this step: fall back to the linear IBB, then to simple
+            // bounce-back (nodes beyond the walls are ghosts and available)
+            const bool av1 = node_avail(i - ea, j - eb, k - ec, p, d.owner_cur);
             L dn;
             if (q < L(0.5)) {
-                const L c0 = q * (L(1) + L(2) * q), c1 = L(1) - L(4) * q * q, c2 = q * (L(1) - L(2) * q);
-                const L d1 = fp_dev<S, L>(f, a, i - ea, j - eb, k - ec, p);
-                const L d2 = fp_dev<S, L>(f, a, i - 2 * ea, j - 2 * eb, k - 2 * ec, p);
-                dn = c0 * dpa + c1 * d1 - c2 * d2 + mv;
-            } else {
+                const bool av2 = node_avail(i - 2 * ea, j - 2 * eb, k - 2 * ec, p, d.owner_cur);
+                if (av1 && av2) {
+                    const L c0 = q * (L(1) + L(2) * q), c1 = L(1) - L(4) * q * q,
+                            c2 = q * (L(1) - L(2) * q);
+                    const L d1 = fp_dev<S, L>(f, a, i - ea, j - eb, k - ec, p);
+                    const L d2 = fp_dev<S, L>(f, a, i - 2 * ea, j - 2 * eb, k - 2 * ec, p);
+                    dn = c0 * dpa + c1 * d1 - c2 * d2 + mv;
+                } else if (av1) {  // case1/mpi_complete/particle_bounceback.F90:66-69
+                    const L d1 = fp_dev<S, L>(f, a, i - ea, j - eb, k - ec, p);
+                    dn = L(2) * q * dpa + (L(1) - L(2) * q) * d1 + mv;
+                } else {
+                    dn = dpa + mv;
+                }
+            } else if (av1) {
                 const L iq = L(1) / q, i2 = L(1) / (L(1) + L(2) * q), a2 = L(2) * q - L(1);
                 const L g0 = fp_dev<S, L>(f, ra, i, j, k, p);
                 const L g1 = fp_dev<S, L>(f, ra, i - ea, j - eb, k - ec, p);
                 dn = (iq * i2) * dpa + (a2 * iq) * g0 - (a2 * i2) * g1 + (iq * i2) * mv;
+            } else {  // case1/mpi_complete/particle_bounceback.F90:70-73
+                const L h = L(0.5) / q;
+                const L g0 = fp_dev<S, L>(f, ra, i, j, k, p);
+                dn = h * dpa + (L(1) - h) * g0 + h * mv;
             }
             const long long fslot = ra * P + (i + (long long)nx * (j + (long long)ny * k));
             if (PSt<S>::SHIFT) {

@@ -538,16 +538,37 @@ static int bounceback_particle(orc_particles* s) {
                         double eu = s->ex[ra] * (U[0] + rot[0]) + s->ey[ra] * (U[1] + rot[1]);
                         if (p->dim == 3) eu = eu + s->ez[ra] * (U[2] + rot[2]);
                         const int ex = s->ex[a], ey = s->ey[a], ez = s->ez[a];
-                        if (q < 0.5) {
+                        /* 3-D generalisation: an interpolation node inside a
+                         * solid (a gap below two lattice units) has no
+                         * post-collision value of this step; the scheme falls
+                         * back to the reference's linear IBB (case1/mpi_complete/
+                         * particle_bounceback.F90:66-76), or to simple
+                         * bounce-back when the linear form lacks its node too.
+                         * Nodes outside the domain are ghosts (omega*rho0) and
+                         * count as available.  The 2-D mode keeps the
+                         * reference's reads of solid f_post. */
+                        const int sol1 = p->dim == 3 && OB_(i - ex, j - ey, k - ez) != 0;
+                        const int sol2 = p->dim == 3 && OB_(i - 2 * ex, j - 2 * ey, k - 2 * ez) != 0;
+                        if (q < 0.5 && !sol1 && !sol2) {
                             F_(ra, i, j, k) = q * (1.0 + 2.0 * q) * FP_(a, i, j, k) +
                                               (1.0 - 4.0 * q * q) * FP_(a, i - ex, j - ey, k - ez) -
                                               q * (1.0 - 2.0 * q) * FP_(a, i - 2 * ex, j - 2 * ey, k - 2 * ez) +
                                               6.0 * s->omega[a] * s->rho_avg * eu;
-                        } else {
+                        } else if (q < 0.5 && !sol1) {
+                            F_(ra, i, j, k) = 2.0 * q * FP_(a, i, j, k) +
+                                              (1.0 - 2.0 * q) * FP_(a, i - ex, j - ey, k - ez) +
+                                              6.0 * s->omega[a] * s->rho_avg * eu;
+                        } else if (q < 0.5) {
+                            F_(ra, i, j, k) = FP_(a, i, j, k) + 6.0 * s->omega[a] * s->rho_avg * eu;
+                        } else if (!sol1) {
                             F_(ra, i, j, k) = FP_(a, i, j, k) / q / (1.0 + 2.0 * q) +
                                               FP_(ra, i, j, k) * (2.0 * q - 1.0) / q -
                                               FP_(ra, i - ex, j - ey, k - ez) * (2.0 * q - 1.0) / (2.0 * q + 1.0) +
                                               6.0 * s->omega[a] * s->rho_avg / q / (1.0 + 2.0 * q) * eu;
+                        } else {
+                            F_(ra, i, j, k) = 0.5 / q * FP_(a, i, j, k) +
+                                              (1.0 - 0.5 / q) * FP_(ra, i, j, k) +
+                                              3.0 * s->omega[a] * s->rho_avg / q * eu;
                         }
                     }
                     if (!found) return 1;

@@ -64,6 +64,43 @@ def test_particles_match_oracle(mg, oracle60, prec, tf, tp):
     assert (st["uc"][:, 0] > 0).all()
 
 
+# Two pairs of spheres whose surfaces are 1.2 and 2.3 lattice units apart: their
+# boundary links have interpolation nodes inside the neighbouring sphere, so
+# the linear and simple bounce-back fall-backs run (springs keep them apart).
+THIN = [[9.0, 11.6, 10.7], [17.2, 12.1, 11.0], [27.3, 11.4, 10.8], [35.5, 12.6, 11.3]]
+
+
+@pytest.mark.parametrize("prec,tf,tp", [("fp64", 1e-10, 1e-9), ("fp32", 1e-4, 1e-4)])
+def test_thin_gaps_match_oracle(mg, prec, tf, tp):
+    d = np.array(THIN)
+    gaps = [np.linalg.norm(d[1] - d[0]) - 2 * CASE["radius"], np.linalg.norm(d[3] - d[2]) - 2 * CASE["radius"]]
+    assert 1.0 < min(gaps) and max(gaps) < 2.5
+    o = O.ParticleOracle(d, dim=3, qmode=1, **CASE)
+    assert o.step(40) == 0
+    r = o.get()
+    with _gpu(mg, prec, centers=THIN) as c:
+        c.initial()
+        c.step(40)
+        st = c.state()
+        mask = c.mask()
+        f = c.get_f()
+    fluid = r["obst"] == 0
+    assert np.array_equal(mask < 0, fluid)
+    assert rel_l2(f[fluid], r["f"][fluid]) <= tf
+    for k_gpu, k_ora in (("uc", "uc"), ("omega", "om"), ("force", "force"), ("torque", "torque")):
+        assert rel_l2(st[k_gpu], r[k_ora]) <= tp * 10, k_gpu
+
+
+def test_steps_are_deterministic(mg):
+    out = []
+    for _ in range(2):
+        with _gpu(mg, "fp32", centers=THIN) as c:
+            c.initial()
+            c.step(25)
+            out.append((c.get_f(), c.state()["torque"]))
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
 def test_macro_marks_solid_nodes(mg):
     with _gpu(mg, "fp64") as c:
         c.initial()
