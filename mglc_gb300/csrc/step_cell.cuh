@@ -103,25 +103,22 @@ __host__ __device__ constexpr unsigned leave_bits(int dx, int dy, int dz) {
 
 // ------------------------------------------------------------ lid kernel --
 // IDX: 32-bit element indices when Q*cells < 2^31, 64-bit otherwise.
+// lid_cell_from: collide and push one cell whose 19 stored populations are
+// already in registers (raw); lid_cell: load them, then the same.
 template <typename S, bool FIRST, typename IDX>
-__device__ __forceinline__ void lid_cell(int i, int j, int k, const S* __restrict__ fin,
-                                         S* __restrict__ fout, const StepK<typename St<S>::C>& K,
-                                         IDX P, const double* __restrict__ mrho,
-                                         const double* __restrict__ mu,
-                                         const double* __restrict__ mv,
-                                         const double* __restrict__ mw) {
+__device__ __forceinline__ void lid_cell_from(int i, int j, int k, const S (&raw)[Q19],
+                                              S* __restrict__ fout,
+                                              const StepK<typename St<S>::C>& K, IDX P,
+                                              const double* __restrict__ mrho,
+                                              const double* __restrict__ mu,
+                                              const double* __restrict__ mv,
+                                              const double* __restrict__ mw) {
     using C = typename St<S>::C;
     const int nx = K.nx, ny = K.ny, nz = K.nz;
     const IDX cell = (IDX)i + (IDX)nx * ((IDX)j + (IDX)ny * (IDX)k);
     C f[Q19];
-    {
-        // every load is issued before the first conversion
-        S raw[Q19];
 #pragma unroll
-        for (int q = 0; q < Q19; q++) raw[q] = St<S>::raw(fin + ((IDX)q * P + cell));
-#pragma unroll
-        for (int q = 0; q < Q19; q++) f[q] = St<S>::cvt(raw[q], K.inv_scale);
-    }
+    for (int q = 0; q < Q19; q++) f[q] = St<S>::cvt(raw[q], K.inv_scale);
     C rho_m, rho, ux, uy, uz;
     if (FIRST) {
         rho = (C)mrho[cell];
@@ -166,6 +163,26 @@ __device__ __forceinline__ void lid_cell(int i, int j, int k, const S* __restric
             St<S>::st(fout + ((IDX)opp19(q) * P + cell), val, K.scale);
         }
     }
+}
+
+template <typename S, typename IDX>
+__device__ __forceinline__ void lid_load(int i, int j, int k, const S* __restrict__ fin, int nx,
+                                         int ny, IDX P, S (&raw)[Q19]) {
+    const IDX cell = (IDX)i + (IDX)nx * ((IDX)j + (IDX)ny * (IDX)k);
+#pragma unroll
+    for (int q = 0; q < Q19; q++) raw[q] = St<S>::raw(fin + ((IDX)q * P + cell));
+}
+
+template <typename S, bool FIRST, typename IDX>
+__device__ __forceinline__ void lid_cell(int i, int j, int k, const S* __restrict__ fin,
+                                         S* __restrict__ fout, const StepK<typename St<S>::C>& K,
+                                         IDX P, const double* __restrict__ mrho,
+                                         const double* __restrict__ mu,
+                                         const double* __restrict__ mv,
+                                         const double* __restrict__ mw) {
+    S raw[Q19];  // every load is issued before the first conversion
+    lid_load<S, IDX>(i, j, k, fin, K.nx, K.ny, P, raw);
+    lid_cell_from<S, FIRST, IDX>(i, j, k, raw, fout, K, P, mrho, mu, mv, mw);
 }
 
 // ------------------------------------------------------ lid kernel, FX64 --
