@@ -168,6 +168,60 @@ int mglc_get_mask(mglc_ctx* ctx, int* owner);
  * Any pointer may be NULL.  Synchronises. */
 int mglc_nusselt(mglc_ctx* ctx, double* nu_vol, double* re_vol, double* nu_hot, double* nu_cold);
 
+/* ---- output, checkpoint/restart, statistics (host side) ------------------ */
+/* Tecplot binary (.plt, "#!TDV101", one zone, point packing, 32-bit floats)
+ * of the current fields: lid X Y Z U V W Pressure (= rho/3)
+ * (mpi_3d_blocked/output.f90:175-296); heated X Y Z U V W T
+ * (Buoyancy_driven_cavity/fortran/3d/seq/bouyancy3d.F90:1034-1164).  Node
+ * coordinates x_i = i - 0.5.  Synchronises. */
+int mglc_write_tecplot(mglc_ctx* ctx, const char* path);
+/* The same writer on host arrays (x fastest); s = rho (thermal = 0) or T. */
+int mglc_tecplot_write_fields(const char* path, int nx, int ny, int nz, const double* u,
+                              const double* v, const double* w, const double* s, int thermal);
+/* Centre-line profiles of getVelocity (output.f90:318-347): u(nx/2,ny/2,z)/U0
+ * against z/nz, and x/nx against w(x,ny/2,nz/2)/U0, one pair per line. */
+int mglc_write_profiles(mglc_ctx* ctx, const char* uz_path, const char* xw_path, double u0);
+int mglc_profiles_write_fields(const char* uz_path, const char* xw_path, int nx, int ny, int nz,
+                               const double* u, const double* w, double u0);
+/* output_binary: Fortran unformatted sequential records, lid u, v, rho
+ * (output.f90:350-367), heated u, v, w, T (bouyancy3d.F90:984-1008). */
+int mglc_write_binary(mglc_ctx* ctx, const char* path);
+/* backupData (bouyancy3d.F90:1011-1030): records u, v, w, T, f(0:18,...),
+ * g(0:6,...) (lid contexts: u, v, w, f).  Records follow gfortran's layout:
+ * 4-byte markers, subrecords of at most 2^31-9 bytes. */
+int mglc_backup_save(mglc_ctx* ctx, const char* path);
+/* Reload (bouyancy3d.F90:367-379): f, g and u, v, w, T from the file with
+ * rho = 1 (:289); the next step collides with those fields, as the reference
+ * does after a reload. */
+int mglc_backup_load(mglc_ctx* ctx, const char* path);
+/* The record writer/reader on host arrays; T and g may be NULL (omitted).
+ * max_subrecord: subrecord payload limit in bytes, 0 = 2^31-9 (gfortran). */
+int mglc_backup_write_fields(const char* path, int nx, int ny, int nz, const double* u,
+                             const double* v, const double* w, const double* T, const double* f,
+                             const double* g, long long max_subrecord);
+int mglc_backup_read_fields(const char* path, int nx, int ny, int nz, double* u, double* v,
+                            double* w, double* T, double* f, double* g);
+
+/* calNuRe statistics (bouyancy3d.F90:1185-1321), one sample per time unit:
+ * running means of Nu and Re, statistical stationarity (means change < 1%
+ * over 100 samples, tested every 100) and convergence (first- and last-half
+ * means of the stationary window within 1%, tested every 200 samples; with
+ * flow reversal, not before flow_reversal_time samples after stationarity). */
+typedef struct mglc_nure_monitor mglc_nure_monitor;
+typedef struct mglc_nure_status {
+    int time;                       /* samples so far (dimensionlessTime) */
+    double nu, re, nu_mean, re_mean;
+    int stationary, stationary_time, converged;
+    double nu_half_change, re_half_change; /* relative change tested now, else -1 */
+    double nu_mean_change, re_mean_change; /* relative change tested now, else -1 */
+} mglc_nure_status;
+int mglc_nure_create(int flow_reversal, int flow_reversal_time, mglc_nure_monitor** out);
+void mglc_nure_destroy(mglc_nure_monitor* m);
+/* add one sample (Nu, Re); out may be NULL */
+int mglc_nure_push(mglc_nure_monitor* m, double nu, double re, mglc_nure_status* out);
+/* sample a heated context (mglc_nusselt's Nu and Re on the device) and push */
+int mglc_nure_sample(mglc_nure_monitor* m, mglc_ctx* ctx, mglc_nure_status* out);
+
 /* ---- device-resident variants (no host copies) --------------------------- */
 /* Same as mglc_get_macros but into device buffers of nx*ny*nz doubles. */
 int mglc_get_macros_device(mglc_ctx* ctx, double* rho, double* u, double* v, double* w,

@@ -5,7 +5,8 @@ kernels for sm_103a under csrc/).  This package builds it and offers a thin
 Python host API that mirrors the reference's routines.
 """
 from .capi import FORMS, MglcError, lib  # noqa: F401
-from .cavity import BuoyancyCavity, LidDrivenCavity, ParticleFlow  # noqa: F401
+from .cavity import BuoyancyCavity, LidDrivenCavity, NuReMonitor, ParticleFlow  # noqa: F401
 from .serve import SolveServer  # noqa: F401
 
-__all__ = ["LidDrivenCavity", "BuoyancyCavity", "ParticleFlow", "SolveServer", "MglcError", "FORMS", "lib"]
+__all__ = ["LidDrivenCavity", "BuoyancyCavity", "ParticleFlow", "NuReMonitor", "SolveServer", "MglcError",
+           "FORMS", "lib"]

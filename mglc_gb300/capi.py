@@ -70,6 +70,13 @@ class ServerStats(ctypes.Structure):
                 ("peak_device_bytes", _LL), ("peak_active", _I)]
 
 
+class NuReStatus(ctypes.Structure):
+    _fields_ = [("time", _I), ("nu", _D), ("re", _D), ("nu_mean", _D), ("re_mean", _D),
+                ("stationary", _I), ("stationary_time", _I), ("converged", _I),
+                ("nu_half_change", _D), ("re_half_change", _D), ("nu_mean_change", _D),
+                ("re_mean_change", _D)]
+
+
 # (name, argtypes, restype) of every exported symbol; tests check that the
 # library exports all of them
 SIGNATURES = {
@@ -101,6 +108,19 @@ SIGNATURES = {
     "mglc_server_get_stats": ([_VP, ctypes.POINTER(ServerStats)], _I),
     "mglc_residual_noalloc": ([_LL, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _I, _VP, _DP, _DP,
                                ctypes.c_char_p, _I], _I),
+    "mglc_write_tecplot": ([_VP, ctypes.c_char_p], _I),
+    "mglc_tecplot_write_fields": ([ctypes.c_char_p, _I, _I, _I, _VP, _VP, _VP, _VP, _I], _I),
+    "mglc_write_profiles": ([_VP, ctypes.c_char_p, ctypes.c_char_p, _D], _I),
+    "mglc_profiles_write_fields": ([ctypes.c_char_p, ctypes.c_char_p, _I, _I, _I, _VP, _VP, _D], _I),
+    "mglc_write_binary": ([_VP, ctypes.c_char_p], _I),
+    "mglc_backup_save": ([_VP, ctypes.c_char_p], _I),
+    "mglc_backup_load": ([_VP, ctypes.c_char_p], _I),
+    "mglc_backup_write_fields": ([ctypes.c_char_p, _I, _I, _I, _VP, _VP, _VP, _VP, _VP, _VP, _LL], _I),
+    "mglc_backup_read_fields": ([ctypes.c_char_p, _I, _I, _I, _VP, _VP, _VP, _VP, _VP, _VP], _I),
+    "mglc_nure_create": ([_I, _I, ctypes.POINTER(_VP)], _I),
+    "mglc_nure_destroy": ([_VP], None),
+    "mglc_nure_push": ([_VP, _D, _D, ctypes.POINTER(NuReStatus)], _I),
+    "mglc_nure_sample": ([_VP, _VP, ctypes.POINTER(NuReStatus)], _I),
 }
 
 _lib = None

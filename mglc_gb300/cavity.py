@@ -20,6 +20,7 @@ for populations, i.e. the Fortran arrays with the index order reversed.
 from __future__ import annotations
 
 import ctypes
+import os
 
 import numpy as np
 
@@ -100,6 +101,61 @@ class _Solve:
         self._ck(capi.lib().mglc_totals(self._ctx, ctypes.byref(m), ctypes.byref(e), ctypes.byref(h)))
         return m.value, e.value, h.value
 
+    # -- output and checkpoint/restart (the reference's output routines) --
+    def _io(self, rc, what, path):
+        if rc != capi.MGLC_OK:
+            raise capi.MglcError(rc, f"{what} {os.fspath(path)!r} failed")
+
+    def write_tecplot(self, path):
+        """output_Tecplot: binary .plt of X Y Z U V W and Pressure (lid) or T."""
+        self._io(capi.lib().mglc_write_tecplot(self._ctx, os.fsencode(path)), "Tecplot output", path)
+
+    def write_binary(self, path):
+        """output_binary: Fortran unformatted records (lid u, v, rho; heated u, v, w, T)."""
+        self._io(capi.lib().mglc_write_binary(self._ctx, os.fsencode(path)), "binary output", path)
+
+    def save_backup(self, path):
+        """backupData: Fortran unformatted records u, v, w, (T,) f, (g)."""
+        self._io(capi.lib().mglc_backup_save(self._ctx, os.fsencode(path)), "backup", path)
+
+    def load_backup(self, path):
+        """The reference's reload: f, g, u, v, w, T from the file, rho = 1."""
+        self._io(capi.lib().mglc_backup_load(self._ctx, os.fsencode(path)), "reload", path)
+        return self
+
+
+class NuReMonitor:
+    """calNuRe (Buoyancy_driven_cavity/fortran/3d/seq/bouyancy3d.F90:1185-1321):
+    feed one (Nu, Re) sample per time unit -- ``sample(cavity)`` takes them
+    from a BuoyancyCavity on the device -- and read the running means and the
+    stationary / converged flags from the returned status."""
+
+    def __init__(self, flow_reversal=False, flow_reversal_time=0):
+        self._m = _P()
+        capi.check(None, capi.lib().mglc_nure_create(int(bool(flow_reversal)),
+                                                     int(flow_reversal_time), ctypes.byref(self._m)))
+
+    def push(self, nu, re) -> capi.NuReStatus:
+        st = capi.NuReStatus()
+        capi.check(None, capi.lib().mglc_nure_push(self._m, float(nu), float(re), ctypes.byref(st)))
+        return st
+
+    def sample(self, cavity) -> capi.NuReStatus:
+        st = capi.NuReStatus()
+        capi.check(cavity.handle, capi.lib().mglc_nure_sample(self._m, cavity.handle, ctypes.byref(st)))
+        return st
+
+    def close(self):
+        if self._m:
+            capi.lib().mglc_nure_destroy(self._m)
+            self._m = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
 
 class LidDrivenCavity(_Solve):
     """D3Q19 MRT lid-driven cavity (reference: Lid_driven_cavity/fortran/3d)."""
@@ -107,6 +163,7 @@ class LidDrivenCavity(_Solve):
     def __init__(self, total_nx, total_ny=None, total_nz=None, reynolds=1000.0, u0=0.1,
                  rho0=1.0, top_layer_u0=True, precision="fp64"):
         super().__init__()
+        self.u0 = float(u0)
         p = capi.LidParams(total_nx, total_ny or total_nx, total_nz or total_nx, float(reynolds),
                            float(rho0), float(u0), int(bool(top_layer_u0)), capi.FORMS[precision])
         ctx = _P()
@@ -116,6 +173,11 @@ class LidDrivenCavity(_Solve):
             msg = capi.lib().mglc_last_error(ctx).decode() if ctx else ""
             self.close()
             raise capi.MglcError(rc, msg)
+
+    def write_profiles(self, uz_path, xw_path):
+        """getVelocity: centre-line u(z)/U0 and w(x)/U0 profiles."""
+        self._io(capi.lib().mglc_write_profiles(self._ctx, os.fsencode(uz_path), os.fsencode(xw_path),
+                                                self.u0), "profiles", uz_path)
 
     def macro(self):
         nz, ny, nx = self.shape
