@@ -28,6 +28,13 @@ module mglc_iface
         integer(c_int) :: bc_y_const_t, bc_z_const_t, precision
     end type
 
+    type, bind(C) :: mglc_nure_status
+        integer(c_int) :: time
+        real(c_double) :: nu, re, nu_mean, re_mean
+        integer(c_int) :: stationary, stationary_time, converged
+        real(c_double) :: nu_half_change, re_half_change, nu_mean_change, re_mean_change
+    end type
+
     interface
         integer(c_int) function mglc_lid_create(p, ctx) bind(C, name="mglc_lid_create")
             import :: c_int, c_ptr, mglc_lid_params
@@ -84,6 +91,50 @@ module mglc_iface
             import :: c_int, c_ptr, c_double
             type(c_ptr), value :: ctx
             real(c_double), intent(out) :: nu_vol, re_vol, nu_hot, nu_cold
+        end function
+        !! output_Tecplot / getVelocity / output_binary / backupData / reload
+        integer(c_int) function mglc_write_tecplot(ctx, path) bind(C, name="mglc_write_tecplot")
+            import :: c_int, c_ptr, c_char
+            type(c_ptr), value :: ctx
+            character(kind=c_char), intent(in) :: path(*)
+        end function
+        integer(c_int) function mglc_write_profiles(ctx, uz_path, xw_path, u0) &
+                bind(C, name="mglc_write_profiles")
+            import :: c_int, c_ptr, c_char, c_double
+            type(c_ptr), value :: ctx
+            character(kind=c_char), intent(in) :: uz_path(*), xw_path(*)
+            real(c_double), value :: u0
+        end function
+        integer(c_int) function mglc_write_binary(ctx, path) bind(C, name="mglc_write_binary")
+            import :: c_int, c_ptr, c_char
+            type(c_ptr), value :: ctx
+            character(kind=c_char), intent(in) :: path(*)
+        end function
+        integer(c_int) function mglc_backup_save(ctx, path) bind(C, name="mglc_backup_save")
+            import :: c_int, c_ptr, c_char
+            type(c_ptr), value :: ctx
+            character(kind=c_char), intent(in) :: path(*)
+        end function
+        integer(c_int) function mglc_backup_load(ctx, path) bind(C, name="mglc_backup_load")
+            import :: c_int, c_ptr, c_char
+            type(c_ptr), value :: ctx
+            character(kind=c_char), intent(in) :: path(*)
+        end function
+        !! calNuRe bookkeeping
+        integer(c_int) function mglc_nure_create(flow_reversal, flow_reversal_time, m) &
+                bind(C, name="mglc_nure_create")
+            import :: c_int, c_ptr
+            integer(c_int), value :: flow_reversal, flow_reversal_time
+            type(c_ptr), intent(out) :: m
+        end function
+        subroutine mglc_nure_destroy(m) bind(C, name="mglc_nure_destroy")
+            import :: c_ptr
+            type(c_ptr), value :: m
+        end subroutine
+        integer(c_int) function mglc_nure_sample(m, ctx, status) bind(C, name="mglc_nure_sample")
+            import :: c_int, c_ptr, mglc_nure_status
+            type(c_ptr), value :: m, ctx
+            type(mglc_nure_status), intent(out) :: status
         end function
     end interface
 
