@@ -28,6 +28,13 @@ module mglc_iface
         integer(c_int) :: bc_y_const_t, bc_z_const_t, precision
     end type
 
+    type, bind(C) :: mglc_particle2d_params
+        integer(c_int) :: total_nx, total_ny
+        real(c_double) :: tauf, rho0, rho_solid, radius, gravity
+        real(c_double) :: threshold_wall, stiff_wall, threshold_particle, stiff_particle
+        integer(c_int) :: q_bisection
+    end type
+
     type, bind(C) :: mglc_nure_status
         integer(c_int) :: time
         real(c_double) :: nu, re, nu_mean, re_mean
@@ -91,6 +98,21 @@ module mglc_iface
             import :: c_int, c_ptr, c_double
             type(c_ptr), value :: ctx
             real(c_double), intent(out) :: nu_vol, re_vol, nu_hot, nu_cold
+        end function
+        !! case4 (D2Q9) particles: centers(2, np)
+        integer(c_int) function mglc_particle2d_create(p, centers, np, ctx) &
+                bind(C, name="mglc_particle2d_create")
+            import :: c_int, c_ptr, c_double, mglc_particle2d_params
+            type(mglc_particle2d_params), intent(in) :: p
+            real(c_double), intent(in) :: centers(*)
+            integer(c_int), value :: np
+            type(c_ptr), intent(out) :: ctx
+        end function
+        integer(c_int) function mglc_particle_state(ctx, xc, uc, omega, force, torque) &
+                bind(C, name="mglc_particle_state")
+            import :: c_int, c_ptr, c_double
+            type(c_ptr), value :: ctx
+            real(c_double), intent(out) :: xc(*), uc(*), omega(*), force(*), torque(*)
         end function
         !! output_Tecplot / getVelocity / output_binary / backupData / reload
         integer(c_int) function mglc_write_tecplot(ctx, path) bind(C, name="mglc_write_tecplot")

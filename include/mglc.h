@@ -46,7 +46,7 @@ extern "C" {
  *  to FP64 per stored population), everything else as FP64. */
 enum { MGLC_FP64 = 0, MGLC_FP32 = 1, MGLC_FP16 = 2, MGLC_BF16 = 3, MGLC_FX64 = 4 };
 
-enum { MGLC_KIND_LID = 1, MGLC_KIND_THERMAL = 2, MGLC_KIND_PARTICLE = 3 };
+enum { MGLC_KIND_LID = 1, MGLC_KIND_THERMAL = 2, MGLC_KIND_PARTICLE = 3, MGLC_KIND_PARTICLE2D = 4 };
 
 typedef struct mglc_ctx mglc_ctx;
 
@@ -112,6 +112,24 @@ int mglc_thermal_create(const mglc_thermal_params* p, mglc_ctx** out);
  * centers = np x (x,y,z) in node coordinates (node i sits at x = i, 1-based). */
 int mglc_particle_create(const mglc_particle_params* p, const double* centers, int np,
                          mglc_ctx** out);
+/* D2Q9 moving circles: the reference's own 2-D case4 step
+ * (MPI/Micro_particles/fortran/case4/mpi_particle, main.F90:35-73) with the
+ * parameters of its commondata.F90: closed box (four halfway-bounce-back
+ * walls), gravity along -y, springs with stiffness and threshold against
+ * particles and the left, right and bottom walls.  FP64, every statement in
+ * the reference's order (bitwise the reference's results).  centers = np x
+ * (x, y), node i at x = i (1-based).  Verbs: mglc_initial, mglc_step,
+ * mglc_get_f (9 per node), mglc_get_macros (w = 0), mglc_particle_state,
+ * mglc_get_mask. */
+typedef struct mglc_particle2d_params {
+    int total_nx, total_ny;
+    double tauf, rho0, rho_solid, radius;
+    double gravity;                          /* magnitude, acting along -y */
+    double threshold_wall, stiff_wall, threshold_particle, stiff_particle;
+    int q_bisection;                         /* 1: calQ bisection (reference), 0: calQ2 */
+} mglc_particle2d_params;
+int mglc_particle2d_create(const mglc_particle2d_params* p, const double* centers, int np,
+                           mglc_ctx** out);
 void mglc_destroy(mglc_ctx* ctx);
 const char* mglc_last_error(const mglc_ctx* ctx);
 /* Bind the context to a caller-owned cudaStream_t (NULL = the context's own stream). */

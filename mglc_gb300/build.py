@@ -41,11 +41,16 @@ def _stale(obj, src):
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 
+# per-file flags: the 2-D particle step reproduces the reference's FP64
+# statements, so no multiply-add contraction there
+FILE_FLAGS = {"k_particle2d.cu": ["-fmad=false"]}
+
+
 def _compile(src, verbose_ptxas=False):
     obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
     if not _stale(obj, src):
         return obj, ""
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", src, "-o", obj]
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *FILE_FLAGS.get(os.path.basename(src), []), "-c", src, "-o", obj]
     if verbose_ptxas:
         cmd[1:1] = ["-Xptxas", "-v"]
     r = subprocess.run(cmd, capture_output=True, text=True)

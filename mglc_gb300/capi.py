@@ -70,6 +70,12 @@ class ServerStats(ctypes.Structure):
                 ("peak_device_bytes", _LL), ("peak_active", _I)]
 
 
+class Particle2DParams(ctypes.Structure):
+    _fields_ = [("total_nx", _I), ("total_ny", _I), ("tauf", _D), ("rho0", _D), ("rho_solid", _D),
+                ("radius", _D), ("gravity", _D), ("threshold_wall", _D), ("stiff_wall", _D),
+                ("threshold_particle", _D), ("stiff_particle", _D), ("q_bisection", _I)]
+
+
 class NuReStatus(ctypes.Structure):
     _fields_ = [("time", _I), ("nu", _D), ("re", _D), ("nu_mean", _D), ("re_mean", _D),
                 ("stationary", _I), ("stationary_time", _I), ("converged", _I),
@@ -84,6 +90,7 @@ SIGNATURES = {
     "mglc_thermal_create": ([ctypes.POINTER(ThermalParams), ctypes.POINTER(_VP)], _I),
     "mglc_particle_create": ([ctypes.POINTER(ParticleParams), _VP, _I, ctypes.POINTER(_VP)], _I),
     "mglc_particle_state": ([_VP, _VP, _VP, _VP, _VP, _VP], _I),
+    "mglc_particle2d_create": ([ctypes.POINTER(Particle2DParams), _VP, _I, ctypes.POINTER(_VP)], _I),
     "mglc_get_mask": ([_VP, _VP], _I),
     "mglc_destroy": ([_VP], None),
     "mglc_last_error": ([_VP], ctypes.c_char_p),

@@ -285,3 +285,56 @@ class ParticleFlow(_Solve):
         m = np.empty((nz, ny, nx), dtype=np.int32)
         self._ck(capi.lib().mglc_get_mask(self._ctx, m.ctypes.data))
         return m
+
+
+class ParticleFlow2D(_Solve):
+    """D2Q9 moving circles, the reference's own 2-D case4 step
+    (Micro_particles/fortran/case4/mpi_particle) with its commondata
+    parameters; bitwise the reference's statements.  Arrays are (ny, nx)."""
+
+    def __init__(self, total_nx, total_ny, centers, radius, tauf=0.65, rho0=1.0, rho_solid=1.01,
+                 gravity=0.0, threshold_wall=6.0, stiff_wall=0.02, threshold_particle=6.0,
+                 stiff_particle=0.08, q_bisection=True):
+        super().__init__()
+        c = np.ascontiguousarray(np.asarray(centers, dtype=np.float64).reshape(-1, 2))
+        self.np = len(c)
+        p = capi.Particle2DParams(total_nx, total_ny, float(tauf), float(rho0), float(rho_solid),
+                                  float(radius), float(gravity), float(threshold_wall),
+                                  float(stiff_wall), float(threshold_particle), float(stiff_particle),
+                                  int(bool(q_bisection)))
+        ctx = _P()
+        rc = capi.lib().mglc_particle2d_create(ctypes.byref(p), c.ctypes.data, len(c), ctypes.byref(ctx))
+        self._ctx = ctx
+        if rc != capi.MGLC_OK:
+            msg = capi.lib().mglc_last_error(ctx).decode() if ctx else ""
+            self.close()
+            raise capi.MglcError(rc, msg)
+
+    @property
+    def shape2(self):
+        i = self.info()
+        return (i.ny, i.nx)
+
+    def get_f(self):
+        ny, nx = self.shape2
+        f = np.empty((ny, nx, 9))
+        self._ck(capi.lib().mglc_get_f(self._ctx, _ptr(f), None))
+        return f
+
+    def macro(self):
+        ny, nx = self.shape2
+        rho, u, v = (np.empty((ny, nx)) for _ in range(3))
+        self._ck(capi.lib().mglc_get_macros(self._ctx, _ptr(rho), _ptr(u), _ptr(v), None, None))
+        return rho, u, v
+
+    def state(self):
+        out = {k: np.zeros((self.np, 3)) for k in ("xc", "uc", "omega", "force", "torque")}
+        self._ck(capi.lib().mglc_particle_state(self._ctx, *[_ptr(out[k]) for k in
+                                                             ("xc", "uc", "omega", "force", "torque")]))
+        return out
+
+    def mask(self):
+        ny, nx = self.shape2
+        m = np.empty((ny, nx), dtype=np.int32)
+        self._ck(capi.lib().mglc_get_mask(self._ctx, m.ctypes.data))
+        return m

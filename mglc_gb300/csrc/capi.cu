@@ -17,12 +17,14 @@
 #include "../../include/mglc.h"
 #include "kernels.cuh"
 #include "particles.cuh"
+#include "particles2d.cuh"
 
 using namespace mglc;
 
 struct mglc_ctx {
     int kind = 0, form = FORM_FP64;
     bool fx64 = false;  // MGLC_FX64: FP64 storage (form FP64), Q55 fixed-point lid collision
+    P2Ctx* p2d = nullptr;  // MGLC_KIND_PARTICLE2D: the D2Q9 case4 state
     Geom geom{};
     long long n = 0;
     cudaStream_t stream = nullptr;
@@ -330,6 +332,8 @@ int mglc_thermal_create(const mglc_thermal_params* p, mglc_ctx** out) {
 
 void mglc_destroy(mglc_ctx* c) {
     if (!c) return;
+    if (c->p2d) p2d_destroy(c->p2d);
+    c->p2d = nullptr;
     if (c->stream) cudaStreamSynchronize(c->stream);
     release(c);
     delete c;
@@ -339,6 +343,7 @@ const char* mglc_last_error(const mglc_ctx* c) { return c ? c->err.c_str() : "nu
 
 int mglc_set_stream(mglc_ctx* c, void* s) {
     if (!c) return MGLC_ERR_INVALID;
+    if (c->p2d) return p2d_set_stream(c->p2d, (cudaStream_t)s);
     CK(cudaStreamSynchronize(c->stream), "synchronize");
     if (c->own_stream) cudaStreamDestroy(c->stream);
     if (s) {
@@ -367,6 +372,12 @@ int mglc_get_info(const mglc_ctx* c, mglc_info* o) {
     o->gbeta = c->gbeta;
     o->omega_rot = c->omega_rot;
     const double pb = (double)form_bytes(c->form);
+    if (c->p2d) {
+        o->itc = p2d_itc(c->p2d);
+        o->bytes_per_cell_step = 2.0 * 9 * 8.0 + 4.0;  // f pulled from fp, the mask read
+        o->device_bytes = p2d_device_bytes(c->p2d);
+        return MGLC_OK;
+    }
     if (c->kind == MGLC_KIND_LID) {
         o->bytes_per_cell_step = 2.0 * Q19 * pb;
     } else if (c->kind == MGLC_KIND_PARTICLE) {
@@ -387,6 +398,11 @@ int particle_initial(mglc_ctx* c);
 int mglc_initial(mglc_ctx* c) {
     if (!c || !c->kind) return MGLC_ERR_INVALID;
     if (c->kind == MGLC_KIND_PARTICLE) return particle_initial(c);
+    if (c->p2d) {
+        int rc = p2d_initial(c->p2d, c->err);
+        c->initialised = rc == MGLC_OK;
+        return rc;
+    }
     const long long n = c->n;
     const Geom& g = c->geom;
     // rho = rho0, u = v = w = 0 (and T); lid top layer u = U0; hot/cold walls
@@ -438,6 +454,7 @@ int mglc_initial(mglc_ctx* c) {
 int mglc_load_state(mglc_ctx* c, const double* f, const double* g, const double* rho,
                     const double* u, const double* v, const double* w, const double* T) {
     if (!c || !c->kind || !f) return c ? fail(c, MGLC_ERR_INVALID, "f is required") : MGLC_ERR_INVALID;
+    if (c->p2d) return fail(c, MGLC_ERR_UNSUPPORTED, "2-D particle contexts start from mglc_initial");
     if (thermal(c) && !g) return fail(c, MGLC_ERR_INVALID, "thermal contexts need g");
     const bool shifted = c->form != FORM_FP64;
     int rc;
@@ -485,6 +502,7 @@ int mglc_load_state(mglc_ctx* c, const double* f, const double* g, const double*
 int mglc_get_f(mglc_ctx* c, double* f, double* g) {
     if (!c || !c->kind) return MGLC_ERR_INVALID;
     if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial or mglc_load_state first");
+    if (c->p2d) return f ? p2d_get_f(c->p2d, f, c->err) : MGLC_OK;
     const bool shifted = c->form != FORM_FP64;
     int rc;
     if (f && (rc = download_pops(c, Q19, c->f[c->cur], f, shifted))) return rc;
@@ -496,6 +514,7 @@ int mglc_step(mglc_ctx* c, int nsteps) {
     if (!c || !c->kind) return MGLC_ERR_INVALID;
     if (nsteps < 0) return fail(c, MGLC_ERR_INVALID, "nsteps must be >= 0");
     if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial or mglc_load_state first");
+    if (c->p2d) return p2d_step(c->p2d, nsteps, c->err);
     if (c->kind == MGLC_KIND_PARTICLE) {
         for (int s = 0; s < nsteps; s++) {
             const int nxt = c->cur ^ 1;
@@ -563,6 +582,7 @@ int mglc_step(mglc_ctx* c, int nsteps) {
 
 int mglc_get_macros_device(mglc_ctx* c, double* rho, double* u, double* v, double* w, double* T) {
     if (!c || !c->kind) return MGLC_ERR_INVALID;
+    if (c->p2d) return fail(c, MGLC_ERR_UNSUPPORTED, "not available for 2-D particle contexts");
     if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial or mglc_load_state first");
     int rc = refresh_macros(c);
     if (rc) return rc;
@@ -579,6 +599,7 @@ int mglc_get_macros_device(mglc_ctx* c, double* rho, double* u, double* v, doubl
 int mglc_get_macros(mglc_ctx* c, double* rho, double* u, double* v, double* w, double* T) {
     if (!c || !c->kind) return MGLC_ERR_INVALID;
     if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial or mglc_load_state first");
+    if (c->p2d) return p2d_get_macros(c->p2d, rho, u, v, w, c->err);
     int rc = refresh_macros(c);
     if (rc) return rc;
     const size_t b = c->n * sizeof(double);
@@ -593,6 +614,7 @@ int mglc_get_macros(mglc_ctx* c, double* rho, double* u, double* v, double* w, d
 
 int mglc_check(mglc_ctx* c, double* error_u, double* error_t) {
     if (!c || !c->kind) return MGLC_ERR_INVALID;
+    if (c->p2d) return fail(c, MGLC_ERR_UNSUPPORTED, "not available for 2-D particle contexts");
     if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial or mglc_load_state first");
     int rc = refresh_macros(c);
     if (rc) return rc;
@@ -767,8 +789,49 @@ int particle_initial(mglc_ctx* c) {
     return MGLC_OK;
 }
 
+int mglc_particle2d_create(const mglc_particle2d_params* p, const double* centers, int np,
+                           mglc_ctx** out) {
+    if (!p || !out || (np > 0 && !centers)) return MGLC_ERR_INVALID;
+    *out = nullptr;
+    mglc_ctx* c = new mglc_ctx();
+    *out = c;
+    if (p->total_nx < 8 || p->total_ny < 8) return fail(c, MGLC_ERR_INVALID, "the 2-D lattice needs nx, ny >= 8");
+    if (np < 0 || np > 65536) return fail(c, MGLC_ERR_INVALID, "np must be in [0, 65536]");
+    if (!(p->tauf > 0.5)) return fail(c, MGLC_ERR_INVALID, "tauf must exceed 0.5");
+    if (!(p->radius > 0.5)) return fail(c, MGLC_ERR_INVALID, "radius must exceed 0.5");
+    if (!(p->stiff_wall > 0.0 && p->stiff_particle > 0.0 && p->threshold_wall > 0.0 &&
+          p->threshold_particle > 0.0))
+        return fail(c, MGLC_ERR_INVALID, "spring stiffnesses and thresholds must be positive");
+    for (int q = 0; q < np; q++) {
+        const double x = centers[2 * q], y = centers[2 * q + 1];
+        if (!(x - p->radius > 1.0 && y - p->radius > 1.0 && x + p->radius < p->total_nx &&
+              y + p->radius < p->total_ny))
+            return fail(c, MGLC_ERR_INVALID, "circle %d does not fit inside the walls", q);
+    }
+    P2Params pp{};
+    pp.nx = p->total_nx; pp.ny = p->total_ny; pp.np = np;
+    pp.q_bisection = p->q_bisection ? 1 : 0;
+    pp.tauf = p->tauf; pp.rho0 = p->rho0; pp.rho_solid = p->rho_solid; pp.radius = p->radius;
+    pp.gravity = p->gravity;
+    pp.threshold_wall = p->threshold_wall; pp.stiff_wall = p->stiff_wall;
+    pp.threshold_particle = p->threshold_particle; pp.stiff_particle = p->stiff_particle;
+    // commondata.F90:33-34
+    pp.snu = 1.0 / p->tauf;
+    pp.sq = 8.0 * (2.0 * p->tauf - 1.0) / (8.0 * p->tauf - 1.0);
+    pp.pi = 4.0 * std::atan(1.0);
+    c->kind = MGLC_KIND_PARTICLE2D;
+    c->form = FORM_FP64;
+    c->geom = {p->total_nx, p->total_ny, 1, (long long)p->total_nx * p->total_ny};
+    c->n = c->geom.plane;
+    c->tauf = pp.tauf;
+    c->snu = pp.snu;
+    c->sq = pp.sq;
+    return p2d_create(pp, centers, &c->p2d, c->err);
+}
+
 int mglc_particle_state(mglc_ctx* c, double* xc, double* uc, double* omega, double* force,
                         double* torque) {
+    if (c && c->p2d) return p2d_state(c->p2d, xc, uc, omega, force, torque, c->err);
     if (!c || c->kind != MGLC_KIND_PARTICLE)
         return c ? fail(c, MGLC_ERR_STATE, "mglc_particle_state needs a particle context") : MGLC_ERR_INVALID;
     const size_t b = sizeof(double) * 3 * (size_t)c->pp.np;
@@ -783,6 +846,10 @@ int mglc_particle_state(mglc_ctx* c, double* xc, double* uc, double* omega, doub
 }
 
 int mglc_get_mask(mglc_ctx* c, int* owner) {
+    if (c && c->p2d && owner) {
+        if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial first");
+        return p2d_mask(c->p2d, owner, c->err);
+    }
     if (!c || c->kind != MGLC_KIND_PARTICLE || !owner)
         return c ? fail(c, MGLC_ERR_STATE, "mglc_get_mask needs a particle context and a buffer") : MGLC_ERR_INVALID;
     if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial first");

@@ -1,0 +1,693 @@
+// k_particle2d.cu -- D2Q9 moving circles, the reference's case4 step
+// (MPI/Micro_particles/fortran/case4/mpi_particle, main.F90:35-73):
+//
+//   collision (fluid.F90:14-64, solid nodes skipped), streaming from fluid
+//   sources (:97-108), four halfway-bounce-back walls (:115-161),
+//   bounceback_particle (particle_bounceback.F90:15-97, calQ :101-141 or
+//   calQ2 :144-185), macro (fluid.F90:164-184), calForce (particle_force.F90:
+//   35-190), updateCenter and refill (particle_update.F90:26-193).
+//
+// Layout: populations as f(0:8, i, j) with two ghost layers each side, the
+// reference's arrays (-1..nx+2 filled with omega*rho0; one more zero layer).
+// Everything is FP64 and this file is compiled without FMA contraction, so
+// each expression rounds as the reference's statement does.  Steps whose
+// order matters in the reference -- the density averages, each particle's
+// link sums, the refill sweep -- run sequentially in its loop order (one
+// thread, or one thread per particle); the rest is one thread per node.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+#include "mglc.h"
+#include "particles2d.cuh"
+
+namespace mglc {
+
+namespace {
+
+__device__ __constant__ int c_ex[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
+__device__ __constant__ int c_ey[9] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
+__device__ __constant__ int c_r[9] = {0, 3, 4, 1, 2, 7, 8, 5, 6};
+__device__ __constant__ double c_w[9] = {4.0 / 9.0, 1.0 / 9.0, 1.0 / 9.0, 1.0 / 9.0, 1.0 / 9.0,
+                                         1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0, 1.0 / 36.0};
+
+enum { S_NO_OWNER = 1, S_Q = 2, S_OVERLAP = 3, S_WALL = 4, S_NO_DIR = 5 };
+
+struct D2 {
+    P2Params p;
+    int X;  // padded row length nx + 6
+    double *f, *fp, *rho, *u, *v;
+    int *ob, *on;
+    double *xc, *uc, *om, *xco, *uco, *omo, *force, *torque;  // np x 3
+    double* ravg;                                             // [0] current average
+    int* status;                                              // [0] code, [1] particle
+};
+
+__device__ __forceinline__ int IX(const D2& d, int i, int j) { return (i + 2) + d.X * (j + 2); }
+__device__ __forceinline__ double& F(const D2& d, int a, int i, int j) { return d.f[9 * IX(d, i, j) + a]; }
+__device__ __forceinline__ double& FP(const D2& d, int a, int i, int j) { return d.fp[9 * IX(d, i, j) + a]; }
+__device__ __forceinline__ double sq(double x) { return x * x; }
+
+// ((x - xc)^2 + (y - yc)^2) <= R^2 (particle_bounceback.F90:50-52)
+__device__ __forceinline__ bool inside(const D2& d, const double* cen, int c, double x, double y) {
+    const double r = d.p.radius;
+    return sq(x - cen[3 * c]) + sq(y - cen[3 * c + 1]) <= sq(r);
+}
+
+__device__ void fail(const D2& d, int code, int c) {
+    if (atomicCAS(d.status, 0, code) == 0) d.status[1] = c;
+}
+
+// ------------------------------------------------------------------ fluid --
+__global__ void k2_collide(D2 d) {
+    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x, j = 1 + blockIdx.y;
+    if (i > d.p.nx || d.status[0] || d.ob[IX(d, i, j)] != 0) return;
+    double f[9], m[9], meq[9], s[9], mp[9];
+    for (int a = 0; a < 9; a++) f[a] = F(d, a, i, j);
+    const double rho = d.rho[IX(d, i, j)], u = d.u[IX(d, i, j)], v = d.v[IX(d, i, j)];
+    m[0] = f[0] + f[1] + f[2] + f[3] + f[4] + f[5] + f[6] + f[7] + f[8];
+    m[1] = -4.0 * f[0] - f[1] - f[2] - f[3] - f[4] + 2.0 * f[5] + 2.0 * f[6] + 2.0 * f[7] + 2.0 * f[8];
+    m[2] = 4.0 * f[0] - 2.0 * f[1] - 2.0 * f[2] - 2.0 * f[3] - 2.0 * f[4] + f[5] + f[6] + f[7] + f[8];
+    m[3] = f[1] - f[3] + f[5] - f[6] - f[7] + f[8];
+    m[4] = -2.0 * f[1] + 2.0 * f[3] + f[5] - f[6] - f[7] + f[8];
+    m[5] = f[2] - f[4] + f[5] + f[6] - f[7] - f[8];
+    m[6] = -2.0 * f[2] + 2.0 * f[4] + f[5] + f[6] - f[7] - f[8];
+    m[7] = f[1] - f[2] + f[3] - f[4];
+    m[8] = f[5] - f[6] + f[7] - f[8];
+    meq[0] = rho;
+    meq[1] = rho * (-2.0 + 3.0 * (u * u + v * v));
+    meq[2] = rho * (1.0 - 3.0 * (u * u + v * v));
+    meq[3] = rho * u;
+    meq[4] = -meq[3];
+    meq[5] = rho * v;
+    meq[6] = -meq[5];
+    meq[7] = rho * (u * u - v * v);
+    meq[8] = rho * (u * v);
+    const double Snu = d.p.snu, Sq = d.p.sq;
+    s[0] = 0.0; s[1] = Snu; s[2] = Snu; s[3] = 0.0; s[4] = Sq; s[5] = 0.0; s[6] = Sq;
+    s[7] = Snu; s[8] = Snu;
+    for (int a = 0; a < 9; a++) mp[a] = m[a] - s[a] * (m[a] - meq[a]);
+    FP(d, 0, i, j) = (mp[0] - mp[1] + mp[2]) / 9.0;
+    FP(d, 1, i, j) = mp[0] / 9.0 - mp[1] / 36.0 - mp[2] / 18.0 + mp[3] / 6.0 - mp[4] / 6.0 + mp[7] * 0.25;
+    FP(d, 2, i, j) = mp[0] / 9.0 - mp[1] / 36.0 - mp[2] / 18.0 + mp[5] / 6.0 - mp[6] / 6.0 - mp[7] * 0.25;
+    FP(d, 3, i, j) = mp[0] / 9.0 - mp[1] / 36.0 - mp[2] / 18.0 - mp[3] / 6.0 + mp[4] / 6.0 + mp[7] * 0.25;
+    FP(d, 4, i, j) = mp[0] / 9.0 - mp[1] / 36.0 - mp[2] / 18.0 - mp[5] / 6.0 + mp[6] / 6.0 - mp[7] * 0.25;
+    FP(d, 5, i, j) = mp[0] / 9.0 + mp[1] / 18.0 + mp[2] / 36.0 + mp[3] / 6.0 + mp[4] / 12.0 + mp[5] / 6.0 +
+                     mp[6] / 12.0 + mp[8] * 0.25;
+    FP(d, 6, i, j) = mp[0] / 9.0 + mp[1] / 18.0 + mp[2] / 36.0 - mp[3] / 6.0 - mp[4] / 12.0 + mp[5] / 6.0 +
+                     mp[6] / 12.0 - mp[8] * 0.25;
+    FP(d, 7, i, j) = mp[0] / 9.0 + mp[1] / 18.0 + mp[2] / 36.0 - mp[3] / 6.0 - mp[4] / 12.0 - mp[5] / 6.0 -
+                     mp[6] / 12.0 + mp[8] * 0.25;
+    FP(d, 8, i, j) = mp[0] / 9.0 + mp[1] / 18.0 + mp[2] / 36.0 + mp[3] / 6.0 + mp[4] / 12.0 - mp[5] / 6.0 -
+                     mp[6] / 12.0 - mp[8] * 0.25;
+}
+
+// pull from fluid sources only; every interior node (fluid or solid) receives
+__global__ void k2_stream(D2 d) {
+    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x, j = 1 + blockIdx.y;
+    if (i > d.p.nx || d.status[0]) return;
+    for (int a = 0; a < 9; a++) {
+        const int ip = i - c_ex[a], jp = j - c_ey[a];
+        if (d.ob[IX(d, ip, jp)] == 0) F(d, a, i, j) = FP(d, a, ip, jp);
+    }
+}
+
+// the four walls; corner nodes receive the same value from both of their walls
+__global__ void k2_walls(D2 d) {
+    const int t = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (d.status[0]) return;
+    const int nx = d.p.nx, ny = d.p.ny;
+    if (t <= ny) {
+        F(d, 1, 1, t) = FP(d, 3, 1, t);
+        F(d, 5, 1, t) = FP(d, 7, 1, t);
+        F(d, 8, 1, t) = FP(d, 6, 1, t);
+        F(d, 3, nx, t) = FP(d, 1, nx, t);
+        F(d, 6, nx, t) = FP(d, 8, nx, t);
+        F(d, 7, nx, t) = FP(d, 5, nx, t);
+    }
+    if (t <= nx) {
+        F(d, 2, t, 1) = FP(d, 4, t, 1);
+        F(d, 5, t, 1) = FP(d, 7, t, 1);
+        F(d, 6, t, 1) = FP(d, 8, t, 1);
+        F(d, 4, t, ny) = FP(d, 2, t, ny);
+        F(d, 7, t, ny) = FP(d, 5, t, ny);
+        F(d, 8, t, ny) = FP(d, 6, t, ny);
+    }
+}
+
+// average density over the fluid nodes of mask, in the reference's loop order
+__global__ void k2_rho_avg(D2 d, const int* mask) {
+    if (d.status[0]) return;
+    double acc = 0.0;
+    long long n = 0;
+    for (int j = 1; j <= d.p.ny; j++)
+        for (int i = 1; i <= d.p.nx; i++)
+            if (mask[IX(d, i, j)] == 0) {
+                acc = acc + d.rho[IX(d, i, j)];
+                n = n + 1;
+            }
+    d.ravg[0] = acc / (double)n;
+}
+
+// calQ / calQ2 from node (x, y) along direction a towards circle c
+__device__ bool calq(const D2& d, int c, double x, double y, int a, double& x0, double& y0,
+                     double& q) {
+    const double xc = d.xc[3 * c], yc = d.xc[3 * c + 1], R = d.p.radius;
+    const double z = 1.0, zc = 0.0;
+    (void)zc;
+    if (!d.p.q_bisection) {
+        const double ea = c_ex[a], eb = c_ey[a], ec = 0.0;
+        const double ca = ea * ea + eb * eb + ec * ec;
+        const double cb = 2.0 * (ea * (x - xc) + eb * (y - yc) + 0.0);
+        const double cc = (x - xc) * (x - xc) + (y - yc) * (y - yc) + 0.0 - R * R;
+        const double delta = cb * cb - 4.0 * ca * cc;
+        if (delta < 0) return false;
+        q = (-cb - sqrt(delta)) / (2.0 * ca);
+        x0 = x + q * ea;
+        y0 = y + q * eb;
+    } else {
+        const double epsR = (double)1e-9f;  // default-real literal 1e-9 (:106)
+        double qq = 0.5, qt = 0.5;
+        double px = x + qt * (double)c_ex[a], py = y + qt * (double)c_ey[a];
+        double pz = z + 0.0;
+        (void)pz;
+        auto dist = [&]() { return sqrt((px - xc) * (px - xc) + (py - yc) * (py - yc) + 0.0); };
+        int guard = 0;
+        while (fabs(dist() - R) >= epsR) {
+            if (++guard > 200) return false;
+            if (dist() > R) {
+                qt = qt / 2.0;
+                px = px + qt * (double)c_ex[a];
+                py = py + qt * (double)c_ey[a];
+                qq = qq + qt;
+            } else if (dist() < R) {
+                qt = qt / 2.0;
+                px = px - qt * (double)c_ex[a];
+                py = py - qt * (double)c_ey[a];
+                qq = qq - qt;
+            } else {
+                return false;
+            }
+        }
+        q = qq;
+        x0 = px;
+        y0 = py;
+    }
+    return !(q > 1.0 || q < 0.0);
+}
+
+// quadratic interpolated bounce-back (particle_bounceback.F90:37-97)
+__global__ void k2_ibb(D2 d) {
+    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x, j = 1 + blockIdx.y;
+    if (i > d.p.nx || d.status[0] || d.ob[IX(d, i, j)] != 0) return;
+    const double ravg = d.ravg[0];
+    for (int a = 1; a < 9; a++) {
+        const int ip = i + c_ex[a], jp = j + c_ey[a];
+        if (d.ob[IX(d, ip, jp)] != 1) continue;
+        bool found = false;
+        for (int c = 0; c < d.p.np; c++) {
+            if (!inside(d, d.xc, c, (double)ip, (double)jp)) continue;
+            found = true;
+            double x0, y0, q;
+            if (!calq(d, c, (double)i, (double)j, a, x0, y0, q)) {
+                fail(d, S_Q, c);
+                return;
+            }
+            const double Om = d.om[3 * c + 2];
+            const double rot0 = -(y0 - d.xc[3 * c + 1]) * Om, rot1 = (x0 - d.xc[3 * c]) * Om;
+            const int ra = c_r[a];
+            const double eu = c_ex[ra] * (d.uc[3 * c] + rot0) + c_ey[ra] * (d.uc[3 * c + 1] + rot1);
+            const int ex = c_ex[a], ey = c_ey[a];
+            if (q < 0.5) {
+                F(d, ra, i, j) = q * (1.0 + 2.0 * q) * FP(d, a, i, j) +
+                                 (1.0 - 4.0 * q * q) * FP(d, a, i - ex, j - ey) -
+                                 q * (1.0 - 2.0 * q) * FP(d, a, i - 2 * ex, j - 2 * ey) +
+                                 6.0 * c_w[a] * ravg * eu;
+            } else {
+                F(d, ra, i, j) = FP(d, a, i, j) / q / (1.0 + 2.0 * q) +
+                                 FP(d, ra, i, j) * (2.0 * q - 1.0) / q -
+                                 FP(d, ra, i - ex, j - ey) * (2.0 * q - 1.0) / (2.0 * q + 1.0) +
+                                 6.0 * c_w[a] * ravg / q / (1.0 + 2.0 * q) * eu;
+            }
+        }
+        if (!found) {
+            fail(d, S_NO_OWNER, -1);
+            return;
+        }
+    }
+}
+
+__global__ void k2_macro(D2 d) {
+    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x, j = 1 + blockIdx.y;
+    if (i > d.p.nx || d.status[0] || d.ob[IX(d, i, j)] != 0) return;
+    double g[9];
+    for (int a = 0; a < 9; a++) g[a] = F(d, a, i, j);
+    const double r = g[0] + g[1] + g[2] + g[3] + g[4] + g[5] + g[6] + g[7] + g[8];
+    d.rho[IX(d, i, j)] = r;
+    d.u[IX(d, i, j)] = (g[1] - g[3] + g[5] - g[6] - g[7] + g[8]) / r;
+    d.v[IX(d, i, j)] = (g[2] - g[4] + g[5] + g[6] - g[7] - g[8]) / r;
+}
+
+// calForce (particle_force.F90:35-190): one thread per circle; its links are
+// visited in the reference's global loop order restricted to its box
+__global__ void k2_force(D2 d) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.p.np || d.status[0]) return;
+    const P2Params& p = d.p;
+    const double PI = p.pi, R0 = p.radius, ravg = d.ravg[0];
+    const double xcc = d.xc[3 * c], ycc = d.xc[3 * c + 1];
+    const int i0 = max(1, (int)floor(xcc - R0) - 2), i1 = min(p.nx, (int)ceil(xcc + R0) + 2);
+    const int j0 = max(1, (int)floor(ycc - R0) - 2), j1 = min(p.ny, (int)ceil(ycc + R0) + 2);
+    double fs0 = 0.0, fs1 = 0.0, ts = 0.0;
+    for (int j = j0; j <= j1; j++)
+        for (int i = i0; i <= i1; i++) {
+            if (d.ob[IX(d, i, j)] != 0) continue;
+            for (int a = 1; a < 9; a++) {
+                const int ip = i + c_ex[a], jp = j + c_ey[a];
+                if (d.ob[IX(d, ip, jp)] != 1) continue;
+                if (!inside(d, d.xc, c, (double)ip, (double)jp)) continue;
+                double x0, y0, q;
+                if (!calq(d, c, (double)i, (double)j, a, x0, y0, q)) {
+                    fail(d, S_Q, c);
+                    return;
+                }
+                const double Om = d.om[3 * c + 2];
+                const double rot0 = -(y0 - ycc) * Om, rot1 = (x0 - xcc) * Om;
+                const int ra = c_r[a];
+                const double U0 = d.uc[3 * c], U1 = d.uc[3 * c + 1];
+                const double Fx = (c_ex[a] - U0 - rot0) * FP(d, a, i, j) - (c_ex[ra] - U0 - rot0) * F(d, ra, i, j);
+                const double Fy = (c_ey[a] - U1 - rot1) * FP(d, a, i, j) - (c_ey[ra] - U1 - rot1) * F(d, ra, i, j);
+                const double rx = x0 - xcc, ry = y0 - ycc;
+                const double T = rx * Fy - ry * Fx;
+                fs0 = fs0 + Fx;
+                fs1 = fs1 + Fy;
+                ts = ts + T;
+            }
+        }
+    const double gmag = fabs(-p.gravity);
+    double fij[3] = {0.0, 0.0, 0.0}, fw[3] = {0.0, 0.0, 0.0};
+    const double Rc = R0;
+    // particle-particle springs (:100-125)
+    const double scale_p = PI * (Rc * Rc) * (p.rho_solid - ravg) * gmag / p.stiff_particle;
+    for (int c2 = 0; c2 < p.np; c2++) {
+        if (c2 == c) continue;
+        const double d0 = d.xc[3 * c] - d.xc[3 * c2];
+        const double d1 = d.xc[3 * c + 1] - d.xc[3 * c2 + 1];
+        const double d2 = 0.0;
+        const double dij = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+        const double R2 = R0, thr = p.threshold_particle;
+        if (dij >= Rc + R2 + thr) {
+        } else if (dij < Rc + R2 + thr && dij >= Rc + R2) {
+            const double t = (dij - Rc - R2 - thr) / thr;
+            fij[0] = fij[0] + scale_p * (t * t) * d0 / dij;
+            fij[1] = fij[1] + scale_p * (t * t) * d1 / dij;
+            fij[2] = fij[2] + scale_p * (t * t) * d2 / dij;
+        } else {
+            fail(d, S_OVERLAP, c);
+            return;
+        }
+    }
+    // particle-wall springs (:128-178): left, right, bottom (no top spring)
+    const double scale_w = PI * (Rc * Rc) * (p.rho_solid - p.rho0) * gmag / p.stiff_wall;
+    const double thw = p.threshold_wall;
+    for (int ax = 0; ax < 2; ax++) {
+        const int n_ax = ax == 0 ? p.nx : p.ny;
+        const bool high = ax == 0;
+        const double cpos = d.xc[3 * c + ax];
+        double dw = cpos - Rc - 1.0;
+        if (dw < 0) { fail(d, S_WALL, c); return; }
+        if (dw < thw) fw[ax] = fw[ax] + scale_w * ((dw - thw) / thw) * ((dw - thw) / thw);
+        if (high) {
+            dw = (double)n_ax - cpos - Rc;
+            if (dw < 0) { fail(d, S_WALL, c); return; }
+            if (dw < thw) fw[ax] = fw[ax] - scale_w * ((dw - thw) / thw) * ((dw - thw) / thw);
+        }
+    }
+    // totals (:184-190)
+    d.force[3 * c] = fs0 + fij[0] + fw[0];
+    d.force[3 * c + 1] = fs1 - (p.rho_solid - ravg) * PI * (R0 * R0) * gmag + fij[1] + fw[1];
+    d.force[3 * c + 2] = 0.0;
+    d.torque[3 * c] = 0.0;
+    d.torque[3 * c + 1] = 0.0;
+    d.torque[3 * c + 2] = ts;
+}
+
+// updateCenter (particle_update.F90:26-50): U += F/M, Omega += T/I, x += U_old + a/2
+__global__ void k2_move(D2 d) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.p.np || d.status[0]) return;
+    const P2Params& p = d.p;
+    for (int q = 0; q < 3; q++) {
+        d.xco[3 * c + q] = d.xc[3 * c + q];
+        d.uco[3 * c + q] = d.uc[3 * c + q];
+        d.omo[3 * c + q] = d.om[3 * c + q];
+    }
+    const double PI = p.pi, R0 = p.radius, r = p.radius;
+    const double ax = d.force[3 * c] / PI / (R0 * R0) / p.rho_solid;
+    const double ay = d.force[3 * c + 1] / PI / (R0 * R0) / p.rho_solid;
+    const double aom = d.torque[3 * c + 2] / (0.5 * p.rho_solid * PI * (r * r * r * r));
+    d.uc[3 * c] = d.uco[3 * c] + ax;
+    d.uc[3 * c + 1] = d.uco[3 * c + 1] + ay;
+    d.om[3 * c + 2] = d.omo[3 * c + 2] + aom;
+    d.xc[3 * c] = d.xco[3 * c] + d.uco[3 * c] + 0.5 * ax;
+    d.xc[3 * c + 1] = d.xco[3 * c + 1] + d.uco[3 * c + 1] + 0.5 * ay;
+}
+
+// obst from the centres over 0..nx+1 x 0..ny+1 (particle_update.F90:80-93);
+// interior solid nodes get rho_s and u = 0 (:94-102)
+__global__ void k2_mask(D2 d, int* mask, bool set_macro) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i > d.p.nx + 1 || d.status[0]) return;
+    int o = 0;
+    for (int c = 0; c < d.p.np; c++)
+        if (inside(d, d.xc, c, (double)i, (double)j)) o = 1;
+    mask[IX(d, i, j)] = o;
+    if (set_macro && o == 1 && i >= 1 && i <= d.p.nx && j >= 1 && j <= d.p.ny) {
+        d.rho[IX(d, i, j)] = d.p.rho_solid;
+        d.u[IX(d, i, j)] = 0.0;
+        d.v[IX(d, i, j)] = 0.0;
+    }
+}
+
+// refill of nodes that left a circle (particle_update.F90:122-193), in the
+// reference's sequential sweep order (each refill may read an earlier one)
+__global__ void k2_refill(D2 d) {
+    if (d.status[0]) return;
+    const P2Params& p = d.p;
+    const double ra = d.ravg[0];
+    for (int j = 1; j <= p.ny; j++)
+        for (int i = 1; i <= p.nx; i++) {
+            if (!(d.ob[IX(d, i, j)] == 1 && d.on[IX(d, i, j)] == 0)) continue;
+            bool found = false;
+            for (int c = 0; c < p.np; c++) {
+                if (!inside(d, d.xco, c, (double)i, (double)j)) continue;
+                found = true;
+                const double xc = d.xc[3 * c], yc = d.xc[3 * c + 1];
+                double out = 0.0;
+                int ec = 0;
+                for (int a = 1; a < 9; a++) {
+                    const double t = ((i - xc) * c_ex[a] + (j - yc) * c_ey[a]) /
+                                     sqrt((i - xc) * (i - xc) + (j - yc) * (j - yc));
+                    if (t > out) {
+                        out = t;
+                        ec = a;
+                    }
+                }
+                if (ec == 0) {
+                    fail(d, S_NO_DIR, c);
+                    return;
+                }
+                const int e0 = c_ex[ec], e1 = c_ey[ec];
+                for (int a = 0; a < 9; a++)
+                    F(d, a, i, j) = 3.0 * F(d, a, i + e0, j + e1) - 3.0 * F(d, a, i + 2 * e0, j + 2 * e1) +
+                                    F(d, a, i + 3 * e0, j + 3 * e1);
+                double G[9], m[9];
+                for (int a = 0; a < 9; a++) G[a] = F(d, a, i, j);
+                m[0] = G[0] + G[1] + G[2] + G[3] + G[4] + G[5] + G[6] + G[7] + G[8];
+                m[1] = -4.0 * G[0] - G[1] - G[2] - G[3] - G[4] + 2.0 * G[5] + 2.0 * G[6] + 2.0 * G[7] + 2.0 * G[8];
+                m[2] = 4.0 * G[0] - 2.0 * G[1] - 2.0 * G[2] - 2.0 * G[3] - 2.0 * G[4] + G[5] + G[6] + G[7] + G[8];
+                m[3] = ra * (d.uc[3 * c] - (j - yc) * d.om[3 * c + 2]);
+                m[4] = -2.0 * G[1] + 2.0 * G[3] + G[5] - G[6] - G[7] + G[8];
+                m[5] = ra * (d.uc[3 * c + 1] + (i - xc) * d.om[3 * c + 2]);
+                m[6] = -2.0 * G[2] + 2.0 * G[4] + G[5] + G[6] - G[7] - G[8];
+                m[7] = G[1] - G[2] + G[3] - G[4];
+                m[8] = G[5] - G[6] + G[7] - G[8];
+                G[0] = (m[0] - m[1] + m[2]) / 9.0;
+                G[1] = m[0] / 9.0 - m[1] / 36.0 - m[2] / 18.0 + m[3] / 6.0 - m[4] / 6.0 + m[7] * 0.25;
+                G[2] = m[0] / 9.0 - m[1] / 36.0 - m[2] / 18.0 + m[5] / 6.0 - m[6] / 6.0 - m[7] * 0.25;
+                G[3] = m[0] / 9.0 - m[1] / 36.0 - m[2] / 18.0 - m[3] / 6.0 + m[4] / 6.0 + m[7] * 0.25;
+                G[4] = m[0] / 9.0 - m[1] / 36.0 - m[2] / 18.0 - m[5] / 6.0 + m[6] / 6.0 - m[7] * 0.25;
+                G[5] = m[0] / 9.0 + m[1] / 18.0 + m[2] / 36.0 + m[3] / 6.0 + m[4] / 12.0 + m[5] / 6.0 +
+                       m[6] / 12.0 + m[8] * 0.25;
+                G[6] = m[0] / 9.0 + m[1] / 18.0 + m[2] / 36.0 - m[3] / 6.0 - m[4] / 12.0 + m[5] / 6.0 +
+                       m[6] / 12.0 - m[8] * 0.25;
+                G[7] = m[0] / 9.0 + m[1] / 18.0 + m[2] / 36.0 - m[3] / 6.0 - m[4] / 12.0 - m[5] / 6.0 -
+                       m[6] / 12.0 + m[8] * 0.25;
+                G[8] = m[0] / 9.0 + m[1] / 18.0 + m[2] / 36.0 + m[3] / 6.0 + m[4] / 12.0 - m[5] / 6.0 -
+                       m[6] / 12.0 - m[8] * 0.25;
+                for (int a = 0; a < 9; a++) F(d, a, i, j) = G[a];
+                const double r = G[0] + G[1] + G[2] + G[3] + G[4] + G[5] + G[6] + G[7] + G[8];
+                d.rho[IX(d, i, j)] = r;
+                d.u[IX(d, i, j)] = (G[1] - G[3] + G[5] - G[6] - G[7] + G[8]) / r;
+                d.v[IX(d, i, j)] = (G[2] - G[4] + G[5] + G[6] - G[7] - G[8]) / r;
+            }
+            if (!found) {
+                fail(d, S_NO_OWNER, -1);
+                return;
+            }
+        }
+}
+
+// initial.F90:103-188 with the centres given by the caller: mask, rho = rho_s
+// (solid) or rho0, u = 0, f = omega on fluid nodes, ghosts omega*rho0
+__global__ void k2_init_fields(D2 d) {
+    const int i = -2 + (int)(blockIdx.x * blockDim.x + threadIdx.x), j = -2 + (int)blockIdx.y;
+    if (i > d.p.nx + 3) return;
+    const int nx = d.p.nx, ny = d.p.ny;
+    const bool interior = i >= 1 && i <= nx && j >= 1 && j <= ny;
+    const bool ghost = !interior && i >= -1 && i <= nx + 2 && j >= -1 && j <= ny + 2;
+    if (interior) {
+        const bool solid = d.ob[IX(d, i, j)] == 1;
+        d.rho[IX(d, i, j)] = solid ? d.p.rho_solid : d.p.rho0;
+        d.u[IX(d, i, j)] = 0.0;
+        d.v[IX(d, i, j)] = 0.0;
+        if (!solid) {
+            const double uu = 0.0, vv = 0.0, us2 = uu * uu + vv * vv;
+            for (int a = 0; a < 9; a++) {
+                const double un = uu * c_ex[a] + vv * c_ey[a];
+                F(d, a, i, j) = c_w[a] * (1.0 + 3.0 * un + 4.5 * un * un - 1.5 * us2);
+            }
+        }
+    } else if (ghost) {
+        for (int a = 0; a < 9; a++) {
+            F(d, a, i, j) = c_w[a] * d.p.rho0;
+            FP(d, a, i, j) = c_w[a] * d.p.rho0;
+        }
+    }
+}
+
+// owner index of every interior node (-1 fluid)
+__global__ void k2_owner(D2 d, int* out) {
+    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x, j = 1 + blockIdx.y;
+    if (i > d.p.nx) return;
+    int o = -1;
+    if (d.ob[IX(d, i, j)] == 1)
+        for (int c = 0; c < d.p.np && o < 0; c++)
+            if (inside(d, d.xc, c, (double)i, (double)j)) o = c;
+    out[(i - 1) + d.p.nx * (j - 1)] = o;
+}
+
+}  // namespace
+
+struct P2Ctx {
+    D2 d{};
+    cudaStream_t s = nullptr;
+    bool own_stream = false;
+    std::vector<double> centers;  // np x 3
+    long long itc = 0;
+    long long bytes = 0;
+    int* owner_tmp = nullptr;
+};
+
+namespace {
+
+int ck(cudaError_t e, const char* what, std::string& err) {
+    if (e == cudaSuccess) return MGLC_OK;
+    err = std::string(what) + ": " + cudaGetErrorString(e);
+    return MGLC_ERR_CUDA;
+}
+
+template <typename T>
+int dal(P2Ctx* c, T** p, size_t n, std::string& err) {
+    cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        err = std::string("device allocation: ") + cudaGetErrorString(e);
+        return MGLC_ERR_NOMEM;
+    }
+    c->bytes += (long long)(n * sizeof(T));
+    return cudaMemsetAsync(*p, 0, n * sizeof(T), c->s) == cudaSuccess ? MGLC_OK : MGLC_ERR_CUDA;
+}
+
+dim3 rows_grid(const D2& d) { return dim3((d.p.nx + 127) / 128, d.p.ny); }
+
+}  // namespace
+
+int p2d_create(const P2Params& p, const double* centers_xy, P2Ctx** out, std::string& err) {
+    P2Ctx* c = new P2Ctx();
+    *out = c;
+    c->d.p = p;
+    c->d.X = p.nx + 6;
+    if (cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) != cudaSuccess) {
+        err = "stream creation failed";
+        return MGLC_ERR_CUDA;
+    }
+    c->own_stream = true;
+    const size_t cells = (size_t)(p.nx + 6) * (p.ny + 6), np3 = 3 * (size_t)(p.np > 0 ? p.np : 1);
+    D2& d = c->d;
+    int rc = 0;
+    if ((rc = dal(c, &d.f, 9 * cells, err)) || (rc = dal(c, &d.fp, 9 * cells, err)) ||
+        (rc = dal(c, &d.rho, cells, err)) || (rc = dal(c, &d.u, cells, err)) ||
+        (rc = dal(c, &d.v, cells, err)) || (rc = dal(c, &d.ob, cells, err)) ||
+        (rc = dal(c, &d.on, cells, err)))
+        return rc;
+    double** pa[] = {&d.xc, &d.uc, &d.om, &d.xco, &d.uco, &d.omo, &d.force, &d.torque};
+    for (double** a : pa)
+        if ((rc = dal(c, a, np3, err))) return rc;
+    if ((rc = dal(c, &d.ravg, 2, err)) || (rc = dal(c, &d.status, 2, err)) ||
+        (rc = dal(c, &c->owner_tmp, (size_t)p.nx * p.ny, err)))
+        return rc;
+    c->centers.assign(3 * (size_t)p.np, 0.0);
+    for (int q = 0; q < p.np; q++) {
+        c->centers[3 * q] = centers_xy[2 * q];
+        c->centers[3 * q + 1] = centers_xy[2 * q + 1];
+    }
+    return ck(cudaStreamSynchronize(c->s), "create", err);
+}
+
+void p2d_destroy(P2Ctx* c) {
+    if (!c) return;
+    D2& d = c->d;
+    void* ps[] = {d.f, d.fp, d.rho, d.u, d.v, d.ob, d.on, d.xc, d.uc, d.om, d.xco, d.uco, d.omo,
+                  d.force, d.torque, d.ravg, d.status, c->owner_tmp};
+    if (c->s) cudaStreamSynchronize(c->s);
+    for (void* p : ps)
+        if (p) cudaFree(p);
+    if (c->own_stream && c->s) cudaStreamDestroy(c->s);
+    delete c;
+}
+
+int p2d_set_stream(P2Ctx* c, cudaStream_t s) {
+    if (c->own_stream && c->s) cudaStreamSynchronize(c->s);
+    if (!s) return MGLC_OK;  // keep the current stream
+    if (c->own_stream) cudaStreamDestroy(c->s);
+    c->s = s;
+    c->own_stream = false;
+    return MGLC_OK;
+}
+
+int p2d_initial(P2Ctx* c, std::string& err) {
+    D2& d = c->d;
+    const size_t cells = (size_t)d.X * (d.p.ny + 6), np3 = 3 * (size_t)(d.p.np > 0 ? d.p.np : 1);
+    int rc = 0;
+    for (auto& pr : {std::make_pair((void*)d.f, 9 * cells * 8), std::make_pair((void*)d.fp, 9 * cells * 8),
+                     std::make_pair((void*)d.ob, cells * 4), std::make_pair((void*)d.on, cells * 4),
+                     std::make_pair((void*)d.uc, np3 * 8), std::make_pair((void*)d.om, np3 * 8),
+                     std::make_pair((void*)d.force, np3 * 8), std::make_pair((void*)d.torque, np3 * 8),
+                     std::make_pair((void*)d.status, (size_t)8)})
+        if ((rc = ck(cudaMemsetAsync(pr.first, 0, pr.second, c->s), "reset", err))) return rc;
+    if (d.p.np > 0) {
+        if ((rc = ck(cudaMemcpyAsync(d.xc, c->centers.data(), sizeof(double) * 3 * d.p.np,
+                                     cudaMemcpyHostToDevice, c->s), "centres", err)))
+            return rc;
+        if ((rc = ck(cudaMemcpyAsync(d.xco, d.xc, sizeof(double) * 3 * d.p.np, cudaMemcpyDeviceToDevice,
+                                     c->s), "centres", err)))
+            return rc;
+    }
+    k2_mask<<<dim3((d.p.nx + 2 + 127) / 128, d.p.ny + 2), 128, 0, c->s>>>(d, d.ob, false);
+    k2_init_fields<<<dim3((d.p.nx + 6 + 127) / 128, d.p.ny + 6), 128, 0, c->s>>>(d);
+    c->itc = 0;
+    return ck(cudaStreamSynchronize(c->s), "initial", err);
+}
+
+int p2d_step(P2Ctx* c, int nsteps, std::string& err) {
+    D2& d = c->d;
+    const dim3 g = rows_grid(d);
+    const int nw = d.p.nx > d.p.ny ? d.p.nx : d.p.ny;
+    const int pg = (d.p.np + 63) / 64;
+    const size_t cells = (size_t)d.X * (d.p.ny + 6);
+    for (int n = 0; n < nsteps; n++) {
+        k2_collide<<<g, 128, 0, c->s>>>(d);
+        k2_stream<<<g, 128, 0, c->s>>>(d);
+        k2_walls<<<(nw + 127) / 128, 128, 0, c->s>>>(d);
+        k2_rho_avg<<<1, 1, 0, c->s>>>(d, d.ob);
+        k2_ibb<<<g, 128, 0, c->s>>>(d);
+        k2_macro<<<g, 128, 0, c->s>>>(d);
+        if (d.p.np > 0) {
+            k2_force<<<pg, 64, 0, c->s>>>(d);
+            k2_move<<<pg, 64, 0, c->s>>>(d);
+        }
+        k2_mask<<<dim3((d.p.nx + 2 + 127) / 128, d.p.ny + 2), 128, 0, c->s>>>(d, d.on, true);
+        k2_rho_avg<<<1, 1, 0, c->s>>>(d, d.on);
+        k2_refill<<<1, 1, 0, c->s>>>(d);
+        cudaMemcpyAsync(d.ob, d.on, cells * sizeof(int), cudaMemcpyDeviceToDevice, c->s);
+        c->itc++;
+    }
+    int st[2] = {0, 0};
+    int rc = ck(cudaGetLastError(), "particle step launch", err);
+    if (!rc) rc = ck(cudaMemcpyAsync(st, d.status, sizeof st, cudaMemcpyDeviceToHost, c->s), "status", err);
+    if (!rc) rc = ck(cudaStreamSynchronize(c->s), "particle step", err);
+    if (rc) return rc;
+    if (st[0]) {
+        static const char* what[] = {"", "no circle owns a solid boundary node",
+                                     "interpolation fraction q outside [0,1]",
+                                     "particle-particle interpenetration",
+                                     "particle penetrates a wall",
+                                     "no refill direction for a node leaving a circle"};
+        char buf[200];
+        std::snprintf(buf, sizeof buf, "%s (circle %d); the state is frozen at that step",
+                      what[st[0] < 6 ? st[0] : 0], st[1]);
+        err = buf;
+        return MGLC_ERR_PARTICLE;
+    }
+    return MGLC_OK;
+}
+
+namespace {
+// interior of a padded device array, row by row (x fastest)
+template <typename T>
+int get_interior(P2Ctx* c, const T* dev, int per, T* host, std::string& err) {
+    const D2& d = c->d;
+    const size_t pitch = sizeof(T) * per * d.X;
+    const T* first = dev + (size_t)per * (3 + (size_t)d.X * 3);  // node (1, 1)
+    cudaError_t e = cudaMemcpy2DAsync(host, sizeof(T) * per * d.p.nx, first, pitch,
+                                      sizeof(T) * per * d.p.nx, d.p.ny, cudaMemcpyDeviceToHost, c->s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->s);
+    return ck(e, "copy to host", err);
+}
+}  // namespace
+
+int p2d_get_f(P2Ctx* c, double* f, std::string& err) { return get_interior(c, c->d.f, 9, f, err); }
+
+int p2d_get_macros(P2Ctx* c, double* rho, double* u, double* v, double* w, std::string& err) {
+    int rc = 0;
+    if (rho && (rc = get_interior(c, c->d.rho, 1, rho, err))) return rc;
+    if (u && (rc = get_interior(c, c->d.u, 1, u, err))) return rc;
+    if (v && (rc = get_interior(c, c->d.v, 1, v, err))) return rc;
+    if (w) std::memset(w, 0, sizeof(double) * (size_t)c->d.p.nx * c->d.p.ny);
+    return MGLC_OK;
+}
+
+int p2d_state(P2Ctx* c, double* xc, double* uc, double* omega, double* force, double* torque,
+              std::string& err) {
+    const D2& d = c->d;
+    const size_t b = sizeof(double) * 3 * d.p.np;
+    const double* src[] = {d.xc, d.uc, d.om, d.force, d.torque};
+    double* dst[] = {xc, uc, omega, force, torque};
+    for (int q = 0; q < 5; q++)
+        if (dst[q] && b) {
+            int rc = ck(cudaMemcpyAsync(dst[q], src[q], b, cudaMemcpyDeviceToHost, c->s), "state", err);
+            if (rc) return rc;
+        }
+    return ck(cudaStreamSynchronize(c->s), "state", err);
+}
+
+int p2d_mask(P2Ctx* c, int* owner, std::string& err) {
+    const D2& d = c->d;
+    k2_owner<<<rows_grid(d), 128, 0, c->s>>>(d, c->owner_tmp);
+    cudaError_t e = cudaMemcpyAsync(owner, c->owner_tmp, sizeof(int) * (size_t)d.p.nx * d.p.ny,
+                                    cudaMemcpyDeviceToHost, c->s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->s);
+    return ck(e, "mask", err);
+}
+
+long long p2d_itc(const P2Ctx* c) { return c->itc; }
+long long p2d_device_bytes(const P2Ctx* c) { return c->bytes; }
+
+double p2d_rho_avg(P2Ctx* c) {
+    double r = 0.0;
+    cudaMemcpyAsync(&r, c->d.ravg, sizeof r, cudaMemcpyDeviceToHost, c->s);
+    cudaStreamSynchronize(c->s);
+    return r;
+}
+
+}  // namespace mglc
