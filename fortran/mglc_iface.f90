@@ -28,6 +28,15 @@ module mglc_iface
         integer(c_int) :: bc_y_const_t, bc_z_const_t, precision
     end type
 
+    type, bind(C) :: mglc_particle_params
+        integer(c_int) :: total_nx, total_ny, total_nz, periodic_x
+        real(c_double) :: tauf, rho0, rho_solid, radius
+        real(c_double) :: gravity(3), body_force(3)
+        real(c_double) :: threshold_wall, threshold_particle
+        real(c_double) :: spring_scale_wall, spring_scale_particle
+        integer(c_int) :: precision
+    end type
+
     type, bind(C) :: mglc_particle2d_params
         integer(c_int) :: total_nx, total_ny
         real(c_double) :: tauf, rho0, rho_solid, radius, gravity
@@ -98,6 +107,20 @@ module mglc_iface
             import :: c_int, c_ptr, c_double
             type(c_ptr), value :: ctx
             real(c_double), intent(out) :: nu_vol, re_vol, nu_hot, nu_cold
+        end function
+        !! spheres (D3Q19): centers(3, np)
+        integer(c_int) function mglc_particle_create(p, centers, np, ctx) &
+                bind(C, name="mglc_particle_create")
+            import :: c_int, c_ptr, c_double, mglc_particle_params
+            type(mglc_particle_params), intent(in) :: p
+            real(c_double), intent(in) :: centers(*)
+            integer(c_int), value :: np
+            type(c_ptr), intent(out) :: ctx
+        end function
+        integer(c_int) function mglc_get_mask(ctx, owner) bind(C, name="mglc_get_mask")
+            import :: c_int, c_ptr
+            type(c_ptr), value :: ctx
+            integer(c_int), intent(out) :: owner(*)
         end function
         !! case4 (D2Q9) particles: centers(2, np)
         integer(c_int) function mglc_particle2d_create(p, centers, np, ctx) &
