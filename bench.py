@@ -35,11 +35,11 @@ sys.path.insert(0, ROOT)
 METRIC = "MLUPS, %HBM roofline: mixed vs FP64 plain at ≤1e-3 err; serve p50/p99 ms"
 
 WORKLOADS = {
-    "lid384": dict(kind="lid", n=384, reynolds=1000.0, u0=0.1,
+    "lid384": dict(kind="lid", n=384, reynolds=1000.0, u0=0.1, error_steps=1000,
                    desc="lid-driven cavity D3Q19 MRT 384^3 Re=1000 U=0.1"),
-    "lid64": dict(kind="lid", n=64, reynolds=400.0, u0=0.1,
+    "lid64": dict(kind="lid", n=64, reynolds=400.0, u0=0.1, error_steps=2000,
                   desc="lid-driven cavity D3Q19 MRT 64^3 Re=400 U=0.1"),
-    "thermal128": dict(kind="thermal", n=128, rayleigh=1e5, prandtl=0.71, mach=0.1,
+    "thermal128": dict(kind="thermal", n=128, rayleigh=1e5, prandtl=0.71, mach=0.1, error_steps=20000,
                        desc="differentially heated cavity D3Q19+D3Q7 128^3 Ra=1e5 Pr=0.71"),
     "particles": dict(kind="particle", n=(256, 128, 128), np=200, radius=5.0, ratio=1.2,
                       body_force=1e-6, tauf=0.65, seed=2026, launches_per_step=11,
@@ -281,6 +281,40 @@ def time_e2e_particles(torch, s, wl, steps, dist=None):
     return dt, 0, (8 * 4 * cells + 8 * 15 * wl["np"]) / steps, 0.0
 
 
+def rel_l2(a, b):
+    return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
+
+
+def form_errors(mg, wl, forms, steps):
+    """Velocity (and temperature, wall Nusselt) error of each form against
+    the FP64 plain method on the workload's own grid, after `steps` steps
+    from the same initial state."""
+    def run(form):
+        s = make_solve(mg, wl, form)
+        s.initial()
+        s.step(steps)
+        r = s.macro()
+        out = {"U": np.stack(r[1:4])}
+        if wl["kind"] == "thermal":
+            out["T"] = r[4]
+            out["nu"] = s.nusselt()
+        s.close()
+        return out
+    ref = run("fp64")
+    res = {}
+    for fm in forms:
+        try:
+            got = run(fm)
+            e = {"u_rel_l2_vs_fp64": rel_l2(got["U"], ref["U"])}
+            if wl["kind"] == "thermal":
+                e["T_rel_l2_vs_fp64"] = rel_l2(got["T"], ref["T"])
+                e["nu_hot_rel_vs_fp64"] = abs(got["nu"][2] - ref["nu"][2]) / abs(ref["nu"][2])
+            res[fm] = e
+        except Exception as ex:  # report, never hide
+            res[fm] = {"error_run_failed": str(ex)}
+    return res
+
+
 def serve_bench(torch, mg, n_req=24, rate=50.0, seed=1234, max_steps=2000, tol=1e-6, K=100,
                 precision="fp16"):
     """Batched serving stream: Poisson arrivals of lid-driven and heated-cavity
@@ -449,12 +483,17 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="mglc", choices=["mglc", "reference"])
     ap.add_argument("--workload", default="lid384", choices=sorted(WORKLOADS))
-    ap.add_argument("--form", default="fp64", choices=["fp64", "fx64", "fp32", "fp16", "bf16"])
+    ap.add_argument("--form", default="fp64",
+                    choices=["fp64", "fx64", "fp32", "fp16", "fp16s", "bf16", "bf16s"])
     ap.add_argument("--no-forms", action="store_true", help="skip timing the other storage forms")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--n", type=int, default=0, help="override the cube size (profiling runs)")
     ap.add_argument("--no-serve", action="store_true", help="skip the batched-serving stream")
+    ap.add_argument("--no-error", action="store_true",
+                    help="skip measuring each form's error against FP64")
+    ap.add_argument("--error-steps", type=int, default=0,
+                    help="steps for the error runs (default: the workload's own count)")
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-max-steps", type=int, default=2000)
     args = ap.parse_args()
@@ -521,8 +560,9 @@ def main():
                                "+ mglc_check, wall clock"}
     if rank == 0 and not args.no_forms:
         forms = {}
-        fms = {"particle": ("fp64", "fp32"), "thermal": ("fp64", "fp32", "fp16", "bf16"),
-               "lid": ("fp64", "fx64", "fp32", "fp16", "bf16")}[wl["kind"]]
+        fms = {"particle": ("fp64", "fp32"),
+               "thermal": ("fp64", "fp32", "fp16", "fp16s", "bf16", "bf16s"),
+               "lid": ("fp64", "fx64", "fp32", "fp16", "fp16s", "bf16", "bf16s")}[wl["kind"]]
         for fm in fms:
             if fm == args.form:
                 continue
@@ -535,7 +575,25 @@ def main():
                              "achieved_gbs": round(a2, 1), "frac": round(a2 / peak, 4)}
             except Exception as e:  # report, never hide
                 forms[fm] = {"error": str(e)}
+        if not args.no_error and wl["kind"] in ("lid", "thermal"):
+            esteps = args.error_steps or wl.get("error_steps", 1000)
+            errs = form_errors(mglc_gb300, wl, [f for f in fms if f != "fp64"], esteps)
+            for fm, e in errs.items():
+                forms.setdefault(fm, {}).update(e)
+                forms[fm]["error_steps"] = esteps
         line["forms"] = forms
+        # the metric's "mixed" form: FP16 deviation storage (stochastic
+        # rounding), FP32 arithmetic
+        mx = forms.get("fp16s", {})
+        base = value if args.form == "fp64" else forms.get("fp64", {}).get("value")
+        if "value" in mx and base:
+            line["mixed"] = {"form": "fp16 storage of f - w rho0 (stochastic rounding), fp32 arithmetic",
+                             "value": mx["value"], "unit": "MLUPS", "frac": mx["frac"],
+                             "speedup_vs_fp64_plain": round(mx["value"] / base, 2),
+                             "u_rel_l2_vs_fp64": mx.get("u_rel_l2_vs_fp64"),
+                             "error_steps": mx.get("error_steps"),
+                             "within_1e-3": (mx["u_rel_l2_vs_fp64"] <= 1e-3)
+                             if "u_rel_l2_vs_fp64" in mx else None}
     if rank == 0 and not args.no_serve and wl["kind"] == "lid":
         line["serve"] = serve_bench(torch, mglc_gb300, n_req=args.serve_requests,
                                     max_steps=args.serve_max_steps)

@@ -43,8 +43,14 @@ extern "C" {
  *  type, FP32 arithmetic; FP64 kept for reductions (residual, totals).
  *  FX64 (lid-driven cavity only): FP64 storage; the collision runs in 64-bit
  *  fixed point with 55 fractional bits (exact moment transforms, one rounding
- *  to FP64 per stored population), everything else as FP64. */
-enum { MGLC_FP64 = 0, MGLC_FP32 = 1, MGLC_FP16 = 2, MGLC_BF16 = 3, MGLC_FX64 = 4 };
+ *  to FP64 per stored population), everything else as FP64.
+ *  FP16S/BF16S: FP16/BF16 deviation storage written with stochastic rounding
+ *  (unbiased; the storage error stays at its one-step level instead of
+ *  accumulating over a transient).  The stored state then fluctuates at the
+ *  16-bit resolution, so a steady state is not a fixed point: for runs to
+ *  convergence (max|du|/U below ~1e-4) use FP16/BF16 (round to nearest). */
+enum { MGLC_FP64 = 0, MGLC_FP32 = 1, MGLC_FP16 = 2, MGLC_BF16 = 3, MGLC_FX64 = 4,
+       MGLC_FP16S = 5, MGLC_BF16S = 6 };
 
 enum { MGLC_KIND_LID = 1, MGLC_KIND_THERMAL = 2, MGLC_KIND_PARTICLE = 3, MGLC_KIND_PARTICLE2D = 4 };
 
@@ -259,7 +265,7 @@ typedef struct mglc_server mglc_server;
 typedef struct mglc_server_params {
     long long hbm_budget_bytes; /* device arena for resident solves */
     int max_active;             /* solve slots (<= 256) */
-    int precision;              /* MGLC_FP16, MGLC_BF16 or MGLC_FP32 storage of f */
+    int precision;              /* MGLC_FP16, MGLC_BF16, MGLC_FP16S, MGLC_BF16S or MGLC_FP32 storage of f */
     int steps_per_iteration;    /* K (even): steps between admission/retirement points */
     double tol;                 /* convergence threshold of max|du|/U */
     long long max_steps;        /* step cap of one solve */

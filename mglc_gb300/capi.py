@@ -15,7 +15,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libmglc_gb300.so")
 MGLC_OK = 0
 ERRORS = {1: "MGLC_ERR_INVALID", 2: "MGLC_ERR_CUDA", 3: "MGLC_ERR_NOMEM", 4: "MGLC_ERR_STATE",
           5: "MGLC_ERR_NUMERIC", 6: "MGLC_ERR_UNSUPPORTED", 7: "MGLC_ERR_PARTICLE"}
-FORMS = {"fp64": 0, "fp32": 1, "fp16": 2, "bf16": 3, "fx64": 4}
+FORMS = {"fp64": 0, "fp32": 1, "fp16": 2, "bf16": 3, "fx64": 4, "fp16s": 5, "bf16s": 6}
 KIND_LID, KIND_THERMAL, KIND_PARTICLE = 1, 2, 3
 
 _D, _I, _LL = ctypes.c_double, ctypes.c_int, ctypes.c_longlong

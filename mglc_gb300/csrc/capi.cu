@@ -25,6 +25,7 @@ struct mglc_ctx {
     int kind = 0, form = FORM_FP64;
     bool fx64 = false;  // MGLC_FX64: FP64 storage (form FP64), Q55 fixed-point lid collision
     P2Ctx* p2d = nullptr;  // MGLC_KIND_PARTICLE2D: the D2Q9 case4 state
+    bool sr = false;       // MGLC_FP16S / MGLC_BF16S: stochastic rounding of the 16-bit stores
     Geom geom{};
     long long n = 0;
     cudaStream_t stream = nullptr;
@@ -111,6 +112,9 @@ void release(mglc_ctx* c) {
 }
 
 bool valid_form(int f) { return f >= FORM_FP64 && f <= FORM_BF16; }
+// MGLC_FP16S / MGLC_BF16S: the 16-bit storage forms with stochastic rounding
+bool sr_form(int f) { return f == MGLC_FP16S || f == MGLC_BF16S; }
+int storage_of(int f) { return f == MGLC_FP16S ? FORM_FP16 : (f == MGLC_BF16S ? FORM_BF16 : f); }
 
 // FP16 deviations are scaled so that typical |f - w rho0| (1e-5 .. 1e-1)
 // stays in the normal FP16 range
@@ -249,7 +253,7 @@ int mglc_lid_create(const mglc_lid_params* p, mglc_ctx** out) {
     *out = nullptr;
     mglc_ctx* c = new mglc_ctx();
     int rc = check_geom(c, p->total_nx, p->total_ny, p->total_nz);
-    if (!rc && !valid_form(p->precision) && p->precision != MGLC_FX64)
+    if (!rc && !valid_form(p->precision) && p->precision != MGLC_FX64 && !sr_form(p->precision))
         rc = fail(c, MGLC_ERR_INVALID, "unknown precision %d", p->precision);
     if (!rc && !(p->reynolds > 0.0)) rc = fail(c, MGLC_ERR_INVALID, "reynolds must be positive");
     if (rc) {
@@ -258,7 +262,8 @@ int mglc_lid_create(const mglc_lid_params* p, mglc_ctx** out) {
     }
     c->kind = MGLC_KIND_LID;
     c->fx64 = p->precision == MGLC_FX64;
-    c->form = c->fx64 ? FORM_FP64 : p->precision;
+    c->sr = sr_form(p->precision);
+    c->form = c->fx64 ? FORM_FP64 : storage_of(p->precision);
     c->geom = {p->total_nx, p->total_ny, p->total_nz,
                (long long)p->total_nx * p->total_ny * p->total_nz};
     c->n = c->geom.plane;
@@ -288,7 +293,8 @@ int mglc_thermal_create(const mglc_thermal_params* p, mglc_ctx** out) {
     int rc = check_geom(c, p->total_nx, p->total_ny, p->total_nz);
     if (!rc && p->precision == MGLC_FX64)
         rc = fail(c, MGLC_ERR_UNSUPPORTED, "MGLC_FX64 is implemented for the lid-driven cavity only");
-    if (!rc && !valid_form(p->precision)) rc = fail(c, MGLC_ERR_INVALID, "unknown precision %d", p->precision);
+    if (!rc && !valid_form(p->precision) && !sr_form(p->precision))
+        rc = fail(c, MGLC_ERR_INVALID, "unknown precision %d", p->precision);
     if (!rc && !(p->rayleigh > 0.0 && p->prandtl > 0.0 && p->mach > 0.0))
         rc = fail(c, MGLC_ERR_INVALID, "rayleigh, prandtl and mach must be positive");
     if (rc) {
@@ -296,7 +302,8 @@ int mglc_thermal_create(const mglc_thermal_params* p, mglc_ctx** out) {
         return rc;
     }
     c->kind = MGLC_KIND_THERMAL;
-    c->form = p->precision;
+    c->sr = sr_form(p->precision);
+    c->form = storage_of(p->precision);
     c->geom = {p->total_nx, p->total_ny, p->total_nz,
                (long long)p->total_nx * p->total_ny * p->total_nz};
     c->n = c->geom.plane;
@@ -358,7 +365,8 @@ int mglc_get_info(const mglc_ctx* c, mglc_info* o) {
     if (!c || !o) return MGLC_ERR_INVALID;
     std::memset(o, 0, sizeof *o);
     o->kind = c->kind;
-    o->precision = c->fx64 ? MGLC_FX64 : c->form;
+    o->precision = c->fx64 ? MGLC_FX64
+                 : c->sr ? (c->form == FORM_FP16 ? MGLC_FP16S : MGLC_BF16S) : c->form;
     o->nx = c->geom.nx;
     o->ny = c->geom.ny;
     o->nz = c->geom.nz;
@@ -555,6 +563,8 @@ int mglc_step(mglc_ctx* c, int nsteps) {
             a.rho0 = c->rho0;
             a.scale = c->scale;
             a.inv_scale = c->inv_scale;
+            a.seed = (unsigned)c->itc;
+            a.sr = c->sr ? 1 : 0;
             a.rho = c->rho; a.u = c->u; a.v = c->v; a.w = c->w;
             e = launch_lid_step(c->fx64 ? FORM_FX64 : c->form, c->first_pending, c->f[c->cur],
                                 c->f[nxt], a, c->stream);
@@ -567,6 +577,8 @@ int mglc_step(mglc_ctx* c, int nsteps) {
             a.t_hot = c->t_hot; a.t_cold = c->t_cold; a.rho0 = c->rho0;
             a.bc_y = c->bc_y; a.bc_z = c->bc_z;
             a.scale = c->scale; a.inv_scale = c->inv_scale;
+            a.seed = (unsigned)c->itc;
+            a.sr = c->sr ? 1 : 0;
             a.rho = c->rho; a.u = c->u; a.v = c->v; a.w = c->w; a.T = c->T;
             e = launch_thermal_step(c->form, c->first_pending, c->f[c->cur], c->f[nxt], c->g[c->cur],
                                     c->g[nxt], c->F, a, c->stream);

@@ -36,7 +36,8 @@ __device__ __forceinline__ int next_tile_warp(unsigned* counter) {
 // lid tiles: [0, lid_tiles); heated tiles: [lid_tiles, total_tiles)
 template <typename S, bool THERMAL>
 __global__ void __launch_bounds__(256, THERMAL ? 2 : 3)
-    k_serve_step(const ServeTable* __restrict__ tab, int parity, unsigned* counter) {
+    k_serve_step(const ServeTable* __restrict__ tab, int kstep, unsigned* counter) {
+    const int parity = kstep & 1;
     const int base = THERMAL ? tab->lid_tiles : 0;
     const int ntiles = (THERMAL ? tab->total_tiles : tab->lid_tiles) - base;
     const int R = tab->rows_per_tile;
@@ -57,12 +58,12 @@ __global__ void __launch_bounds__(256, THERMAL ? 2 : 3)
             const int j = r % ny, k = r / ny;
             if (!THERMAL)
                 lid_cell<S, false, unsigned>(i, j, k, fin, fout, sv.K, sv.plane, nullptr, nullptr,
-                                             nullptr, nullptr);
+                                             nullptr, nullptr, sv.step0 + (unsigned)kstep);
             else
                 thermal_cell<S, false, false, unsigned>(i, j, k, fin, fout, sv.g[parity],
                                                         sv.g[parity ^ 1], sv.F, sv.K, sv.plane,
                                                         nullptr, nullptr, nullptr, nullptr,
-                                                        nullptr, 0u);
+                                                        nullptr, 0u, sv.step0 + (unsigned)kstep);
         }
     }
 }
@@ -160,27 +161,33 @@ __global__ void k_serve_fields(ServeSolve sv, float* out) {
 }
 
 template <typename S>
-static void serve_go(int thermal, const ServeTable* tab, int parity, unsigned* counter, int grid,
+static void serve_go(int thermal, const ServeTable* tab, int k, unsigned* counter, int grid,
                      int block, cudaStream_t st) {
-    if (thermal) k_serve_step<S, true><<<grid, block, 0, st>>>(tab, parity, counter);
-    else k_serve_step<S, false><<<grid, block, 0, st>>>(tab, parity, counter);
+    if (thermal) k_serve_step<S, true><<<grid, block, 0, st>>>(tab, k, counter);
+    else k_serve_step<S, false><<<grid, block, 0, st>>>(tab, k, counter);
 }
 
-cudaError_t launch_serve_step(int form, int thermal, const ServeTable* tab, int parity,
+cudaError_t launch_serve_step(int form, int thermal, const ServeTable* tab, int k,
                               unsigned* counter, int grid, int block, cudaStream_t st) {
-    if (form == FORM_FP16) serve_go<__half>(thermal, tab, parity, counter, grid, block, st);
-    else if (form == FORM_FP32) serve_go<float>(thermal, tab, parity, counter, grid, block, st);
-    else if (form == FORM_BF16) serve_go<__nv_bfloat16>(thermal, tab, parity, counter, grid, block, st);
+    if (form == FORM_FP16) serve_go<__half>(thermal, tab, k, counter, grid, block, st);
+    else if (form == FORM_FP32) serve_go<float>(thermal, tab, k, counter, grid, block, st);
+    else if (form == FORM_BF16) serve_go<__nv_bfloat16>(thermal, tab, k, counter, grid, block, st);
     else return cudaErrorInvalidValue;
     return cudaGetLastError();
 }
 
-cudaError_t launch_serve_resid(int form, const ServeTable* tab, unsigned* counter,
-                               unsigned* resid, int grid, int block, cudaStream_t st) {
+// step0 += steps for every active solve (after the iteration's steps)
+__global__ void k_serve_advance(ServeTable* tab, int steps) {
+    for (int s = threadIdx.x; s < tab->n_active; s += blockDim.x) tab->s[s].step0 += (unsigned)steps;
+}
+
+cudaError_t launch_serve_resid(int form, ServeTable* tab, unsigned* counter, unsigned* resid,
+                               int steps, int grid, int block, cudaStream_t st) {
     if (form == FORM_FP16) k_serve_resid<__half><<<grid, block, 0, st>>>(tab, counter, resid);
     else if (form == FORM_FP32) k_serve_resid<float><<<grid, block, 0, st>>>(tab, counter, resid);
     else if (form == FORM_BF16) k_serve_resid<__nv_bfloat16><<<grid, block, 0, st>>>(tab, counter, resid);
     else return cudaErrorInvalidValue;
+    k_serve_advance<<<1, 256, 0, st>>>(tab, steps);
     return cudaGetLastError();
 }
 

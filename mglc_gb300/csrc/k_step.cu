@@ -25,7 +25,7 @@ __global__ void __launch_bounds__(128)
                const double* __restrict__ mv, const double* __restrict__ mw) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= K.nx) return;
-    lid_cell<S, FIRST, IDX>(i, blockIdx.y, blockIdx.z, fin, fout, K, P, mrho, mu, mv, mw);
+    lid_cell<S, FIRST, IDX>(i, blockIdx.y, blockIdx.z, fin, fout, K, P, mrho, mu, mv, mw, K.seed);
 }
 
 template <bool FIRST, typename IDX>
@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(128)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= K.nx) return;
     thermal_cell<S, FIRST, ROT, IDX>(i, blockIdx.y, blockIdx.z, fin, fout, gin, gout, F, K, P,
-                                     mrho, mu, mv, mw, mT, (IDX)2 * P);
+                                     mrho, mu, mv, mw, mT, (IDX)2 * P, K.seed);
 }
 
 // --------------------------------------------------------------- launch --
@@ -67,6 +67,8 @@ static cudaError_t lid_go(bool first, const void* fin, void* fout, const LidStep
                           cudaStream_t s) {
     using C = typename St<S>::C;
     StepK<C> K = make_k<C>(a.g, a.cd, a.u0, a.rho0, a.scale, a.inv_scale);
+    K.seed = a.seed;
+    K.sr = a.sr;
     dim3 b = step_block(a.g.nx), gr = step_grid(a.g, b);
     const bool small = (long long)Q19 * a.g.plane < (1ll << 31);
 #define LID_LAUNCH(FI, IT)                                                                    \
@@ -118,6 +120,8 @@ static cudaError_t th_go(bool first, const void* fin, void* fout, const void* gi
                          void* F, const ThermalStepArgs& a, cudaStream_t s) {
     using C = typename St<S>::C;
     StepK<C> K = make_k<C>(a.g, a.cd, 0.0, a.rho0, a.scale, a.inv_scale);
+    K.seed = a.seed;
+    K.sr = a.sr;
     K.gbeta = (C)a.gbeta; K.omega_rot = (C)a.omega_rot; K.t_ref = (C)a.t_ref;
     K.para_a = (C)a.para_a; K.qd = (C)a.qd; K.qnu = (C)a.qnu;
     K.chot = (C)((6.0 + a.para_a) / 21.0 * a.t_hot);

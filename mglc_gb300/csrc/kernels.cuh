@@ -26,6 +26,8 @@ struct LidStepArgs {
     MrtCoef<double> cd;
     double u0, rho0;
     float scale, inv_scale;  // deviation storage scale (FP16); 1 otherwise
+    unsigned seed;           // step index: stochastic rounding of 16-bit stores
+    int sr;                  // 1: stochastic rounding of 16-bit stores
     // macroscopic fields used by the first step after initial()/load (the
     // reference's collision reads the stored rho,u,v,w)
     const double *rho, *u, *v, *w;
@@ -37,6 +39,8 @@ struct ThermalStepArgs {
     double gbeta, omega_rot, t_ref, para_a, qd, qnu, t_hot, t_cold, rho0;
     int bc_y, bc_z;
     float scale, inv_scale;
+    unsigned seed;  // step index: stochastic rounding of 16-bit stores
+    int sr;         // 1: stochastic rounding of 16-bit stores
     const double *rho, *u, *v, *w, *T;
 };
 

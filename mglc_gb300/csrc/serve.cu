@@ -116,6 +116,7 @@ struct mglc_server {
     size_t fields_bytes = 0;
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t done = nullptr;
+    bool sr = false;  // stochastic rounding of the 16-bit stores
     cudaStream_t side = nullptr;        // heated-solve branch of the captured step
     cudaEvent_t fork = nullptr, join = nullptr;
     int block = 256, rows = 2, ctas_per_sm = 4, nsm = 152;
@@ -166,6 +167,7 @@ void fill_solve(const mglc_server* s, const mglc_request& r, ServeSolve* sv) {
     K.nx = K.ny = K.nz = n;
     K.rho0 = 1.0f;
     const bool fp16 = s->p.precision == MGLC_FP16;
+    K.sr = s->sr ? 1 : 0;
     K.scale = fp16 ? 256.0f : 1.0f;
     K.inv_scale = fp16 ? 1.0f / 256.0f : 1.0f;
     if (r.kind == MGLC_KIND_LID) {
@@ -232,6 +234,7 @@ int upload_table(mglc_server* s) {
         q.slot = a;
         q.sv.tile0 = tile;
         q.sv.ntiles = tiles_of(s, q.sv);
+        q.sv.step0 = (unsigned)q.steps;  // the device copy advances by K per iteration too
         tile += q.sv.ntiles;
         if (q.r.kind == MGLC_KIND_LID) t->lid_tiles = tile;
         t->s[a] = q.sv;
@@ -259,14 +262,15 @@ int build_graph(mglc_server* s) {
         e = cudaEventRecord(s->fork, s->stream);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(s->side, s->fork, 0);
         if (e == cudaSuccess)
-            e = launch_serve_step(s->p.precision, 1, s->tab_dev, k & 1, s->counters + K + k, grid, s->block, s->side);
+            e = launch_serve_step(s->p.precision, 1, s->tab_dev, k, s->counters + K + k, grid, s->block, s->side);
         if (e == cudaSuccess)
-            e = launch_serve_step(s->p.precision, 0, s->tab_dev, k & 1, s->counters + k, grid, s->block, s->stream);
+            e = launch_serve_step(s->p.precision, 0, s->tab_dev, k, s->counters + k, grid, s->block, s->stream);
         if (e == cudaSuccess) e = cudaEventRecord(s->join, s->side);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(s->stream, s->join, 0);
     }
     if (e == cudaSuccess)
-        e = launch_serve_resid(s->p.precision, s->tab_dev, s->counters + 2 * K, s->resid_dev, grid, s->block, s->stream);
+        e = launch_serve_resid(s->p.precision, s->tab_dev, s->counters + 2 * K, s->resid_dev, K, grid,
+                               s->block, s->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(s->resid_host, s->resid_dev, sizeof(unsigned) * SERVE_MAX_ACTIVE,
                             cudaMemcpyDeviceToHost, s->stream);
@@ -335,8 +339,8 @@ int autotune(mglc_server* s) {
                 launch_serve_step(s->p.precision, 1, s->tab_dev, 0, s->counters + 5, grid, blk, s->stream);
                 cudaEventRecord(a, s->stream);
                 for (int k = 0; k < 4; k++) {
-                    launch_serve_step(s->p.precision, 0, s->tab_dev, (k + 1) & 1, s->counters + 1 + k, grid, blk, s->stream);
-                    launch_serve_step(s->p.precision, 1, s->tab_dev, (k + 1) & 1, s->counters + 6 + k, grid, blk, s->stream);
+                    launch_serve_step(s->p.precision, 0, s->tab_dev, k + 1, s->counters + 1 + k, grid, blk, s->stream);
+                    launch_serve_step(s->p.precision, 1, s->tab_dev, k + 1, s->counters + 6 + k, grid, blk, s->stream);
                 }
                 cudaEventRecord(b, s->stream);
                 cudaEventSynchronize(b);
@@ -393,8 +397,14 @@ int mglc_server_create(const mglc_server_params* p, mglc_server** out) {
     mglc_server* s = new mglc_server();
     *out = s;
     s->p = *p;
-    if (p->precision != MGLC_FP16 && p->precision != MGLC_FP32 && p->precision != MGLC_BF16)
+    if (p->precision != MGLC_FP16 && p->precision != MGLC_FP32 && p->precision != MGLC_BF16 &&
+        p->precision != MGLC_FP16S && p->precision != MGLC_BF16S)
         return sfail(s, MGLC_ERR_INVALID, "the server stores populations as FP16, BF16 or FP32");
+    // FP16S / BF16S: 16-bit storage with stochastic rounding; from here on the
+    // precision field holds the storage form
+    s->sr = p->precision == MGLC_FP16S || p->precision == MGLC_BF16S;
+    if (p->precision == MGLC_FP16S) s->p.precision = MGLC_FP16;
+    if (p->precision == MGLC_BF16S) s->p.precision = MGLC_BF16;
     if (p->steps_per_iteration < 2 || p->steps_per_iteration % 2)
         return sfail(s, MGLC_ERR_INVALID, "steps_per_iteration must be even and >= 2");
     if (p->max_active < 1) return sfail(s, MGLC_ERR_INVALID, "max_active must be >= 1");

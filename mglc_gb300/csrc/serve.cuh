@@ -22,6 +22,7 @@ struct ServeSolve {
     float* F;      // F_z (no rotation in served solves)
     float* uprev;  // 3 planes: velocity at the previous residual check
     float uref;    // velocity scale of the residual
+    unsigned step0;  // steps taken before this iteration (stochastic-rounding seed base)
     StepK<float> K;
 };
 
@@ -35,13 +36,15 @@ struct ServeTable {
     ServeSolve s[SERVE_MAX_ACTIVE];
 };
 
-// One time step of every active solve of one kind (parity selects the
-// ping-pong buffer); thermal = 0 runs the lid tiles, 1 the heated ones.
-cudaError_t launch_serve_step(int form, int thermal, const ServeTable* tab, int parity,
+// Time step k of the iteration for every active solve of one kind (k & 1
+// selects the ping-pong buffer, step0 + k seeds the stochastic rounding);
+// thermal = 0 runs the lid tiles, 1 the heated ones.
+cudaError_t launch_serve_step(int form, int thermal, const ServeTable* tab, int k,
                               unsigned* counter, int grid, int block, cudaStream_t st);
-// resid[s] = max over cells of |u - uprev| / uref (as float bits); uprev <- u
-cudaError_t launch_serve_resid(int form, const ServeTable* tab, unsigned* counter,
-                               unsigned* resid, int grid, int block, cudaStream_t st);
+// resid[s] = max over cells of |u - uprev| / uref (as float bits); uprev <- u;
+// then every solve's step0 advances by steps (the iteration's step count)
+cudaError_t launch_serve_resid(int form, ServeTable* tab, unsigned* counter, unsigned* resid,
+                               int steps, int grid, int block, cudaStream_t st);
 // equilibrium state of one solve (rho = 1, u = 0; wall temperatures)
 cudaError_t launch_serve_init(int form, const ServeSolve& s, double t_hot, double t_cold,
                               cudaStream_t st);

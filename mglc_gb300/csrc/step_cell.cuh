@@ -19,6 +19,7 @@ struct St<double> {
     static constexpr bool SHIFT = false;
     __device__ static C ld(const double* p, float) { return __ldg(p); }
     __device__ static double raw(const double* p) { return __ldg(p); }
+    __device__ static void st_sr(double* p, C v, float, unsigned) { *p = v; }
     __device__ static C cvt(double v, float) { return v; }
     __device__ static void st(double* p, C v, float) { *p = v; }
 };
@@ -28,6 +29,7 @@ struct St<float> {
     static constexpr bool SHIFT = true;
     __device__ static C ld(const float* p, float) { return __ldg(p); }
     __device__ static float raw(const float* p) { return __ldg(p); }
+    __device__ static void st_sr(float* p, C v, float, unsigned) { *p = v; }
     __device__ static C cvt(float v, float) { return v; }
     __device__ static void st(float* p, C v, float) { *p = v; }
 };
@@ -37,6 +39,12 @@ struct St<__half> {
     static constexpr bool SHIFT = true;
     __device__ static C ld(const __half* p, float inv) { return __half2float(__ldg(p)) * inv; }
     __device__ static __half raw(const __half* p) { return __ldg(p); }
+    // stochastic rounding: 13 uniform bits added below the 10 kept mantissa
+    // bits, then truncation (unbiased; rounding errors do not correlate from
+    // step to step, so they do not accumulate into a drift)
+    __device__ static void st_sr(__half* p, C v, float sc, unsigned r) {
+        *p = __float2half_rz(__uint_as_float(__float_as_uint(v * sc) + (r >> 19)));
+    }
     __device__ static C cvt(__half v, float inv) { return __half2float(v) * inv; }
     __device__ static void st(__half* p, C v, float sc) { *p = __float2half_rn(v * sc); }
 };
@@ -48,6 +56,9 @@ struct St<__nv_bfloat16> {
         return __bfloat162float(__ldg(p)) * inv;
     }
     __device__ static __nv_bfloat16 raw(const __nv_bfloat16* p) { return __ldg(p); }
+    __device__ static void st_sr(__nv_bfloat16* p, C v, float sc, unsigned r) {
+        *p = __float2bfloat16_rz(__uint_as_float(__float_as_uint(v * sc) + (r >> 16)));
+    }
     __device__ static C cvt(__nv_bfloat16 v, float inv) { return __bfloat162float(v) * inv; }
     __device__ static void st(__nv_bfloat16* p, C v, float sc) { *p = __float2bfloat16_rn(v * sc); }
 };
@@ -72,6 +83,8 @@ struct StepK {
     int nx, ny, nz;
     C u0, rho0;
     float scale, inv_scale;
+    unsigned seed;  // one-solve kernels: the step index (stochastic rounding)
+    int sr;         // 1: 16-bit stores round stochastically, 0: to nearest
     MrtCoef<C> c;
     // thermal
     C gbeta, omega_rot, t_ref, para_a, qd, qnu, chot, ccold;
@@ -101,6 +114,24 @@ __host__ __device__ constexpr unsigned leave_bits(int dx, int dy, int dz) {
            (dz < 0 ? 16u : 0u) | (dz > 0 ? 32u : 0u);
 }
 
+// Uniform bits for the stochastic rounding of 16-bit stores: one integer
+// hash (lowbias32 finaliser) of (cell, step) per cell, then the high bits of
+// its product with a distinct odd constant per population.
+__device__ __forceinline__ unsigned sr_hash(unsigned x) {
+    x ^= x >> 16;
+    x *= 0x7FEB352Du;
+    x ^= x >> 15;
+    x *= 0x846CA68Bu;
+    x ^= x >> 16;
+    return x;
+}
+__device__ __forceinline__ unsigned sr_cell(unsigned cell, unsigned step) {
+    return sr_hash(cell * 0x9E3779B1u ^ sr_hash(step + 0x632BE5ABu));
+}
+__device__ __forceinline__ unsigned sr_pop(unsigned h, int q) {
+    return h * (0x2545F491u + 2u * 0x9E3779B9u * (unsigned)q);
+}
+
 // ------------------------------------------------------------ lid kernel --
 // IDX: 32-bit element indices when Q*cells < 2^31, 64-bit otherwise.
 // lid_cell_from: collide and push one cell whose 19 stored populations are
@@ -112,7 +143,7 @@ __device__ __forceinline__ void lid_cell_from(int i, int j, int k, const S (&raw
                                               const double* __restrict__ mrho,
                                               const double* __restrict__ mu,
                                               const double* __restrict__ mv,
-                                              const double* __restrict__ mw) {
+                                              const double* __restrict__ mw, unsigned seed) {
     using C = typename St<S>::C;
     const int nx = K.nx, ny = K.ny, nz = K.nz;
     const IDX cell = (IDX)i + (IDX)nx * ((IDX)j + (IDX)ny * (IDX)k);
@@ -138,12 +169,16 @@ __device__ __forceinline__ void lid_cell_from(int i, int j, int k, const S (&raw
     mrt_collide<C, false, true>(f, rho_m, rho, ux, uy, uz, C(0), C(0), C(0), K.c);
     const IDX sy = (IDX)nx, sz = (IDX)nx * (IDX)ny;
     const unsigned bm = face_mask(i, j, k, nx, ny, nz);
+    const unsigned h0 = sr_cell((unsigned)cell, seed);
+    auto put = [&](S* p, C v, int q) {
+        if (K.sr) St<S>::st_sr(p, v, K.scale, sr_pop(h0, q));
+        else St<S>::st(p, v, K.scale);
+    };
     if (bm == 0) {  // interior cell: every population streams
 #pragma unroll
         for (int q = 0; q < Q19; q++) {
             const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
-            St<S>::st(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), f[q],
-                      K.scale);
+            put(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), f[q], q);
         }
         return;
     }
@@ -155,12 +190,11 @@ __device__ __forceinline__ void lid_cell_from(int i, int j, int k, const S (&raw
     for (int q = 0; q < Q19; q++) {
         const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
         if ((bm & leave_bits(dx, dy, dz)) == 0) {
-            St<S>::st(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), f[q],
-                      K.scale);
+            put(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), f[q], q);
         } else {
             C val = f[q];
             if (dz > 0 && dx != 0) val = val - C(dx) * lid;
-            St<S>::st(fout + ((IDX)opp19(q) * P + cell), val, K.scale);
+            put(fout + ((IDX)opp19(q) * P + cell), val, q);
         }
     }
 }
@@ -179,10 +213,10 @@ __device__ __forceinline__ void lid_cell(int i, int j, int k, const S* __restric
                                          IDX P, const double* __restrict__ mrho,
                                          const double* __restrict__ mu,
                                          const double* __restrict__ mv,
-                                         const double* __restrict__ mw) {
+                                         const double* __restrict__ mw, unsigned seed) {
     S raw[Q19];  // every load is issued before the first conversion
     lid_load<S, IDX>(i, j, k, fin, K.nx, K.ny, P, raw);
-    lid_cell_from<S, FIRST, IDX>(i, j, k, raw, fout, K, P, mrho, mu, mv, mw);
+    lid_cell_from<S, FIRST, IDX>(i, j, k, raw, fout, K, P, mrho, mu, mv, mw, seed);
 }
 
 // ------------------------------------------------------ lid kernel, FX64 --
@@ -280,7 +314,7 @@ __device__ __forceinline__ void thermal_cell(
     const typename St<S>::C* __restrict__ gin, typename St<S>::C* __restrict__ gout,
     typename St<S>::C* __restrict__ F, const StepK<typename St<S>::C>& K, IDX P,
     const double* __restrict__ mrho, const double* __restrict__ mu, const double* __restrict__ mv,
-    const double* __restrict__ mw, const double* __restrict__ mT, IDX fz_off) {
+    const double* __restrict__ mw, const double* __restrict__ mT, IDX fz_off, unsigned seed) {
     // F holds F_x, F_y at planes 0 and 1 (rotation only) and F_z at element offset fz_off
     using C = typename St<S>::C;
     const int nx = K.nx, ny = K.ny, nz = K.nz;
@@ -330,12 +364,16 @@ __device__ __forceinline__ void thermal_cell(
 
     const IDX sy = (IDX)nx, sz = (IDX)nx * (IDX)ny;
     const unsigned bm = face_mask(i, j, k, nx, ny, nz);
+    const unsigned h0 = sr_cell((unsigned)cell, seed);
+    auto put = [&](S* p, C v, int q) {
+        if (K.sr) St<S>::st_sr(p, v, K.scale, sr_pop(h0, q));
+        else St<S>::st(p, v, K.scale);
+    };
     if (bm == 0) {
 #pragma unroll
         for (int q = 0; q < Q19; q++) {
             const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
-            St<S>::st(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), f[q],
-                      K.scale);
+            put(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), f[q], q);
         }
 #pragma unroll
         for (int q = 0; q < Q7; q++) {
@@ -348,10 +386,9 @@ __device__ __forceinline__ void thermal_cell(
     for (int q = 0; q < Q19; q++) {
         const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
         if ((bm & leave_bits(dx, dy, dz)) == 0)
-            St<S>::st(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), f[q],
-                      K.scale);
+            put(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), f[q], q);
         else
-            St<S>::st(fout + ((IDX)opp19(q) * P + cell), f[q], K.scale);
+            put(fout + ((IDX)opp19(q) * P + cell), f[q], q);
     }
     // D3Q7: adiabatic walls reflect, constant-T walls anti-bounce-back
     // g_in = -g_out + (6+paraA)/21 * T_wall (bouyancy3d_mpi.F90:1101-1210)

@@ -32,7 +32,8 @@ def lid_ref(mg):
 
 
 @pytest.mark.parametrize("form,tol,tmass", [("fp32", 1e-6, 1e-6), ("fp16", 1e-3, 1e-4),
-                                            ("bf16", 5e-2, 1e-3)])
+                                            ("bf16", 5e-2, 1e-3), ("fp16s", 4e-4, 1e-5),
+                                            ("bf16s", 4e-3, 1e-4)])
 def test_lid_forms_velocity_error(mg, lid_ref, form, tol, tmass):
     with mg.LidDrivenCavity(64, reynolds=400.0, u0=0.1, top_layer_u0=False, precision=form) as c:
         c.initial()
@@ -53,7 +54,8 @@ def th_ref(mg):
 
 
 @pytest.mark.parametrize("form,tu,tt,tnu", [("fp32", 1e-5, 1e-5, 1e-5), ("fp16", 1.5e-3, 1e-3, 1e-3),
-                                            ("bf16", 0.2, 0.05, 0.05)])
+                                            ("bf16", 0.2, 0.05, 0.05), ("fp16s", 1e-3, 1e-4, 1e-4),
+                                            ("bf16s", 1e-2, 1e-3, 1e-3)])
 def test_thermal_forms_error(mg, th_ref, form, tu, tt, tnu):
     with mg.BuoyancyCavity(48, rayleigh=1e5, t_hot=0.5, t_cold=-0.5, precision=form) as c:
         c.initial()

@@ -62,6 +62,28 @@ def test_lid_request_equals_one_solve_context(mg):
     np.testing.assert_allclose(fld[3], w, rtol=0, atol=1e-7)
 
 
+@pytest.mark.parametrize("kind", ["lid", "thermal"])
+def test_stochastic_rounding_request_matches_one_solve_context(mg, kind):
+    """FP16S: the rounding bits come from (cell, step), so a served solve
+    stays identical to a one-solve context, in the mix and across iterations."""
+    n, steps = 32, 400
+    with _server(mg, max_steps=steps, precision="fp16s") as srv:
+        other = srv.submit("thermal" if kind == "lid" else "lid", 24, reynolds=200.0, rayleigh=1e4)
+        rid = srv.submit(kind, n, reynolds=300.0, rayleigh=1e4)
+        srv.run()
+        fld = srv.field(rid)
+    if kind == "lid":
+        c = mg.LidDrivenCavity(n, reynolds=300.0, u0=0.1, top_layer_u0=False, precision="fp16s")
+    else:
+        c = mg.BuoyancyCavity(n, rayleigh=1e4, prandtl=0.71, mach=0.1, t_hot=0.5, t_cold=-0.5,
+                              precision="fp16s")
+    with c:
+        c.initial()
+        c.step(steps)
+        u = c.macro()[1]
+    np.testing.assert_allclose(fld[1], u, rtol=0, atol=1e-7)
+
+
 def test_thermal_request_matches_one_solve_context(mg):
     n, steps = 32, 400
     with _server(mg, max_steps=steps) as srv:
