@@ -136,11 +136,15 @@ __global__ void __launch_bounds__(128, (sizeof(S) == 4 ? 6 : 4))
     C cacc[2] = {C(0), C(0)};  // per-cell sums in the arithmetic type, widened per warp
     const bool active = i < nx;
     const IDX cell = (IDX)i + (IDX)nx * ((IDX)j + (IDX)ny * k);
-    const bool fluid = active && owner[cell] < 0;
-    if (fluid) {
-        C f[Q19];
+    // the populations are loaded before the mask answers (solid cells read
+    // in-bounds values they do not use), so both loads are in flight together
+    C f[Q19];
+    if (active) {
 #pragma unroll
-        for (int q = 0; q < Q19; q++) f[q] = (C)fin[q * P + cell];
+        for (int q = 0; q < Q19; q++) f[q] = (C)__ldg(fin + (q * P + cell));
+    }
+    const bool fluid = active && __ldg(owner + cell) < 0;
+    if (fluid) {
         const C rho0 = bk.rho0, ax = bk.ax, ay = bk.ay, az = bk.az;
         C rho_m, rho, ux, uy, uz;
         if (FIRST) {  // the reference's initial fields: rho0, u = 0
@@ -313,6 +317,10 @@ constexpr bool opp_rt_ok() {
 }
 static_assert(opp_rt_ok(), "opp_rt must match opp19");
 
+// largest owner tile k_plinks stages in dynamic shared memory (beside its
+// ~38 KB of static shared memory); bigger spheres read the mask from global
+constexpr size_t TILE_MAX_BYTES = 160 * 1024;
+
 // Link-list capacity of k_plinks: one scan round adds at most PB * 18 links,
 // so the list is processed as soon as fewer than that many slots are free.
 constexpr int LINK_CAP = PB * 27;
@@ -340,7 +348,10 @@ __device__ __forceinline__ bool node_avail(int i, int j, int k, const PartParams
 // because r = o + q e gives r x e = o x e, and o = n - X with n the node's
 // (unwrapped) coordinates.  The variable parts use the population arithmetic
 // type; q (calQ2) is computed in FP64 in both forms.
-template <typename S>
+// TILE: the owner ids of the slab's box plus a one-node halo are staged in
+// dynamic shared memory (walls and, without periodicity, the x faces as -2),
+// so the scan's 19 lookups per node stay on chip.
+template <typename S, bool TILE>
 __global__ void __launch_bounds__(PB) k_plinks(S* __restrict__ f, PartParams p, PartDev d) {
     using L = typename PC<S>::C;
     if (d.status[0]) return;
@@ -369,6 +380,24 @@ __global__ void __launch_bounds__(PB) k_plinks(S* __restrict__ f, PartParams p, 
     __shared__ unsigned char s_dir[LINK_CAP];
     __shared__ int s_n;
     __shared__ int s_wsum[PB / 32];
+    extern __shared__ int s_own[];
+    const int TX = bw + 2, TY = bw + 2, TZ = kz1 - kz0 + 2;
+    if (TILE) {
+        for (int e = threadIdx.x; e < TX * TY * TZ; e += PB) {
+            const int ti = e % TX, tj = (e / TX) % TY, tk = e / (TX * TY);
+            int i = ci - h + ti - 1;
+            const int j = cj - h + tj - 1, k = ck - h + kz0 + tk - 1;
+            int o = -2;
+            if (j >= 0 && j < ny && k >= 0 && k < nz) {
+                if (p.periodic_x) i = i < 0 ? i + nx : (i >= nx ? i - nx : i);
+                if (i >= 0 && i < nx) o = d.owner_cur[i + (long long)nx * (j + (long long)ny * k)];
+            }
+            s_own[e] = o;
+        }
+    }
+    auto own_at = [&](int bi, int bj, int bk) {  // box coordinates, bk absolute in the box
+        return s_own[(bi + 1) + TX * ((bj + 1) + TY * (bk - kz0 + 1))];
+    };
     if (threadIdx.x == 0) s_n = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -389,7 +418,13 @@ __global__ void __launch_bounds__(PB) k_plinks(S* __restrict__ f, PartParams p, 
                 if (p.periodic_x) i = wrapx(i, nx);
                 else ok = i >= 0 && i < nx;
             }
-            if (ok && d.owner_cur[i + (long long)nx * (j + (long long)ny * k)] < 0) {
+            if (TILE) {
+                if (ok && own_at(bi, bj, bk) < 0) {
+#pragma unroll
+                    for (int a = 1; a < Q19; a++)
+                        if (own_at(bi + ex19(a), bj + ey19(a), bk + ez19(a)) == c) my_dirs |= 1u << a;
+                }
+            } else if (ok && d.owner_cur[i + (long long)nx * (j + (long long)ny * k)] < 0) {
                 for (int a = 1; a < Q19; a++) {
                     const int jn = j + ey19(a), kn = k + ez19(a);
                     if (jn < 0 || jn >= ny || kn < 0 || kn >= nz) continue;
@@ -956,7 +991,19 @@ static cudaError_t pstep_go(bool first, const void* fin, void* fout, const PartP
     k_pfinish<<<FINISH_BLOCKS, 256, 0, s>>>(d, d.nblocks);
     k_pfinish2<<<1, 32, 0, s>>>(d, d.nblocks);
     if (p.np > 0) {
-        k_plinks<S><<<dim3(p.np, NSLAB), PB, 0, s>>>((S*)fout, p, d);
+        const int bw = 2 * ((int)ceil(p.radius) + 2) + 2;
+        const size_t tile = sizeof(int) * (size_t)(bw + 2) * (bw + 2) * ((bw + NSLAB - 1) / NSLAB + 2);
+        if (tile <= TILE_MAX_BYTES) {
+            static bool attr_set[2] = {false, false};  // per storage type
+            if (!attr_set[sizeof(S) == 4]) {
+                cudaFuncSetAttribute(k_plinks<S, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)TILE_MAX_BYTES);
+                attr_set[sizeof(S) == 4] = true;
+            }
+            k_plinks<S, true><<<dim3(p.np, NSLAB), PB, tile, s>>>((S*)fout, p, d);
+        } else {
+            k_plinks<S, false><<<dim3(p.np, NSLAB), PB, 0, s>>>((S*)fout, p, d);
+        }
         k_pforce<<<(p.np + 7) / 8, 256, 0, s>>>(p, d);
         k_pmove<<<(p.np + 127) / 128, 128, 0, s>>>(p, d);
     }
