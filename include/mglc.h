@@ -41,9 +41,9 @@ extern "C" {
  *  FP64: FP64 storage and FP64 arithmetic -- the drop-in for the reference.
  *  FP32/FP16/BF16: populations stored as deviations f_i - w_i*rho0 in that
  *  type, FP32 arithmetic; FP64 kept for reductions (residual, totals).
- *  FX64 (lid-driven cavity only): FP64 storage; the collision runs in 64-bit
- *  fixed point with 55 fractional bits (exact moment transforms, one rounding
- *  to FP64 per stored population), everything else as FP64.
+ *  FX64 (lid-driven and heated cavities): FP64 storage; the collisions run in
+ *  64-bit fixed point with 55 fractional bits (exact moment transforms, one
+ *  rounding to FP64 per stored value), everything else as FP64.
  *  FP16S/BF16S: FP16/BF16 deviation storage written with stochastic rounding
  *  (unbiased; the storage error stays at its one-step level instead of
  *  accumulating over a transient).  The stored state then fluctuates at the

@@ -291,9 +291,7 @@ int mglc_thermal_create(const mglc_thermal_params* p, mglc_ctx** out) {
     *out = nullptr;
     mglc_ctx* c = new mglc_ctx();
     int rc = check_geom(c, p->total_nx, p->total_ny, p->total_nz);
-    if (!rc && p->precision == MGLC_FX64)
-        rc = fail(c, MGLC_ERR_UNSUPPORTED, "MGLC_FX64 is implemented for the lid-driven cavity only");
-    if (!rc && !valid_form(p->precision) && !sr_form(p->precision))
+    if (!rc && !valid_form(p->precision) && !sr_form(p->precision) && p->precision != MGLC_FX64)
         rc = fail(c, MGLC_ERR_INVALID, "unknown precision %d", p->precision);
     if (!rc && !(p->rayleigh > 0.0 && p->prandtl > 0.0 && p->mach > 0.0))
         rc = fail(c, MGLC_ERR_INVALID, "rayleigh, prandtl and mach must be positive");
@@ -303,7 +301,8 @@ int mglc_thermal_create(const mglc_thermal_params* p, mglc_ctx** out) {
     }
     c->kind = MGLC_KIND_THERMAL;
     c->sr = sr_form(p->precision);
-    c->form = storage_of(p->precision);
+    c->fx64 = p->precision == MGLC_FX64;
+    c->form = c->fx64 ? FORM_FP64 : storage_of(p->precision);
     c->geom = {p->total_nx, p->total_ny, p->total_nz,
                (long long)p->total_nx * p->total_ny * p->total_nz};
     c->n = c->geom.plane;
@@ -580,7 +579,7 @@ int mglc_step(mglc_ctx* c, int nsteps) {
             a.seed = (unsigned)c->itc;
             a.sr = c->sr ? 1 : 0;
             a.rho = c->rho; a.u = c->u; a.v = c->v; a.w = c->w; a.T = c->T;
-            e = launch_thermal_step(c->form, c->first_pending, c->f[c->cur], c->f[nxt], c->g[c->cur],
+            e = launch_thermal_step(c->fx64 ? FORM_FX64 : c->form, c->first_pending, c->f[c->cur], c->f[nxt], c->g[c->cur],
                                     c->g[nxt], c->F, a, c->stream);
         }
         if (e != cudaSuccess) return cuda_fail(c, e, "step kernel launch");

@@ -36,6 +36,12 @@ __device__ __forceinline__ bool fx_bad(double x) {
     return ((unsigned)(__double_as_longlong(x) >> 52) & 0x7FFu) >= 1023u;
 }
 
+// |x| >= 2, infinity or NaN (temperatures, which reach 1 at a hot wall, and
+// their populations)
+__device__ __forceinline__ bool fx_bad2(double x) {
+    return ((unsigned)(__double_as_longlong(x) >> 52) & 0x7FFu) >= 1024u;
+}
+
 // FP64 -> Q55 for |x| < 256: exact for |x| >= 1/8, rounded to nearest
 // (ties away from zero) below; larger inputs give unspecified values (the
 // callers replace such cells by NaN).
@@ -242,6 +248,185 @@ __device__ __forceinline__ bool mrt_collide_fx(long long* f, long long rho_in, l
     E = bz - r14; O = Y - Z + (r17 + r18);
     f[17] -= E + O; f[16] -= E - O;
     return ok;
+}
+
+
+// ------------------------------------------------------------ heated cavity --
+// Constants of the forced D3Q19 MRT and of the D3Q7 MRT (bouyancy3d_mpi.F90:
+// 641-864, 1014-1070) for the Q55 form.  Factors below 1/2 are round(c 2^64)
+// (qmulc); the others are Q55 values (qmul).
+struct FxThermalCoef {
+    FxCoef c;                                         // relaxation c_k (u0_6 unused)
+    long long h1, h2, h3, h4, h9, h10, h11, h12, h13; // (1 - s_k/2) / |M_k|^2, qmulc
+    long long gbeta;                                  // g beta, qmulc
+    long long omega2;                                 // 2 Omega (Q55)
+    long long t_ref;                                  // Q55
+    long long para_a;                                 // Q55
+    long long qd_half;                                // q_d / 2 (Q55)
+    long long qnu42, qnu12, qnu4;                     // q_nu / |N_k|^2, qmulc
+    long long chot, ccold;                            // (6 + paraA) / 21 * T_wall (Q55)
+};
+inline long long fx_q55(double x) {
+    long double v = (long double)x * (long double)FX_ONE;
+    return (long long)(v < 0 ? v - 0.5L : v + 0.5L);
+}
+inline FxThermalCoef make_fx_thermal(const MrtCoef<double>& m, double gbeta, double omega_rot,
+                                     double t_ref, double para_a, double qd, double qnu,
+                                     double t_hot, double t_cold) {
+    FxThermalCoef t;
+    t.c = make_fx_coef(m, 0.0);
+    t.h1 = fx_const(m.h1); t.h2 = fx_const(m.h2); t.h3 = fx_const(m.h3); t.h4 = fx_const(m.h4);
+    t.h9 = fx_const(m.h9); t.h10 = fx_const(m.h10); t.h11 = fx_const(m.h11);
+    t.h12 = fx_const(m.h12); t.h13 = fx_const(m.h13);
+    t.gbeta = fx_const(gbeta);
+    t.omega2 = fx_q55(2.0 * omega_rot);
+    t.t_ref = fx_q55(t_ref);
+    t.para_a = fx_q55(para_a);
+    t.qd_half = fx_q55(0.5 * qd);
+    t.qnu42 = fx_const(qnu / 42.0); t.qnu12 = fx_const(qnu / 12.0); t.qnu4 = fx_const(qnu / 4.0);
+    t.chot = fx_q55((6.0 + para_a) / 21.0 * t_hot);
+    t.ccold = fx_q55((6.0 + para_a) / 21.0 * t_cold);
+    return t;
+}
+
+// Forced MRT collision of the heated cavity on Q55 populations, in place
+// (meq(12) with rho; source (1 - s/2) S in moment space).  rho, u and the force
+// (fx, fy, fz) are given; rux = rho u (= j + F/2 when u came from the
+// populations).  Returns false when rho or u leaves the range box.
+__device__ __forceinline__ bool mrt_collide_fx_forced(long long* f, long long rho, long long ux,
+                                                      long long uy, long long uz, long long rux,
+                                                      long long ruy, long long ruz, long long fx,
+                                                      long long fy, long long fz,
+                                                      const FxThermalCoef& T) {
+    using ll = long long;
+    const FxCoef& c = T.c;
+    ll s1 = f[1] + f[2], d1 = f[1] - f[2];
+    ll s2 = f[3] + f[4], d2 = f[3] - f[4];
+    ll s3 = f[5] + f[6], d3 = f[5] - f[6];
+    ll s4 = f[7] + f[10], d4 = f[7] - f[10];
+    ll s5 = f[9] + f[8], d5 = f[9] - f[8];
+    ll s6 = f[11] + f[14], d6 = f[11] - f[14];
+    ll s7 = f[13] + f[12], d7 = f[13] - f[12];
+    ll s8 = f[15] + f[18], d8 = f[15] - f[18];
+    ll s9 = f[17] + f[16], d9 = f[17] - f[16];
+    const ll sa = s1 + s2 + s3;
+    const ll sxy = s4 + s5, sxz = s6 + s7, syz = s8 + s9;
+    const ll se = sxy + sxz + syz;
+    const ll ex_ = (d4 + d5) + (d6 + d7);
+    const ll ey_ = (d4 - d5) + (d8 + d9);
+    const ll ez_ = (d6 - d7) + (d8 - d9);
+    const ll uh = FX_ONE / 2;
+    const bool ok = rho >= FX_ONE / 4 && rho < 2 * FX_ONE && ux > -uh && ux < uh && uy > -uh &&
+                    uy < uh && uz > -uh && uz < uh;
+    const ll m1 = -30 * f[0] - 11 * sa + 8 * se;
+    const ll m2 = 12 * f[0] - 4 * sa + se;
+    const ll m4 = -4 * d1 + ex_;
+    const ll m6 = -4 * d2 + ey_;
+    const ll m8 = -4 * d3 + ez_;
+    const ll m9 = 2 * s1 - (s2 + s3) + (sxy + sxz) - 2 * syz;
+    const ll m10 = -4 * s1 + 2 * (s2 + s3) + (sxy + sxz) - 2 * syz;
+    const ll m11 = (s2 - s3) + (sxy - sxz);
+    const ll m12 = -2 * (s2 - s3) + (sxy - sxz);
+    const ll m13 = s4 - s5;
+    const ll m14 = s8 - s9;
+    const ll m15 = s6 - s7;
+    const ll m16 = (d4 + d5) - (d6 + d7);
+    const ll m17 = (d5 - d4) + (d8 + d9);
+    const ll m18 = (d6 - d7) - (d8 - d9);
+    const ll ux2 = qmul(ux, ux), uy2 = qmul(uy, uy), uz2 = qmul(uz, uz);
+    const ll rusq = qmul(rho, ux2 + uy2 + uz2);
+    const ll p9 = 2 * ux2 - uy2 - uz2;
+    const ll p11 = uy2 - uz2;
+    const ll rp9 = qmul(rho, p9);
+    const ll n1 = m1 - (-11 * rho + 19 * rusq);
+    const ll n2 = m2 - (3 * rho - ((11 * rusq) >> 1));
+    const ll n4 = m4 + qmulc(2 * rux, FX_THIRD);
+    const ll n6 = m6 + qmulc(2 * ruy, FX_THIRD);
+    const ll n8 = m8 + qmulc(2 * ruz, FX_THIRD);
+    const ll n9 = m9 - rp9;
+    const ll n10 = m10 + (rp9 >> 1);
+    const ll rp11 = qmul(rho, p11);
+    const ll n11 = m11 - rp11;
+    const ll n12 = m12 + (rp11 >> 1);
+    const ll n13 = m13 - qmul(rux, uy);
+    const ll n14 = m14 - qmul(ruy, uz);
+    const ll n15 = m15 - qmul(rux, uz);
+    ll r1 = qmulc(n1, c.c1), r2 = qmulc(n2, c.c2);
+    ll r4 = qmulc(n4, c.c4), r6 = qmulc(n6, c.c4), r8 = qmulc(n8, c.c4);
+    ll r9 = qmulc(n9, c.c9), r10 = qmulc(n10, c.c10), r11 = qmulc(n11, c.c11);
+    ll r12 = qmulc(n12, c.c12);
+    ll r13 = qmulc(n13, c.c13), r14 = qmulc(n14, c.c13), r15 = qmulc(n15, c.c13);
+    const ll r16 = qmulc(m16, c.c16), r17 = qmulc(m17, c.c16), r18 = qmulc(m18, c.c16);
+    // source terms (evolution_f.F90:107-129): r -= h S
+    const ll ufx = qmul(ux, fx), vfy = qmul(uy, fy), wfz = qmul(uz, fz);
+    const ll uf = ufx + vfy + wfz;
+    r1 -= qmulc(38 * uf, T.h1);
+    r2 += qmulc(11 * uf, T.h2);
+    const ll r3 = -qmulc(fx, T.h3), r5 = -qmulc(fy, T.h3), r7 = -qmulc(fz, T.h3);
+    r4 += qmulc(qmulc(2 * fx, FX_THIRD), T.h4);
+    r6 += qmulc(qmulc(2 * fy, FX_THIRD), T.h4);
+    r8 += qmulc(qmulc(2 * fz, FX_THIRD), T.h4);
+    r9 -= qmulc(4 * ufx - 2 * vfy - 2 * wfz, T.h9);
+    r10 -= qmulc(-2 * ufx + vfy + wfz, T.h10);
+    r11 -= qmulc(2 * vfy - 2 * wfz, T.h11);
+    r12 -= qmulc(wfz - vfy, T.h12);
+    r13 -= qmulc(qmul(ux, fy) + qmul(uy, fx), T.h13);
+    r14 -= qmulc(qmul(uy, fz) + qmul(uz, fy), T.h13);
+    r15 -= qmulc(qmul(ux, fz) + qmul(uz, fx), T.h13);
+    // inverse transform M^T r by pairs
+    const ll bax = -11 * r1 - 4 * r2;
+    const ll bed = 8 * r1 + r2;
+    f[0] -= -30 * r1 + 12 * r2;
+    const ll A9 = -r9 + 2 * r10, B11 = r11 - 2 * r12;
+    const ll S910 = r9 + r10, S1112 = r11 + r12;
+    const ll X = r3 + r4, Y = r5 + r6, Z = r7 + r8;
+    ll E, O;
+    E = bax + (2 * r9 - 4 * r10); O = r3 - 4 * r4;
+    f[1] -= E + O; f[2] -= E - O;
+    E = bax + A9 + B11; O = r5 - 4 * r6;
+    f[3] -= E + O; f[4] -= E - O;
+    E = bax + A9 - B11; O = r7 - 4 * r8;
+    f[5] -= E + O; f[6] -= E - O;
+    const ll be = bed + S910;
+    E = be + S1112 + r13; O = X + Y + (r16 - r17);
+    f[7] -= E + O; f[10] -= E - O;
+    E = be + S1112 - r13; O = X - Y + (r16 + r17);
+    f[9] -= E + O; f[8] -= E - O;
+    E = be - S1112 + r15; O = X + Z + (r18 - r16);
+    f[11] -= E + O; f[14] -= E - O;
+    E = be - S1112 - r15; O = X - Z - (r16 + r18);
+    f[13] -= E + O; f[12] -= E - O;
+    const ll bz = bed - 2 * S910;
+    E = bz + r14; O = Y + Z + (r17 - r18);
+    f[15] -= E + O; f[18] -= E - O;
+    E = bz - r14; O = Y - Z + (r17 + r18);
+    f[17] -= E + O; f[16] -= E - O;
+    return ok;
+}
+
+// D3Q7 MRT of the temperature populations (evolution_g.F90:1-57) on Q55, in
+// place: n = N g, t = q (n - neq) / |N|^2, g -= N^T t.
+__device__ __forceinline__ void mrt_collide_t_fx(long long* g, long long temp, long long ux,
+                                                 long long uy, long long uz,
+                                                 const FxThermalCoef& T) {
+    using ll = long long;
+    const ll n1 = g[1] - g[2], n2 = g[3] - g[4], n3 = g[5] - g[6];
+    const ll sx = g[1] + g[2], sy = g[3] + g[4], sz = g[5] + g[6];
+    const ll n4 = -6 * g[0] + (sx + sy + sz);
+    const ll n5 = 2 * sx - (sy + sz);
+    const ll n6 = sy - sz;
+    const ll t1 = qmul(n1 - qmul(temp, ux), T.qd_half);
+    const ll t2 = qmul(n2 - qmul(temp, uy), T.qd_half);
+    const ll t3 = qmul(n3 - qmul(temp, uz), T.qd_half);
+    const ll t4 = qmulc(n4 - qmul(temp, T.para_a), T.qnu42);
+    const ll t5 = qmulc(n5, T.qnu12);
+    const ll t6 = qmulc(n6, T.qnu4);
+    g[0] -= -6 * t4;
+    const ll ex5 = t4 + 2 * t5;
+    const ll ey5 = t4 - t5;
+    g[1] -= ex5 + t1; g[2] -= ex5 - t1;
+    g[3] -= (ey5 + t6) + t2; g[4] -= (ey5 + t6) - t2;
+    g[5] -= (ey5 - t6) + t3; g[6] -= (ey5 - t6) - t3;
 }
 
 }  // namespace mglc

@@ -38,6 +38,19 @@ __global__ void __launch_bounds__(128)
     lid_cell_fx<FIRST, IDX>(i, blockIdx.y, blockIdx.z, fin, fout, K, P, mrho, mu, mv, mw);
 }
 
+template <bool FIRST, bool ROT, typename IDX>
+__global__ void __launch_bounds__(128)
+    k_thermal_step_fx(const double* __restrict__ fin, double* __restrict__ fout,
+                      const double* __restrict__ gin, double* __restrict__ gout,
+                      double* __restrict__ F, FxTK K, IDX P, const double* __restrict__ mrho,
+                      const double* __restrict__ mu, const double* __restrict__ mv,
+                      const double* __restrict__ mw, const double* __restrict__ mT) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= K.nx) return;
+    thermal_cell_fx<FIRST, ROT, IDX>(i, blockIdx.y, blockIdx.z, fin, fout, gin, gout, F, K, P,
+                                     mrho, mu, mv, mw, mT);
+}
+
 template <typename S, bool FIRST, bool ROT, typename IDX>
 __global__ void __launch_bounds__(128)
     k_thermal_step(const S* __restrict__ fin, S* __restrict__ fout,
@@ -149,10 +162,42 @@ static cudaError_t th_go(bool first, const void* fin, void* fout, const void* gi
     return cudaGetLastError();
 }
 
+static cudaError_t th_go_fx(bool first, const void* fin, void* fout, const void* gin, void* gout,
+                            void* F, const ThermalStepArgs& a, cudaStream_t s) {
+    FxTK K;
+    K.nx = a.g.nx; K.ny = a.g.ny; K.nz = a.g.nz; K.bc_y = a.bc_y; K.bc_z = a.bc_z;
+    K.t = make_fx_thermal(a.cd, a.gbeta, a.omega_rot, a.t_ref, a.para_a, a.qd, a.qnu, a.t_hot,
+                          a.t_cold);
+    dim3 b = step_block(a.g.nx), gr = step_grid(a.g, b);
+    const bool rot = a.omega_rot != 0.0;
+    const bool small = (long long)Q19 * a.g.plane < (1ll << 31);
+    const double* fi = (const double*)fin;
+    const double* gi = (const double*)gin;
+    double* fo = (double*)fout;
+    double* go = (double*)gout;
+    double* Fp = (double*)F;
+#define THX_LAUNCH(FI, RO, IT) \
+    k_thermal_step_fx<FI, RO, IT><<<gr, b, 0, s>>>(fi, fo, gi, go, Fp, K, (IT)a.g.plane, a.rho, a.u, a.v, a.w, a.T)
+#define THX_ROT(IT)                                 \
+    if (first && rot) THX_LAUNCH(true, true, IT);    \
+    else if (first) THX_LAUNCH(true, false, IT);     \
+    else if (rot) THX_LAUNCH(false, true, IT);       \
+    else THX_LAUNCH(false, false, IT);
+    if (small) {
+        THX_ROT(unsigned)
+    } else {
+        THX_ROT(long long)
+    }
+#undef THX_ROT
+#undef THX_LAUNCH
+    return cudaGetLastError();
+}
+
 cudaError_t launch_thermal_step(int form, bool first, const void* fin, void* fout,
                                 const void* gin, void* gout, void* F, const ThermalStepArgs& a,
                                 cudaStream_t s) {
     switch (form) {
+        case FORM_FX64: return th_go_fx(first, fin, fout, gin, gout, F, a, s);
         case FORM_FP64: return th_go<double>(first, fin, fout, gin, gout, F, a, s);
         case FORM_FP32: return th_go<float>(first, fin, fout, gin, gout, F, a, s);
         case FORM_FP16: return th_go<__half>(first, fin, fout, gin, gout, F, a, s);

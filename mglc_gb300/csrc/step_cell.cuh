@@ -406,4 +406,112 @@ __device__ __forceinline__ void thermal_cell(
     }
 }
 
+
+// -------------------------------------------------- heated cavity, FX64 --
+// FP64 storage (f, g and the carried force as in the FP64 form); forced
+// D3Q19 and D3Q7 collisions in Q55 (fixed64.cuh); the streaming, bounce-back
+// and anti-bounce-back of thermal_cell.
+struct FxTK {
+    int nx, ny, nz, bc_y, bc_z;
+    FxThermalCoef t;
+};
+
+template <bool FIRST, bool ROT, typename IDX>
+__device__ __forceinline__ void thermal_cell_fx(
+    int i, int j, int k, const double* __restrict__ fin, double* __restrict__ fout,
+    const double* __restrict__ gin, double* __restrict__ gout, double* __restrict__ F,
+    const FxTK& K, IDX P, const double* __restrict__ mrho, const double* __restrict__ mu,
+    const double* __restrict__ mv, const double* __restrict__ mw, const double* __restrict__ mT) {
+    using ll = long long;
+    const int nx = K.nx, ny = K.ny, nz = K.nz;
+    const IDX cell = (IDX)i + (IDX)nx * ((IDX)j + (IDX)ny * (IDX)k);
+    ll f[Q19], g[Q7];
+    bool bad = false;
+    {
+        double rf[Q19], rg[Q7];
+#pragma unroll
+        for (int q = 0; q < Q19; q++) rf[q] = __ldg(fin + ((IDX)q * P + cell));
+#pragma unroll
+        for (int q = 0; q < Q7; q++) rg[q] = __ldg(gin + ((IDX)q * P + cell));
+#pragma unroll
+        for (int q = 0; q < Q19; q++) {
+            bad |= fx_bad(rf[q]);
+            f[q] = q < FX_CVT_IN ? d2q_cvt(rf[q]) : d2q(rf[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < Q7; q++) {
+            bad |= fx_bad2(rg[q]);
+            g[q] = d2q(rg[q]);
+        }
+    }
+    ll rho, ux, uy, uz, temp, rux, ruy, ruz;
+    if (FIRST) {
+        const double r = mrho[cell], a = mu[cell], b = mv[cell], c = mw[cell], t = mT[cell];
+        bad |= ((unsigned)(__double_as_longlong(r) >> 52) & 0x7FFu) >= 1024u;
+        bad |= fx_bad(a) || fx_bad(b) || fx_bad(c) || fx_bad2(t);
+        rho = d2q(r); ux = d2q(a); uy = d2q(b); uz = d2q(c); temp = d2q(t);
+        rux = qmul(rho, ux); ruy = qmul(rho, uy); ruz = qmul(rho, uz);
+    } else {
+        // u = (sum f e + F/2) / rho with the force carried from the previous step
+        ll fxp = 0, fyp = 0;
+        if (ROT) {
+            fxp = d2q(F[cell]);
+            fyp = d2q(F[P + cell]);
+        }
+        const ll fzp = d2q(F[2 * P + cell]);
+        const ll s1 = f[1] + f[2], s2 = f[3] + f[4], s3 = f[5] + f[6];
+        const ll s4 = f[7] + f[10], s5 = f[9] + f[8], s6 = f[11] + f[14], s7 = f[13] + f[12];
+        const ll s8 = f[15] + f[18], s9 = f[17] + f[16];
+        rho = f[0] + (s1 + s2 + s3) + ((s4 + s5) + (s6 + s7) + (s8 + s9));
+        const ll d4 = f[7] - f[10], d5 = f[9] - f[8], d6 = f[11] - f[14], d7 = f[13] - f[12];
+        const ll d8 = f[15] - f[18], d9 = f[17] - f[16];
+        rux = (f[1] - f[2]) + (d4 + d5) + (d6 + d7) + (fxp >> 1);
+        ruy = (f[3] - f[4]) + (d4 - d5) + (d8 + d9) + (fyp >> 1);
+        ruz = (f[5] - f[6]) + (d6 - d7) + (d8 - d9) + (fzp >> 1);
+        const ll inv = fx_recip(rho);
+        ux = qmul(rux, inv);
+        uy = qmul(ruy, inv);
+        uz = qmul(ruz, inv);
+        temp = ((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + g[6]);
+    }
+    // body force from (rho, u, T) of the previous macro (bouyancy3d_mpi.F90:743-745)
+    ll fx = 0, fy = 0;
+    if (ROT) {
+        fx = -qmul(qmul(rho, uy), K.t.omega2);
+        fy = qmul(qmul(rho, ux), K.t.omega2);
+        F[cell] = q2d(fx);
+        F[P + cell] = q2d(fy);
+    }
+    const ll fz = qmul(rho, qmulc(temp - K.t.t_ref, K.t.gbeta));
+    F[2 * P + cell] = q2d(fz);
+    bad |= !mrt_collide_fx_forced(f, rho, ux, uy, uz, rux, ruy, ruz, fx, fy, fz, K.t);
+    mrt_collide_t_fx(g, temp, ux, uy, uz, K.t);
+
+    const double nan = __longlong_as_double(0x7ff8000000000000LL);
+    const IDX sy = (IDX)nx, sz = (IDX)nx * (IDX)ny;
+    const unsigned bm = face_mask(i, j, k, nx, ny, nz);
+#pragma unroll
+    for (int q = 0; q < Q19; q++) {
+        const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
+        const double o = bad ? nan : (q < FX_CVT_OUT ? q2d_cvt(f[q]) : q2d(f[q]));
+        if ((bm & leave_bits(dx, dy, dz)) == 0)
+            fout[(IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz] = o;
+        else
+            fout[(IDX)opp19(q) * P + cell] = o;
+    }
+    // D3Q7: adiabatic walls reflect, constant-T walls anti-bounce-back
+#pragma unroll
+    for (int q = 0; q < Q7; q++) {
+        const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
+        if ((bm & leave_bits(dx, dy, dz)) == 0) {
+            gout[(IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz] = bad ? nan : q2d(g[q]);
+        } else {
+            ll val = g[q];
+            if (dy != 0 && K.bc_y) val = -val + (dy < 0 ? K.t.chot : K.t.ccold);
+            if (dz != 0 && K.bc_z) val = -val + (dz < 0 ? K.t.chot : K.t.ccold);
+            gout[(IDX)opp19(q) * P + cell] = bad ? nan : q2d(val);
+        }
+    }
+}
+
 }  // namespace mglc

@@ -106,3 +106,57 @@ def test_cell_outside_the_range_box_writes_nan(mg):
         c.step(1)
         g = c.get_f()
     assert np.isnan(g).sum() == 19 and np.isfinite(g[0, 0, 0]).all()
+
+
+# ------------------------------------------------------------ heated cavity --
+def _thermal(mg, d):
+    ek = float(d["ekman"])
+    rb = str(d["variant"]) == "rb"
+    return mg.BuoyancyCavity(int(d["nx"]), int(d["ny"]), int(d["nz"]), rayleigh=float(d["rayleigh"]),
+                             prandtl=float(d["prandtl"]), mach=float(d["mach"]),
+                             t_hot=float(d["thot"]), t_cold=float(d["tcold"]), t_ref=float(d["tref"]),
+                             ekman=ek if np.isfinite(ek) else 0.0, bc_y_const_t=not rb,
+                             bc_z_const_t=rb, precision="fx64")
+
+
+@pytest.mark.parametrize("case", ["thermal_6x7x5_ref", "thermal_5x6x7_pm", "thermal_6x5x6_rb"])
+def test_thermal_matches_reference_statement_fixtures(mg, case):
+    d = np.load(os.path.join(GOLD, case + ".npz"))
+    with _thermal(mg, d) as c:
+        assert c.info().precision == 4
+        c.initial()
+        c.step(int(d["nsteps"]))
+        rho, u, v, w, T = c.macro()
+        f, g = c.get_f()
+    assert rel_l2(f, d["f"]) < 1e-13 and rel_l2(g, d["g"]) < 1e-13
+    for got, key in ((rho, "rho"), (T, "T")):
+        assert rel_l2(got, d[key]) < 1e-12, key
+    for got, key in ((u, "u"), (v, "v"), (w, "w")):
+        np.testing.assert_allclose(got, d[key], rtol=1e-9, atol=1e-14, err_msg=key)
+
+
+@pytest.mark.parametrize("ekman", [0.0, 1e-3])
+def test_thermal_32_cubed_1000_steps_rel_l2_1e_10(mg, ekman):
+    n, steps = 32, 1000
+    o = O.ThermalOracle(n, n, n, 1e5, 0.71, 0.1, ekman, 0.5, -0.5, 0.0)
+    o.run(steps, nthreads=NT)
+    with mg.BuoyancyCavity(n, rayleigh=1e5, prandtl=0.71, mach=0.1, t_hot=0.5, t_cold=-0.5,
+                           ekman=ekman, precision="fx64") as c:
+        c.initial()
+        c.step(steps)
+        rho, u, v, w, T = c.macro()
+    for got, ref, key in ((rho, o.rho, "rho"), (u, o.u, "u"), (v, o.v, "v"), (w, o.w, "w"),
+                          (T, o.T, "T")):
+        e = rel_l2(got, ref)
+        assert e <= 1e-10, (key, e)
+
+
+def test_thermal_one_step_agrees_with_ieee_fp64(mg):
+    out = {}
+    for form in ("fp64", "fx64"):
+        with mg.BuoyancyCavity(20, 18, 16, rayleigh=1e5, t_hot=0.5, t_cold=-0.5, precision=form) as c:
+            c.initial()
+            c.step(60)
+            out[form] = c.get_f()
+    assert rel_l2(out["fx64"][0], out["fp64"][0]) < 1e-13
+    assert rel_l2(out["fx64"][1], out["fp64"][1]) < 1e-13
