@@ -561,7 +561,7 @@ def main():
     if rank == 0 and not args.no_forms:
         forms = {}
         fms = {"particle": ("fp64", "fp32"),
-               "thermal": ("fp64", "fp32", "fp16", "fp16s", "bf16", "bf16s"),
+               "thermal": ("fp64", "fx64", "fp32", "fp16", "fp16s", "bf16", "bf16s"),
                "lid": ("fp64", "fx64", "fp32", "fp16", "fp16s", "bf16", "bf16s")}[wl["kind"]]
         for fm in fms:
             if fm == args.form:

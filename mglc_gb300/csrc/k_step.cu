@@ -38,8 +38,10 @@ __global__ void __launch_bounds__(128)
     lid_cell_fx<FIRST, IDX>(i, blockIdx.y, blockIdx.z, fin, fout, K, P, mrho, mu, mv, mw);
 }
 
+// 4 blocks of 128 per SM (128 registers): measured faster than the 168-register
+// allocation at 3 blocks and than 5 blocks with spills
 template <bool FIRST, bool ROT, typename IDX>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, 4)
     k_thermal_step_fx(const double* __restrict__ fin, double* __restrict__ fout,
                       const double* __restrict__ gin, double* __restrict__ gout,
                       double* __restrict__ F, FxTK K, IDX P, const double* __restrict__ mrho,

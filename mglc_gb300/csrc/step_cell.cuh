@@ -411,6 +411,11 @@ __device__ __forceinline__ void thermal_cell(
 // FP64 storage (f, g and the carried force as in the FP64 form); forced
 // D3Q19 and D3Q7 collisions in Q55 (fixed64.cuh); the streaming, bounce-back
 // and anti-bounce-back of thermal_cell.
+// temperature populations converted on the FP64 unit (the rest with integer
+// bit operations)
+#ifndef FXT_CVT_G
+#define FXT_CVT_G 4
+#endif
 struct FxTK {
     int nx, ny, nz, bc_y, bc_z;
     FxThermalCoef t;
@@ -441,7 +446,7 @@ __device__ __forceinline__ void thermal_cell_fx(
 #pragma unroll
         for (int q = 0; q < Q7; q++) {
             bad |= fx_bad2(rg[q]);
-            g[q] = d2q(rg[q]);
+            g[q] = q < FXT_CVT_G ? d2q_cvt(rg[q]) : d2q(rg[q]);
         }
     }
     ll rho, ux, uy, uz, temp, rux, ruy, ruz;
@@ -504,12 +509,13 @@ __device__ __forceinline__ void thermal_cell_fx(
     for (int q = 0; q < Q7; q++) {
         const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
         if ((bm & leave_bits(dx, dy, dz)) == 0) {
-            gout[(IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz] = bad ? nan : q2d(g[q]);
+            gout[(IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz] =
+                bad ? nan : (q < FXT_CVT_G ? q2d_cvt(g[q]) : q2d(g[q]));
         } else {
             ll val = g[q];
             if (dy != 0 && K.bc_y) val = -val + (dy < 0 ? K.t.chot : K.t.ccold);
             if (dz != 0 && K.bc_z) val = -val + (dz < 0 ? K.t.chot : K.t.ccold);
-            gout[(IDX)opp19(q) * P + cell] = bad ? nan : q2d(val);
+            gout[(IDX)opp19(q) * P + cell] = bad ? nan : (q < FXT_CVT_G ? q2d_cvt(val) : q2d(val));
         }
     }
 }
