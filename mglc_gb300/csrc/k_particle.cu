@@ -30,6 +30,8 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <atomic>
+
 #include "particles.cuh"
 
 namespace mglc {
@@ -994,11 +996,17 @@ static cudaError_t pstep_go(bool first, const void* fin, void* fout, const PartP
         const int bw = 2 * ((int)ceil(p.radius) + 2) + 2;
         const size_t tile = sizeof(int) * (size_t)(bw + 2) * (bw + 2) * ((bw + NSLAB - 1) / NSLAB + 2);
         if (tile <= TILE_MAX_BYTES) {
-            static bool attr_set[2] = {false, false};  // per storage type
-            if (!attr_set[sizeof(S) == 4]) {
-                cudaFuncSetAttribute(k_plinks<S, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)TILE_MAX_BYTES);
-                attr_set[sizeof(S) == 4] = true;
+            // the shared-memory opt-in is a per-device attribute of the kernel
+            static std::atomic<unsigned long long> opted{0};  // bit = device ordinal
+            int dev = 0;
+            cudaGetDevice(&dev);
+            const unsigned long long bit = 1ull << (dev & 63);
+            if (!(opted.load() & bit)) {
+                cudaError_t e = cudaFuncSetAttribute(k_plinks<S, true>,
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)TILE_MAX_BYTES);
+                if (e != cudaSuccess) return e;
+                opted.fetch_or(bit);
             }
             k_plinks<S, true><<<dim3(p.np, NSLAB), PB, tile, s>>>((S*)fout, p, d);
         } else {
