@@ -42,6 +42,8 @@ struct St<__half> {
     // stochastic rounding: 13 uniform bits added below the 10 kept mantissa
     // bits, then truncation (unbiased; rounding errors do not correlate from
     // step to step, so they do not accumulate into a drift)
+    // (finite values only: adding to a NaN pattern could wrap into the sign
+    // bit; the cell bodies round to nearest in cells whose rho or u is not finite)
     __device__ static void st_sr(__half* p, C v, float sc, unsigned r) {
         *p = __float2half_rz(__uint_as_float(__float_as_uint(v * sc) + (r >> 19)));
     }
@@ -170,8 +172,11 @@ __device__ __forceinline__ void lid_cell_from(int i, int j, int k, const S (&raw
     const IDX sy = (IDX)nx, sz = (IDX)nx * (IDX)ny;
     const unsigned bm = face_mask(i, j, k, nx, ny, nz);
     const unsigned h0 = sr_cell((unsigned)cell, seed);
+    // stochastic rounding for finite cells; a NaN or infinite cell rounds to
+    // nearest so that the non-finite values propagate unchanged
+    const bool sr = K.sr && isfinite(rho + ux + uy + uz);
     auto put = [&](S* p, C v, int q) {
-        if (K.sr) St<S>::st_sr(p, v, K.scale, sr_pop(h0, q));
+        if (sr) St<S>::st_sr(p, v, K.scale, sr_pop(h0, q));
         else St<S>::st(p, v, K.scale);
     };
     if (bm == 0) {  // interior cell: every population streams
@@ -365,8 +370,9 @@ __device__ __forceinline__ void thermal_cell(
     const IDX sy = (IDX)nx, sz = (IDX)nx * (IDX)ny;
     const unsigned bm = face_mask(i, j, k, nx, ny, nz);
     const unsigned h0 = sr_cell((unsigned)cell, seed);
+    const bool sr = K.sr && isfinite(rho + ux + uy + uz + temp);
     auto put = [&](S* p, C v, int q) {
-        if (K.sr) St<S>::st_sr(p, v, K.scale, sr_pop(h0, q));
+        if (sr) St<S>::st_sr(p, v, K.scale, sr_pop(h0, q));
         else St<S>::st(p, v, K.scale);
     };
     if (bm == 0) {
