@@ -375,6 +375,44 @@ def serve_bench(torch, mg, n_req=24, rate=50.0, seed=1234, max_steps=2000, tol=1
                      "ctas_per_sm": st["ctas_per_sm"]}}
 
 
+def lid2d_bench(torch, mg, n=1024, steps=400, warmup=20, cpu_s=3.0):
+    """The D2Q9 lid cavity (the reference's 2-D code; FP64, bitwise the
+    reference's statements) at n^2: device MLUPS between CUDA events on the
+    context's stream, and the oracle on all host cores for a bounded sample.
+    The kernel is bound by the FP64 pipe, not by HBM (144 B per node)."""
+    c = mg.LidDrivenCavity2D(n, reynolds=1000.0, u0=0.1)
+    stream = torch.cuda.Stream()
+    c.set_stream(stream.cuda_stream)
+    c.initial()
+    c.step(warmup)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    c.step(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    c.set_stream(None)
+    c.close()
+    v = n * n * steps / (ms * 1e-3) / 1e6
+    out = {"workload": f"D2Q9 MRT lid cavity {n}^2, Re=1000 (2d_revised/mpi_blocked), FP64 bitwise",
+           "value": round(v, 1), "unit": "MLUPS", "steps": steps,
+           "ms_per_step": round(ms / steps, 4), "bound": "fp64 pipe",
+           "hbm_gbs": round(144.0 * n * n / (ms / steps * 1e-3) / 1e9, 1),
+           "gpu_launches": steps}
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    o = O.Lid2DOracle(n, n, 1000.0, 0.1)
+    t0, k = time.perf_counter(), 0
+    while time.perf_counter() - t0 < cpu_s:
+        o.run(2, nthreads=threads)
+        k += 2
+    cv = n * n * k / (time.perf_counter() - t0) / 1e6
+    out["cpu_baseline"] = {"value": round(cv, 1), "unit": "MLUPS", "cores": threads, "kind": "port",
+                           "sample": f"{k} steps of the same {n}^2 cavity (oracle, OpenMP)"}
+    return out
+
+
 def cpu_sample(wl, target_s=10.0):
     """The oracle (restatement of the reference's CPU code) with OpenMP on all
     host cores, on a bounded sample of the workload."""
@@ -494,6 +532,7 @@ def main():
                     help="skip measuring each form's error against FP64")
     ap.add_argument("--error-steps", type=int, default=0,
                     help="steps for the error runs (default: the workload's own count)")
+    ap.add_argument("--no-lid2d", action="store_true", help="skip the D2Q9 lid cavity line")
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-max-steps", type=int, default=2000)
     args = ap.parse_args()
@@ -597,6 +636,8 @@ def main():
     if rank == 0 and not args.no_serve and wl["kind"] == "lid":
         line["serve"] = serve_bench(torch, mglc_gb300, n_req=args.serve_requests,
                                     max_steps=args.serve_max_steps)
+    if rank == 0 and not args.no_lid2d and wl["kind"] == "lid":
+        line["lid2d"] = lid2d_bench(torch, mglc_gb300)
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_sample(wl)
     if rank == 0:

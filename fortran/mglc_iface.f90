@@ -44,6 +44,12 @@ module mglc_iface
         integer(c_int) :: q_bisection
     end type
 
+    type, bind(C) :: mglc_lid2d_params
+        integer(c_int) :: total_nx, total_ny
+        real(c_double) :: reynolds, rho0, u0
+        integer(c_int) :: precision
+    end type
+
     type, bind(C) :: mglc_nure_status
         integer(c_int) :: time
         real(c_double) :: nu, re, nu_mean, re_mean
@@ -129,6 +135,12 @@ module mglc_iface
             type(mglc_particle2d_params), intent(in) :: p
             real(c_double), intent(in) :: centers(*)
             integer(c_int), value :: np
+            type(c_ptr), intent(out) :: ctx
+        end function
+        !! 2-D lid-driven cavity (2d_revised/mpi_blocked), f(0:8,nx,ny)
+        integer(c_int) function mglc_lid2d_create(p, ctx) bind(C, name="mglc_lid2d_create")
+            import :: c_int, c_ptr, mglc_lid2d_params
+            type(mglc_lid2d_params), intent(in) :: p
             type(c_ptr), intent(out) :: ctx
         end function
         integer(c_int) function mglc_particle_state(ctx, xc, uc, omega, force, torque) &

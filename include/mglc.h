@@ -52,7 +52,8 @@ extern "C" {
 enum { MGLC_FP64 = 0, MGLC_FP32 = 1, MGLC_FP16 = 2, MGLC_BF16 = 3, MGLC_FX64 = 4,
        MGLC_FP16S = 5, MGLC_BF16S = 6 };
 
-enum { MGLC_KIND_LID = 1, MGLC_KIND_THERMAL = 2, MGLC_KIND_PARTICLE = 3, MGLC_KIND_PARTICLE2D = 4 };
+enum { MGLC_KIND_LID = 1, MGLC_KIND_THERMAL = 2, MGLC_KIND_PARTICLE = 3, MGLC_KIND_PARTICLE2D = 4,
+       MGLC_KIND_LID2D = 5 };
 
 typedef struct mglc_ctx mglc_ctx;
 
@@ -136,6 +137,21 @@ typedef struct mglc_particle2d_params {
 } mglc_particle2d_params;
 int mglc_particle2d_create(const mglc_particle2d_params* p, const double* centers, int np,
                            mglc_ctx** out);
+/* D2Q9 MRT lid-driven cavity: the reference's 2-D code
+ * (MPI/Lid_driven_cavity/fortran/2d/2d_revised/mpi_blocked; commondata.f90:4-30
+ * for the parameters, tauf = u0*total_nx/reynolds*3 + 0.5).  Lid along +x on
+ * the top row (j = ny), initial u = u0 on that row (initial.f90:47-51).  FP64,
+ * every statement in the reference's order: bitwise the reference's fields and
+ * check() residual.  Verbs: mglc_initial, mglc_load_state (f, and rho,u,v or
+ * none), mglc_step, mglc_get_f (9 per node), mglc_get_macros(_device) (w = 0),
+ * mglc_check (error_t = 0), mglc_totals. */
+typedef struct mglc_lid2d_params {
+    int total_nx, total_ny;
+    double reynolds, rho0, u0;
+    int precision; /* MGLC_FP64 */
+} mglc_lid2d_params;
+/* Replaces the allocation part of 2d_revised/mpi_blocked/initial.f90:32-38. */
+int mglc_lid2d_create(const mglc_lid2d_params* p, mglc_ctx** out);
 void mglc_destroy(mglc_ctx* ctx);
 const char* mglc_last_error(const mglc_ctx* ctx);
 /* Bind the context to a caller-owned cudaStream_t (NULL = the context's own stream). */

@@ -5,10 +5,10 @@ kernels for sm_103a under csrc/).  This package builds it and offers a thin
 Python host API that mirrors the reference's routines.
 """
 from .capi import FORMS, MglcError, lib  # noqa: F401
-from .cavity import (BuoyancyCavity, LidDrivenCavity, NuReMonitor, ParticleFlow,  # noqa: F401
-                     ParticleFlow2D)
+from .cavity import (BuoyancyCavity, LidDrivenCavity, LidDrivenCavity2D, NuReMonitor,  # noqa: F401
+                     ParticleFlow, ParticleFlow2D)
 from .serve import SolveServer  # noqa: F401
 
-__all__ = ["LidDrivenCavity", "BuoyancyCavity", "ParticleFlow", "ParticleFlow2D", "NuReMonitor",
+__all__ = ["LidDrivenCavity", "LidDrivenCavity2D", "BuoyancyCavity", "ParticleFlow", "ParticleFlow2D", "NuReMonitor",
            "SolveServer", "MglcError",
            "FORMS", "lib"]

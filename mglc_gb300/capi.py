@@ -76,6 +76,11 @@ class Particle2DParams(ctypes.Structure):
                 ("threshold_particle", _D), ("stiff_particle", _D), ("q_bisection", _I)]
 
 
+class Lid2DParams(ctypes.Structure):
+    _fields_ = [("total_nx", _I), ("total_ny", _I), ("reynolds", _D), ("rho0", _D), ("u0", _D),
+                ("precision", _I)]
+
+
 class NuReStatus(ctypes.Structure):
     _fields_ = [("time", _I), ("nu", _D), ("re", _D), ("nu_mean", _D), ("re_mean", _D),
                 ("stationary", _I), ("stationary_time", _I), ("converged", _I),
@@ -91,6 +96,7 @@ SIGNATURES = {
     "mglc_particle_create": ([ctypes.POINTER(ParticleParams), _VP, _I, ctypes.POINTER(_VP)], _I),
     "mglc_particle_state": ([_VP, _VP, _VP, _VP, _VP, _VP], _I),
     "mglc_particle2d_create": ([ctypes.POINTER(Particle2DParams), _VP, _I, ctypes.POINTER(_VP)], _I),
+    "mglc_lid2d_create": ([ctypes.POINTER(Lid2DParams), ctypes.POINTER(_VP)], _I),
     "mglc_get_mask": ([_VP, _VP], _I),
     "mglc_destroy": ([_VP], None),
     "mglc_last_error": ([_VP], ctypes.c_char_p),

@@ -338,3 +338,50 @@ class ParticleFlow2D(_Solve):
         m = np.empty((ny, nx), dtype=np.int32)
         self._ck(capi.lib().mglc_get_mask(self._ctx, m.ctypes.data))
         return m
+
+
+class LidDrivenCavity2D(_Solve):
+    """D2Q9 MRT lid-driven cavity, the reference's 2-D code
+    (Lid_driven_cavity/fortran/2d/2d_revised/mpi_blocked); bitwise the
+    reference's statements, check() included.  Arrays are (ny, nx)."""
+
+    def __init__(self, total_nx, total_ny=None, reynolds=1000.0, u0=0.1, rho0=1.0,
+                 precision="fp64"):
+        super().__init__()
+        self.u0 = float(u0)
+        p = capi.Lid2DParams(total_nx, total_ny or total_nx, float(reynolds), float(rho0),
+                             float(u0), capi.FORMS[precision])
+        ctx = _P()
+        rc = capi.lib().mglc_lid2d_create(ctypes.byref(p), ctypes.byref(ctx))
+        self._ctx = ctx
+        if rc != capi.MGLC_OK:
+            msg = capi.lib().mglc_last_error(ctx).decode() if ctx else ""
+            self.close()
+            raise capi.MglcError(rc, msg)
+
+    @property
+    def shape2(self):
+        i = self.info()
+        return (i.ny, i.nx)
+
+    def get_f(self):
+        ny, nx = self.shape2
+        f = np.empty((ny, nx, 9))
+        self._ck(capi.lib().mglc_get_f(self._ctx, _ptr(f), None))
+        return f
+
+    def macro(self):
+        ny, nx = self.shape2
+        rho, u, v = (np.empty((ny, nx)) for _ in range(3))
+        self._ck(capi.lib().mglc_get_macros(self._ctx, _ptr(rho), _ptr(u), _ptr(v), None, None))
+        return rho, u, v
+
+    def check(self) -> float:
+        e = ctypes.c_double()
+        self._ck(capi.lib().mglc_check(self._ctx, ctypes.byref(e), None))
+        return e.value
+
+    def load_state(self, f, rho=None, u=None, v=None):
+        self._ck(capi.lib().mglc_load_state(self._ctx, _ptr(np.ascontiguousarray(f)), None,
+                                            _ptr(rho), _ptr(u), _ptr(v), None, None))
+        return self

@@ -18,6 +18,7 @@
 #include "kernels.cuh"
 #include "particles.cuh"
 #include "particles2d.cuh"
+#include "lid2d.cuh"
 
 using namespace mglc;
 
@@ -25,6 +26,7 @@ struct mglc_ctx {
     int kind = 0, form = FORM_FP64;
     bool fx64 = false;  // MGLC_FX64: FP64 storage (form FP64), Q55 fixed-point lid collision
     P2Ctx* p2d = nullptr;  // MGLC_KIND_PARTICLE2D: the D2Q9 case4 state
+    L2Ctx* l2d = nullptr;  // MGLC_KIND_LID2D: the D2Q9 lid-driven cavity
     bool sr = false;       // MGLC_FP16S / MGLC_BF16S: stochastic rounding of the 16-bit stores
     Geom geom{};
     long long n = 0;
@@ -340,6 +342,8 @@ void mglc_destroy(mglc_ctx* c) {
     if (!c) return;
     if (c->p2d) p2d_destroy(c->p2d);
     c->p2d = nullptr;
+    if (c->l2d) l2d_destroy(c->l2d);
+    c->l2d = nullptr;
     if (c->stream) cudaStreamSynchronize(c->stream);
     release(c);
     delete c;
@@ -350,6 +354,7 @@ const char* mglc_last_error(const mglc_ctx* c) { return c ? c->err.c_str() : "nu
 int mglc_set_stream(mglc_ctx* c, void* s) {
     if (!c) return MGLC_ERR_INVALID;
     if (c->p2d) return p2d_set_stream(c->p2d, (cudaStream_t)s);
+    if (c->l2d) return l2d_set_stream(c->l2d, (cudaStream_t)s);
     CK(cudaStreamSynchronize(c->stream), "synchronize");
     if (c->own_stream) cudaStreamDestroy(c->stream);
     if (s) {
@@ -373,7 +378,8 @@ int mglc_get_info(const mglc_ctx* c, mglc_info* o) {
     o->tauf = c->tauf;
     o->snu = c->snu;
     o->sq = c->sq;
-    o->viscosity = c->kind == MGLC_KIND_LID ? (c->tauf - 0.5) / 3.0 : c->viscosity;
+    o->viscosity = (c->kind == MGLC_KIND_LID || c->kind == MGLC_KIND_LID2D) ? (c->tauf - 0.5) / 3.0
+                                                                              : c->viscosity;
     o->diffusivity = c->diffusivity;
     o->para_a = c->para_a;
     o->gbeta = c->gbeta;
@@ -383,6 +389,12 @@ int mglc_get_info(const mglc_ctx* c, mglc_info* o) {
         o->itc = p2d_itc(c->p2d);
         o->bytes_per_cell_step = 2.0 * 9 * 8.0 + 4.0;  // f pulled from fp, the mask read
         o->device_bytes = p2d_device_bytes(c->p2d);
+        return MGLC_OK;
+    }
+    if (c->l2d) {
+        o->itc = l2d_itc(c->l2d);
+        o->bytes_per_cell_step = 2.0 * 9 * 8.0;
+        o->device_bytes = l2d_device_bytes(c->l2d);
         return MGLC_OK;
     }
     if (c->kind == MGLC_KIND_LID) {
@@ -407,6 +419,11 @@ int mglc_initial(mglc_ctx* c) {
     if (c->kind == MGLC_KIND_PARTICLE) return particle_initial(c);
     if (c->p2d) {
         int rc = p2d_initial(c->p2d, c->err);
+        c->initialised = rc == MGLC_OK;
+        return rc;
+    }
+    if (c->l2d) {
+        int rc = l2d_initial(c->l2d, c->err);
         c->initialised = rc == MGLC_OK;
         return rc;
     }
@@ -462,6 +479,11 @@ int mglc_load_state(mglc_ctx* c, const double* f, const double* g, const double*
                     const double* u, const double* v, const double* w, const double* T) {
     if (!c || !c->kind || !f) return c ? fail(c, MGLC_ERR_INVALID, "f is required") : MGLC_ERR_INVALID;
     if (c->p2d) return fail(c, MGLC_ERR_UNSUPPORTED, "2-D particle contexts start from mglc_initial");
+    if (c->l2d) {
+        int rc = l2d_load(c->l2d, f, rho, u, v, c->err);
+        c->initialised = c->initialised || rc == MGLC_OK;
+        return rc;
+    }
     if (thermal(c) && !g) return fail(c, MGLC_ERR_INVALID, "thermal contexts need g");
     const bool shifted = c->form != FORM_FP64;
     int rc;
@@ -510,6 +532,7 @@ int mglc_get_f(mglc_ctx* c, double* f, double* g) {
     if (!c || !c->kind) return MGLC_ERR_INVALID;
     if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial or mglc_load_state first");
     if (c->p2d) return f ? p2d_get_f(c->p2d, f, c->err) : MGLC_OK;
+    if (c->l2d) return f ? l2d_get_f(c->l2d, f, c->err) : MGLC_OK;
     const bool shifted = c->form != FORM_FP64;
     int rc;
     if (f && (rc = download_pops(c, Q19, c->f[c->cur], f, shifted))) return rc;
@@ -522,6 +545,7 @@ int mglc_step(mglc_ctx* c, int nsteps) {
     if (nsteps < 0) return fail(c, MGLC_ERR_INVALID, "nsteps must be >= 0");
     if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial or mglc_load_state first");
     if (c->p2d) return p2d_step(c->p2d, nsteps, c->err);
+    if (c->l2d) return l2d_step(c->l2d, nsteps, c->err);
     if (c->kind == MGLC_KIND_PARTICLE) {
         for (int s = 0; s < nsteps; s++) {
             const int nxt = c->cur ^ 1;
@@ -595,6 +619,7 @@ int mglc_get_macros_device(mglc_ctx* c, double* rho, double* u, double* v, doubl
     if (!c || !c->kind) return MGLC_ERR_INVALID;
     if (c->p2d) return fail(c, MGLC_ERR_UNSUPPORTED, "not available for 2-D particle contexts");
     if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial or mglc_load_state first");
+    if (c->l2d) return l2d_get_macros_device(c->l2d, rho, u, v, w, c->err);
     int rc = refresh_macros(c);
     if (rc) return rc;
     const size_t b = c->n * sizeof(double);
@@ -611,6 +636,7 @@ int mglc_get_macros(mglc_ctx* c, double* rho, double* u, double* v, double* w, d
     if (!c || !c->kind) return MGLC_ERR_INVALID;
     if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial or mglc_load_state first");
     if (c->p2d) return p2d_get_macros(c->p2d, rho, u, v, w, c->err);
+    if (c->l2d) return l2d_get_macros(c->l2d, rho, u, v, w, c->err);
     int rc = refresh_macros(c);
     if (rc) return rc;
     const size_t b = c->n * sizeof(double);
@@ -627,6 +653,17 @@ int mglc_check(mglc_ctx* c, double* error_u, double* error_t) {
     if (!c || !c->kind) return MGLC_ERR_INVALID;
     if (c->p2d) return fail(c, MGLC_ERR_UNSUPPORTED, "not available for 2-D particle contexts");
     if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial or mglc_load_state first");
+    if (c->l2d) {
+        double eu = 0.0;
+        int rc = l2d_check(c->l2d, &eu, c->err);
+        if (rc) return rc;
+        if (error_u) *error_u = eu;
+        if (error_t) *error_t = 0.0;
+        if (!std::isfinite(eu))
+            return fail(c, MGLC_ERR_NUMERIC, "non-finite velocity field at step %lld",
+                        l2d_itc(c->l2d));
+        return MGLC_OK;
+    }
     int rc = refresh_macros(c);
     if (rc) return rc;
     CK(launch_residual(c->n, c->u, c->v, c->w, thermal(c) ? c->T : nullptr, c->up, c->vp, c->wp,
@@ -646,6 +683,26 @@ int mglc_check(mglc_ctx* c, double* error_u, double* error_t) {
 int mglc_totals(mglc_ctx* c, double* mass, double* energy, double* heat) {
     if (!c || !c->kind) return MGLC_ERR_INVALID;
     if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial or mglc_load_state first");
+    if (c->p2d) return fail(c, MGLC_ERR_UNSUPPORTED, "not available for 2-D particle contexts");
+    if (c->l2d) {  // host sums of the 2-D fields
+        mglc_info in;
+        mglc_get_info(c, &in);
+        const size_t n = (size_t)in.nx * in.ny;
+        std::vector<double> r(n), u(n), v(n);
+        int rc = l2d_get_macros(c->l2d, r.data(), u.data(), v.data(), nullptr, c->err);
+        if (rc) return rc;
+        double m = 0.0, e = 0.0;
+        for (size_t q = 0; q < n; q++) {
+            m += r[q];
+            e += 0.5 * r[q] * (u[q] * u[q] + v[q] * v[q]);
+        }
+        if (mass) *mass = m;
+        if (energy) *energy = e;
+        if (heat) *heat = 0.0;
+        if (!std::isfinite(m) || !std::isfinite(e))
+            return fail(c, MGLC_ERR_NUMERIC, "non-finite totals at step %lld", l2d_itc(c->l2d));
+        return MGLC_OK;
+    }
     int rc = refresh_macros(c);
     if (rc) return rc;
     CK(launch_totals(c->n, c->rho, c->u, c->v, c->w, thermal(c) ? c->T : nullptr, c->partials,
@@ -838,6 +895,38 @@ int mglc_particle2d_create(const mglc_particle2d_params* p, const double* center
     c->snu = pp.snu;
     c->sq = pp.sq;
     return p2d_create(pp, centers, &c->p2d, c->err);
+}
+
+int mglc_lid2d_create(const mglc_lid2d_params* p, mglc_ctx** out) {
+    if (!p || !out) return MGLC_ERR_INVALID;
+    *out = nullptr;
+    mglc_ctx* c = new mglc_ctx();
+    *out = c;
+    if (p->total_nx < 2 || p->total_ny < 2 || (long long)p->total_nx * p->total_ny > (1LL << 31))
+        return fail(c, MGLC_ERR_INVALID, "the 2-D lattice needs 2 <= nx, ny and nx*ny <= 2^31");
+    if (p->precision != MGLC_FP64)
+        return fail(c, MGLC_ERR_UNSUPPORTED, "the 2-D lid cavity is built for MGLC_FP64");
+    if (!(p->reynolds > 0.0)) return fail(c, MGLC_ERR_INVALID, "reynolds must be positive");
+    L2Params lp{};
+    lp.nx = p->total_nx;
+    lp.ny = p->total_ny;
+    lp.u0 = p->u0;
+    lp.rho0 = p->rho0;
+    // commondata.f90:9,30
+    lp.tauf = p->u0 * (double)p->total_nx / p->reynolds * 3.0 + 0.5;
+    lp.snu = 1.0 / lp.tauf;
+    lp.sq = 8.0 * (2.0 * lp.tauf - 1.0) / (8.0 * lp.tauf - 1.0);
+    if (!(lp.tauf > 0.5)) return fail(c, MGLC_ERR_INVALID, "tauf must exceed 0.5");
+    c->kind = MGLC_KIND_LID2D;
+    c->form = FORM_FP64;
+    c->geom = {p->total_nx, p->total_ny, 1, (long long)p->total_nx * p->total_ny};
+    c->n = c->geom.plane;
+    c->u0 = p->u0;
+    c->rho0 = p->rho0;
+    c->tauf = lp.tauf;
+    c->snu = lp.snu;
+    c->sq = lp.sq;
+    return l2d_create(lp, &c->l2d, c->err);
 }
 
 int mglc_particle_state(mglc_ctx* c, double* xc, double* uc, double* omega, double* force,

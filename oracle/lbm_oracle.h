@@ -47,6 +47,24 @@ double orc_lid_run(int nx, int ny, int nz, double snu, double sq, double u0,
                    double* f, double* f_post, double* rho, double* u, double* v, double* w,
                    double* up, double* vp, double* wp);
 
+/* ---- D2Q9 lid-driven cavity (MPI/Lid_driven_cavity/fortran/2d/2d_revised/mpi_blocked),
+ * lid2d_oracle.c.  f(0:8,1:nx,1:ny), f_post(0:8,0:nx+1,0:ny+1), fields (1:nx,1:ny). ---- */
+void orc_lid2d_params(int total_nx, double reynolds, double u0, double* tauf, double* snu,
+                      double* sq);
+void orc_lid2d_initial(int nx, int ny, double u0, double rho0, double* f, double* rho,
+                       double* u, double* v);
+void orc_lid2d_collision(int nx, int ny, double snu, double sq, const double* f,
+                         const double* rho, const double* u, const double* v, double* f_post);
+void orc_lid2d_streaming(int nx, int ny, double* f, const double* f_post);
+void orc_lid2d_bounceback(int nx, int ny, double uwall, double* f, const double* f_post,
+                          const double* rho);
+void orc_lid2d_macro(int nx, int ny, const double* f, double* rho, double* u, double* v);
+double orc_lid2d_check(int nx, int ny, const double* u, const double* v, double* up,
+                       double* vp);
+double orc_lid2d_run(int nx, int ny, double snu, double sq, double u0, int nsteps,
+                     int check_every, int nthreads, double* f, double* f_post, double* rho,
+                     double* u, double* v, double* up, double* vp);
+
 /* ---- buoyancy-driven cavity (MPI/Buoyancy_driven_cavity/fortran/3d/bouyancy3d_mpi.F90) ---- */
 typedef struct {
     double tauf, viscosity, diffusivity, omega_rot, para_a, gbeta, snu, sq, qd, qnu;

@@ -26,7 +26,7 @@ LIB = os.path.join(BUILD, "liboracle.so")
 
 def build(force: bool = False) -> str:
     """Compile the oracle with gcc (-O2 -ffp-contract=off, OpenMP for the timed baseline)."""
-    srcs = [os.path.join(HERE, f) for f in ("lbm_oracle.c", "particle_oracle.c")]
+    srcs = [os.path.join(HERE, f) for f in ("lbm_oracle.c", "particle_oracle.c", "lid2d_oracle.c")]
     hdr = os.path.join(HERE, "lbm_oracle.h")
     os.makedirs(BUILD, exist_ok=True)
     newest = max(os.path.getmtime(x) for x in srcs + [hdr])
@@ -71,6 +71,12 @@ def _declare(L):
     L.orc_lid_check.restype = _D
     L.orc_lid_run.argtypes = [_I, _I, _I, _D, _D, _D, _I, _I, _I] + [_P] * 9
     L.orc_lid_run.restype = _D
+    L.orc_lid2d_params.argtypes = [_I, _D, _D, _P, _P, _P]
+    L.orc_lid2d_initial.argtypes = [_I, _I, _D, _D, _P, _P, _P, _P]
+    L.orc_lid2d_check.argtypes = [_I, _I, _P, _P, _P, _P]
+    L.orc_lid2d_check.restype = _D
+    L.orc_lid2d_run.argtypes = [_I, _I, _D, _D, _D, _I, _I, _I] + [_P] * 7
+    L.orc_lid2d_run.restype = _D
     TP = ctypes.POINTER(ThConsts)
     L.orc_th_params.argtypes = [_I, _D, _D, _D, _D, TP]
     L.orc_th_initial.argtypes = [_I, _I, _I, TP, _D, _D, _I, _I] + [_P] * 7
@@ -148,6 +154,35 @@ class LidOracle:
         s = self.s
         return lib().orc_lid_check(self.nx, self.ny, self.nz, _p(s.u), _p(s.v), _p(s.w),
                                    _p(s.up), _p(s.vp), _p(s.wp))
+
+
+class Lid2DOracle:
+    """Reference D2Q9 lid-driven cavity (2d_revised/mpi_blocked on one rank).
+    f has shape (ny, nx, 9), f_post (ny+2, nx+2, 9), fields (ny, nx)."""
+
+    def __init__(self, nx, ny, reynolds, u0, rho0=1.0, total_nx=None):
+        self.nx, self.ny, self.u0 = nx, ny, u0
+        t, s1, s2 = _D(), _D(), _D()
+        lib().orc_lid2d_params(total_nx or nx, reynolds, u0, ctypes.byref(t), ctypes.byref(s1),
+                               ctypes.byref(s2))
+        self.tauf, self.snu, self.sq = t.value, s1.value, s2.value
+        z = lambda *s: np.zeros(s, dtype=np.float64)
+        self.f, self.f_post = z(ny, nx, 9), z(ny + 2, nx + 2, 9)
+        self.rho, self.u, self.v, self.up, self.vp = (z(ny, nx) for _ in range(5))
+        lib().orc_lid2d_initial(nx, ny, u0, rho0, _p(self.f), _p(self.rho), _p(self.u),
+                                _p(self.v))
+        self.itc = 0
+
+    def run(self, nsteps: int, check_every: int = 0, nthreads: int = 1) -> float:
+        err = lib().orc_lid2d_run(self.nx, self.ny, self.snu, self.sq, self.u0, nsteps,
+                                  check_every, nthreads, _p(self.f), _p(self.f_post),
+                                  _p(self.rho), _p(self.u), _p(self.v), _p(self.up), _p(self.vp))
+        self.itc += nsteps
+        return err
+
+    def check(self) -> float:
+        return lib().orc_lid2d_check(self.nx, self.ny, _p(self.u), _p(self.v), _p(self.up),
+                                     _p(self.vp))
 
 
 def th_params(total_nz, rayleigh, prandtl, mach, ekman) -> ThConsts:

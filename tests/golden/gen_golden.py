@@ -30,6 +30,7 @@ from fortran_exec import FArr, Program, preprocess  # noqa: E402
 LID_DIR = "MPI/Lid_driven_cavity/fortran/3d/mpi_3d_blocked"
 PART_DIR = "MPI/Micro_particles/fortran/case4/mpi_particle"
 THERMAL_FILE = "MPI/Buoyancy_driven_cavity/fortran/3d/bouyancy3d_mpi.F90"
+LID2D_DIR = "MPI/Lid_driven_cavity/fortran/2d/2d_revised/mpi_blocked"
 
 
 def _mpi_single_rank(ndim=3):
@@ -137,6 +138,45 @@ def thermal_case(ref, nx, ny, nz, rayleigh, prandtl, mach, ekman, thot, tcold, t
     return out
 
 
+def lid2d_case(ref, nx, ny, reynolds, nsteps, check_every, u0=0.1):
+    """D2Q9 MRT lid-driven cavity on one rank (2d_revised/mpi_blocked,
+    main.f90:69-89 order; message_passing is a no-op on one rank)."""
+    p = Program()
+    p.overrides = {"total_nx": nx, "total_ny": ny, "reynolds": float(reynolds), "u0": float(u0),
+                   "rank": 0, "rank2d": 0, "num_process": 1, "comm2d": 0,
+                   "dims": FArr([(0, 1)], np.int64, 1), "coords": FArr([(0, 1)], np.int64, 0),
+                   "periods": FArr([(0, 1)], np.int64, 0)}
+    src = open(os.path.join(ref, LID2D_DIR, "commondata.f90")).read()
+    src = src.replace("data periods/2*.false./", "")  # overridden; MPI topology only
+    p.load_module(preprocess(src, p.defines))
+    p.ns.update({"nx": nx, "ny": ny})
+    for fn in ("initial.f90", "evolution.f90", "bounceback.f90"):
+        p.load_subroutines(preprocess(open(os.path.join(ref, LID2D_DIR, fn)).read(), p.defines))
+    names = ["initial", "collision", "streaming", "bounceback", "macro", "check"]
+    p.build(names)
+    p.call("initial")
+    ns = p.ns
+    out = {"nx": nx, "ny": ny, "reynolds": float(reynolds), "u0": float(u0),
+           "tauf": ns["tauf"], "snu": ns["snu"], "sq": ns["sq"], "nsteps": nsteps,
+           "check_every": check_every, "f0": ns["f"].numpy(), "u_init": ns["u"].numpy()}
+    errs = []
+    for itc in range(1, nsteps + 1):
+        ns["itc"] = itc
+        p.call("collision")
+        p.call("streaming")
+        p.call("bounceback")
+        p.call("macro")
+        if itc == 1:
+            out["f_step1"] = ns["f"].numpy()
+        if check_every and itc % check_every == 0:
+            p.call("check")
+            errs.append(ns["erroru"])
+    out.update(f=ns["f"].numpy(), rho=ns["rho"].numpy(), u=ns["u"].numpy(), v=ns["v"].numpy(),
+               erroru=np.array(errs))
+    assert not np.isnan(out["f"]).any(), "NaN in f: a halo value was read"
+    return out
+
+
 def particle2d_case(ref, nx, ny, radius0, gravity, rnd, nsteps):
     """case4 (D2Q9 moving circles) on one rank, main.F90:35-73 order.
 
@@ -193,6 +233,10 @@ CASES = {
     # case4 moving circles: two particles settling, mask updates and refills
     "particle2d_80x50": lambda ref: particle2d_case(ref, 80, 50, 6.0, 0.04,
                                                     [0.513, 0.47, 0.421, 0.552], nsteps=30),
+    # D2Q9 lid cavity: non-square grid, Re for tau ~ 0.6 and 1000 (tau ~ 0.52)
+    "lid2d_9x7": lambda ref: lid2d_case(ref, 9, 7, reynolds=30.0, nsteps=40, check_every=10),
+    "lid2d_12x10_re1000": lambda ref: lid2d_case(ref, 12, 10, reynolds=1000.0, nsteps=25,
+                                                 check_every=5),
     # lid: non-cubic grid to catch axis mix-ups; Re chosen for tau ~ 0.6
     "lid_7x6x5": lambda ref: lid_case(ref, 7, 6, 5, reynolds=21.0, nsteps=12, check_every=4),
     "lid_6x6x6_re400": lambda ref: lid_case(ref, 6, 6, 6, reynolds=400.0, nsteps=6,

@@ -60,3 +60,14 @@ def test_null_arguments(lib):
     assert lib.mglc_step(None, 1) == 1
     assert lib.mglc_last_error(None) == b"null context"
     lib.mglc_destroy(None)
+
+
+def test_lid2d_parameters_are_rejected_without_a_gpu(lib):
+    for args, rc_want, msg in (((1, 8, 400.0, 1.0, 0.1, 0), 1, b"nx, ny"),
+                               ((8, 8, -5.0, 1.0, 0.1, 0), 1, b"reynolds"),
+                               ((8, 8, 400.0, 1.0, 0.1, 1), 6, b"MGLC_FP64")):
+        ctx = ctypes.c_void_p()
+        p = capi.Lid2DParams(*args)
+        assert lib.mglc_lid2d_create(ctypes.byref(p), ctypes.byref(ctx)) == rc_want
+        assert msg in lib.mglc_last_error(ctx)
+        lib.mglc_destroy(ctx)

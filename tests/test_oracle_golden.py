@@ -85,3 +85,31 @@ def test_particle2d_oracle_matches_reference_statements(case):
     assert np.array_equal(g["om"][:, 2], d["omega"])
     assert np.array_equal(g["force"][:, :2], d["force"]) and np.array_equal(g["torque"][:, 2], d["torque"])
     assert g["rho_avg"] == float(d["rho_avg"])
+
+
+@pytest.mark.parametrize("case", _cases("lid2d_"))
+def test_lid2d_oracle_matches_reference_statements(case):
+    """D2Q9 MRT lid cavity (2d_revised/mpi_blocked): initial state, step 1,
+    the last step and every check() residual, bit for bit."""
+    d = np.load(os.path.join(GOLD, case + ".npz"))
+    o = O.Lid2DOracle(int(d["nx"]), int(d["ny"]), float(d["reynolds"]), float(d["u0"]))
+    assert (o.tauf, o.snu, o.sq) == (float(d["tauf"]), float(d["snu"]), float(d["sq"]))
+    assert np.array_equal(o.f, d["f0"]) and np.array_equal(o.u, d["u_init"])
+    errs = []
+    for it in range(1, int(d["nsteps"]) + 1):
+        o.run(1)
+        if it == 1:
+            assert np.array_equal(o.f, d["f_step1"])
+        if it % int(d["check_every"]) == 0:
+            errs.append(o.check())
+    for k in ("f", "rho", "u", "v"):
+        assert np.array_equal(getattr(o, k), d[k]), k
+    assert np.array_equal(np.array(errs), d["erroru"])
+
+
+def test_lid2d_oracle_threads_and_run_checks_agree():
+    a = O.Lid2DOracle(33, 21, 400.0, 0.1)
+    b = O.Lid2DOracle(33, 21, 400.0, 0.1)
+    ea = a.run(60, check_every=20, nthreads=1)
+    eb = b.run(60, check_every=20, nthreads=4)
+    assert np.array_equal(a.f, b.f) and ea == eb and 0 < ea < 1
