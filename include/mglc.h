@@ -137,6 +137,27 @@ typedef struct mglc_particle2d_params {
 } mglc_particle2d_params;
 int mglc_particle2d_create(const mglc_particle2d_params* p, const double* centers, int np,
                            mglc_ctx** out);
+/* D2Q9 circles carried through a shear flow: the reference's 2-D case1 step
+ * (MPI/Micro_particles/fortran/case1/mpi_complete, main.F90:34-67;
+ * commondata.F90:25-34 for the parameters).  Walls at j = 1 and j = ny move at
+ * -uwall and +uwall, x is periodic; every circle moves at the prescribed
+ * (u0, 0) with no rotation (stationaryFrame) or stays put while the walls move
+ * at -uwall-u0 and uwall-u0 (movingFrame); momentum-exchange force and torque
+ * are reported, no springs or gravity.  Quadratic (shipped) or linear
+ * interpolated bounce-back and refill.  FP64 in the reference's statement
+ * order: bitwise its results while circles stay clear of the periodic
+ * boundary (the reference's solid mask has no periodic images).  The refill
+ * uses the first circle's velocity for every circle, as the reference does.
+ * Verbs as for mglc_particle2d_create. */
+typedef struct mglc_shear2d_params {
+    int total_nx, total_ny;
+    double tauf, rho0, rho_solid, radius;
+    double u0, uwall;
+    int moving_frame;   /* 0: stationaryFrame (shipped), 1: movingFrame */
+    int linear;         /* 0: quadratic (shipped), 1: linear */
+} mglc_shear2d_params;
+int mglc_shear2d_create(const mglc_shear2d_params* p, const double* centers, int np,
+                        mglc_ctx** out);
 /* D2Q9 MRT lid-driven cavity: the reference's 2-D code
  * (MPI/Lid_driven_cavity/fortran/2d/2d_revised/mpi_blocked; commondata.f90:4-30
  * for the parameters, tauf = u0*total_nx/reynolds*3 + 0.5).  Lid along +x on

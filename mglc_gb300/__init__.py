@@ -6,9 +6,9 @@ Python host API that mirrors the reference's routines.
 """
 from .capi import FORMS, MglcError, lib  # noqa: F401
 from .cavity import (BuoyancyCavity, LidDrivenCavity, LidDrivenCavity2D, NuReMonitor,  # noqa: F401
-                     ParticleFlow, ParticleFlow2D)
+                     ParticleFlow, ParticleFlow2D, ShearFlow2D)
 from .serve import SolveServer  # noqa: F401
 
-__all__ = ["LidDrivenCavity", "LidDrivenCavity2D", "BuoyancyCavity", "ParticleFlow", "ParticleFlow2D", "NuReMonitor",
-           "SolveServer", "MglcError",
-           "FORMS", "lib"]
+__all__ = ["LidDrivenCavity", "LidDrivenCavity2D", "BuoyancyCavity", "ParticleFlow",
+           "ParticleFlow2D", "ShearFlow2D", "NuReMonitor", "SolveServer", "MglcError", "FORMS",
+           "lib"]

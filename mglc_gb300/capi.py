@@ -76,6 +76,11 @@ class Particle2DParams(ctypes.Structure):
                 ("threshold_particle", _D), ("stiff_particle", _D), ("q_bisection", _I)]
 
 
+class Shear2DParams(ctypes.Structure):
+    _fields_ = [("total_nx", _I), ("total_ny", _I), ("tauf", _D), ("rho0", _D), ("rho_solid", _D),
+                ("radius", _D), ("u0", _D), ("uwall", _D), ("moving_frame", _I), ("linear", _I)]
+
+
 class Lid2DParams(ctypes.Structure):
     _fields_ = [("total_nx", _I), ("total_ny", _I), ("reynolds", _D), ("rho0", _D), ("u0", _D),
                 ("precision", _I)]
@@ -97,6 +102,7 @@ SIGNATURES = {
     "mglc_particle_state": ([_VP, _VP, _VP, _VP, _VP, _VP], _I),
     "mglc_particle2d_create": ([ctypes.POINTER(Particle2DParams), _VP, _I, ctypes.POINTER(_VP)], _I),
     "mglc_lid2d_create": ([ctypes.POINTER(Lid2DParams), ctypes.POINTER(_VP)], _I),
+    "mglc_shear2d_create": ([ctypes.POINTER(Shear2DParams), _VP, _I, ctypes.POINTER(_VP)], _I),
     "mglc_get_mask": ([_VP, _VP], _I),
     "mglc_destroy": ([_VP], None),
     "mglc_last_error": ([_VP], ctypes.c_char_p),

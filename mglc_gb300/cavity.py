@@ -340,6 +340,30 @@ class ParticleFlow2D(_Solve):
         return m
 
 
+class ShearFlow2D(ParticleFlow2D):
+    """D2Q9 circles carried through a shear flow between walls moving at
+    -/+uwall, periodic in x: the reference's 2-D case1 step
+    (Micro_particles/fortran/case1/mpi_complete) with its commondata
+    parameters as defaults; bitwise the reference's statements.  Arrays are
+    (ny, nx)."""
+
+    def __init__(self, total_nx, total_ny, centers, radius, tauf=3.0 * (1.0 / 9.0) + 0.5,
+                 rho0=1.0, rho_solid=2.0, u0=0.02, uwall=0.1, moving_frame=False, linear=False):
+        _Solve.__init__(self)
+        c = np.ascontiguousarray(np.asarray(centers, dtype=np.float64).reshape(-1, 2))
+        self.np = len(c)
+        p = capi.Shear2DParams(total_nx, total_ny, float(tauf), float(rho0), float(rho_solid),
+                               float(radius), float(u0), float(uwall), int(bool(moving_frame)),
+                               int(bool(linear)))
+        ctx = _P()
+        rc = capi.lib().mglc_shear2d_create(ctypes.byref(p), c.ctypes.data, len(c), ctypes.byref(ctx))
+        self._ctx = ctx
+        if rc != capi.MGLC_OK:
+            msg = capi.lib().mglc_last_error(ctx).decode() if ctx else ""
+            self.close()
+            raise capi.MglcError(rc, msg)
+
+
 class LidDrivenCavity2D(_Solve):
     """D2Q9 MRT lid-driven cavity, the reference's 2-D code
     (Lid_driven_cavity/fortran/2d/2d_revised/mpi_blocked); bitwise the

@@ -897,6 +897,46 @@ int mglc_particle2d_create(const mglc_particle2d_params* p, const double* center
     return p2d_create(pp, centers, &c->p2d, c->err);
 }
 
+int mglc_shear2d_create(const mglc_shear2d_params* p, const double* centers, int np,
+                        mglc_ctx** out) {
+    if (!p || !out || (np > 0 && !centers)) return MGLC_ERR_INVALID;
+    *out = nullptr;
+    mglc_ctx* c = new mglc_ctx();
+    *out = c;
+    if (p->total_nx < 8 || p->total_ny < 8) return fail(c, MGLC_ERR_INVALID, "the 2-D lattice needs nx, ny >= 8");
+    if (np < 0 || np > 65536) return fail(c, MGLC_ERR_INVALID, "np must be in [0, 65536]");
+    if (!(p->tauf > 0.5)) return fail(c, MGLC_ERR_INVALID, "tauf must exceed 0.5");
+    if (!(p->radius > 0.5)) return fail(c, MGLC_ERR_INVALID, "radius must exceed 0.5");
+    for (int q = 0; q < np; q++) {
+        const double x = centers[2 * q], y = centers[2 * q + 1];
+        if (!(x - p->radius > 3.0 && x + p->radius < p->total_nx - 2.0 && y - p->radius > 1.0 &&
+              y + p->radius < p->total_ny))
+            return fail(c, MGLC_ERR_INVALID,
+                        "circle %d must fit between the walls and clear the periodic boundary", q);
+    }
+    P2Params pp{};
+    pp.nx = p->total_nx; pp.ny = p->total_ny; pp.np = np;
+    pp.q_bisection = 1;  // case1 calls calQ (particle_bounceback.F90:59)
+    pp.tauf = p->tauf; pp.rho0 = p->rho0; pp.rho_solid = p->rho_solid; pp.radius = p->radius;
+    // commondata.F90:32
+    pp.snu = 1.0 / p->tauf;
+    pp.sq = 8.0 * (2.0 * p->tauf - 1.0) / (8.0 * p->tauf - 1.0);
+    pp.pi = 4.0 * std::atan(1.0);
+    pp.variant = P2_SHEAR;
+    pp.moving_frame = p->moving_frame ? 1 : 0;
+    pp.linear = p->linear ? 1 : 0;
+    pp.u0 = p->u0;
+    pp.uwall = p->uwall;
+    c->kind = MGLC_KIND_PARTICLE2D;
+    c->form = FORM_FP64;
+    c->geom = {p->total_nx, p->total_ny, 1, (long long)p->total_nx * p->total_ny};
+    c->n = c->geom.plane;
+    c->tauf = pp.tauf;
+    c->snu = pp.snu;
+    c->sq = pp.sq;
+    return p2d_create(pp, centers, &c->p2d, c->err);
+}
+
 int mglc_lid2d_create(const mglc_lid2d_params* p, mglc_ctx** out) {
     if (!p || !out) return MGLC_ERR_INVALID;
     *out = nullptr;

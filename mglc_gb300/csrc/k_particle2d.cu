@@ -1,5 +1,9 @@
 // k_particle2d.cu -- D2Q9 moving circles, the reference's case4 step
-// (MPI/Micro_particles/fortran/case4/mpi_particle, main.F90:35-73):
+// (MPI/Micro_particles/fortran/case4/mpi_particle, main.F90:35-73) and, as the
+// P2_SHEAR variant, its case1 step (MPI/Micro_particles/fortran/case1/
+// mpi_complete, main.F90:34-67: a circle carried through the shear between
+// two moving walls, periodic in x, both compile-time frames and both
+// interpolation orders).  The case4 routines are:
 //
 //   collision (fluid.F90:14-64, solid nodes skipped), streaming from fluid
 //   sources (:97-108), four halfway-bounce-back walls (:115-161),
@@ -58,6 +62,14 @@ __device__ void fail(const D2& d, int code, int c) {
     if (atomicCAS(d.status, 0, code) == 0) d.status[1] = c;
 }
 
+// x index of a population read: case1 is periodic in x (its MPI exchange
+// fills the ghost columns with the periodic partner's values); case4 reads
+// its own ghost columns
+__device__ __forceinline__ int wxi(const D2& d, int i) {
+    if (d.p.variant != P2_SHEAR) return i;
+    return i < 1 ? i + d.p.nx : (i > d.p.nx ? i - d.p.nx : i);
+}
+
 // ------------------------------------------------------------------ fluid --
 __global__ void k2_collide(D2 d) {
     const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x, j = 1 + blockIdx.y;
@@ -66,8 +78,13 @@ __global__ void k2_collide(D2 d) {
     for (int a = 0; a < 9; a++) f[a] = F(d, a, i, j);
     const double rho = d.rho[IX(d, i, j)], u = d.u[IX(d, i, j)], v = d.v[IX(d, i, j)];
     m[0] = f[0] + f[1] + f[2] + f[3] + f[4] + f[5] + f[6] + f[7] + f[8];
-    m[1] = -4.0 * f[0] - f[1] - f[2] - f[3] - f[4] + 2.0 * f[5] + 2.0 * f[6] + 2.0 * f[7] + 2.0 * f[8];
-    m[2] = 4.0 * f[0] - 2.0 * f[1] - 2.0 * f[2] - 2.0 * f[3] - 2.0 * f[4] + f[5] + f[6] + f[7] + f[8];
+    if (d.p.variant == P2_SHEAR) {  // case1 fluid.F90:15-16 groups the sums
+        m[1] = -4.0 * f[0] - f[1] - f[2] - f[3] - f[4] + 2.0 * (f[5] + f[6] + f[7] + f[8]);
+        m[2] = 4.0 * f[0] - 2.0 * (f[1] + f[2] + f[3] + f[4]) + f[5] + f[6] + f[7] + f[8];
+    } else {
+        m[1] = -4.0 * f[0] - f[1] - f[2] - f[3] - f[4] + 2.0 * f[5] + 2.0 * f[6] + 2.0 * f[7] + 2.0 * f[8];
+        m[2] = 4.0 * f[0] - 2.0 * f[1] - 2.0 * f[2] - 2.0 * f[3] - 2.0 * f[4] + f[5] + f[6] + f[7] + f[8];
+    }
     m[3] = f[1] - f[3] + f[5] - f[6] - f[7] + f[8];
     m[4] = -2.0 * f[1] + 2.0 * f[3] + f[5] - f[6] - f[7] + f[8];
     m[5] = f[2] - f[4] + f[5] + f[6] - f[7] - f[8];
@@ -103,20 +120,43 @@ __global__ void k2_collide(D2 d) {
 }
 
 // pull from fluid sources only; every interior node (fluid or solid) receives
+// (case1 wraps the source column, fluid.F90:105-110)
 __global__ void k2_stream(D2 d) {
     const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x, j = 1 + blockIdx.y;
     if (i > d.p.nx || d.status[0]) return;
     for (int a = 0; a < 9; a++) {
-        const int ip = i - c_ex[a], jp = j - c_ey[a];
+        const int ip = wxi(d, i - c_ex[a]), jp = j - c_ey[a];
         if (d.ob[IX(d, ip, jp)] == 0) F(d, a, i, j) = FP(d, a, ip, jp);
     }
 }
 
-// the four walls; corner nodes receive the same value from both of their walls
+// the four walls; corner nodes receive the same value from both of their walls.
+// case1: only the two moving walls (fluid.F90:127-169)
 __global__ void k2_walls(D2 d) {
     const int t = 1 + blockIdx.x * blockDim.x + threadIdx.x;
     if (d.status[0]) return;
     const int nx = d.p.nx, ny = d.p.ny;
+    if (d.p.variant == P2_SHEAR) {
+        if (t > nx) return;
+        const double uw = d.p.uwall, u0 = d.p.u0;
+        F(d, 2, t, 1) = FP(d, 4, t, 1);
+        if (d.p.moving_frame) {
+            F(d, 5, t, 1) = FP(d, 7, t, 1) + (-uw - u0) / 6.0;
+            F(d, 6, t, 1) = FP(d, 8, t, 1) - (-uw - u0) / 6.0;
+        } else {
+            F(d, 5, t, 1) = FP(d, 7, t, 1) + (-uw) / 6.0;
+            F(d, 6, t, 1) = FP(d, 8, t, 1) - (-uw) / 6.0;
+        }
+        F(d, 4, t, ny) = FP(d, 2, t, ny);
+        if (d.p.moving_frame) {
+            F(d, 7, t, ny) = FP(d, 5, t, ny) - (uw - u0) / 6.0;
+            F(d, 8, t, ny) = FP(d, 6, t, ny) + (uw - u0) / 6.0;
+        } else {
+            F(d, 7, t, ny) = FP(d, 5, t, ny) - (uw) / 6.0;
+            F(d, 8, t, ny) = FP(d, 6, t, ny) + (uw) / 6.0;
+        }
+        return;
+    }
     if (t <= ny) {
         F(d, 1, 1, t) = FP(d, 3, 1, t);
         F(d, 5, 1, t) = FP(d, 7, 1, t);
@@ -218,15 +258,24 @@ __global__ void k2_ibb(D2 d) {
             const int ra = c_r[a];
             const double eu = c_ex[ra] * (d.uc[3 * c] + rot0) + c_ey[ra] * (d.uc[3 * c + 1] + rot1);
             const int ex = c_ex[a], ey = c_ey[a];
-            if (q < 0.5) {
+            const int i1 = wxi(d, i - ex), i2 = wxi(d, i - 2 * ex);
+            if (d.p.linear) {  // case1 particle_bounceback.F90:66-76
+                if (q < 0.5) {
+                    F(d, ra, i, j) = 2.0 * q * FP(d, a, i, j) + (1.0 - 2.0 * q) * FP(d, a, i1, j - ey) +
+                                     6.0 * c_w[a] * ravg * eu;
+                } else {
+                    F(d, ra, i, j) = 0.5 / q * FP(d, a, i, j) + (1.0 - 0.50 / q) * FP(d, ra, i, j) +
+                                     3.0 * c_w[a] * ravg / q * eu;
+                }
+            } else if (q < 0.5) {
                 F(d, ra, i, j) = q * (1.0 + 2.0 * q) * FP(d, a, i, j) +
-                                 (1.0 - 4.0 * q * q) * FP(d, a, i - ex, j - ey) -
-                                 q * (1.0 - 2.0 * q) * FP(d, a, i - 2 * ex, j - 2 * ey) +
+                                 (1.0 - 4.0 * q * q) * FP(d, a, i1, j - ey) -
+                                 q * (1.0 - 2.0 * q) * FP(d, a, i2, j - 2 * ey) +
                                  6.0 * c_w[a] * ravg * eu;
             } else {
                 F(d, ra, i, j) = FP(d, a, i, j) / q / (1.0 + 2.0 * q) +
                                  FP(d, ra, i, j) * (2.0 * q - 1.0) / q -
-                                 FP(d, ra, i - ex, j - ey) * (2.0 * q - 1.0) / (2.0 * q + 1.0) +
+                                 FP(d, ra, i1, j - ey) * (2.0 * q - 1.0) / (2.0 * q + 1.0) +
                                  6.0 * c_w[a] * ravg / q / (1.0 + 2.0 * q) * eu;
             }
         }
@@ -284,6 +333,15 @@ __global__ void k2_force(D2 d) {
                 ts = ts + T;
             }
         }
+    if (p.variant == P2_SHEAR) {  // case1 particle_force.F90:86-92: momentum exchange only
+        d.force[3 * c] = fs0;
+        d.force[3 * c + 1] = fs1;
+        d.force[3 * c + 2] = 0.0;
+        d.torque[3 * c] = 0.0;
+        d.torque[3 * c + 1] = 0.0;
+        d.torque[3 * c + 2] = ts;
+        return;
+    }
     const double gmag = fabs(-p.gravity);
     double fij[3] = {0.0, 0.0, 0.0}, fw[3] = {0.0, 0.0, 0.0};
     const double Rc = R0;
@@ -342,6 +400,14 @@ __global__ void k2_move(D2 d) {
         d.uco[3 * c + q] = d.uc[3 * c + q];
         d.omo[3 * c + q] = d.om[3 * c + q];
     }
+    if (p.variant == P2_SHEAR) {  // case1 particle_update.F90:21-35: prescribed motion
+        d.uc[3 * c] = p.moving_frame ? 0.0 : p.u0;
+        d.uc[3 * c + 1] = 0.0;
+        d.om[3 * c + 2] = 0.0;
+        d.xc[3 * c] = d.xco[3 * c] + d.uco[3 * c];
+        d.xc[3 * c + 1] = d.xco[3 * c + 1] + d.uco[3 * c + 1];
+        return;
+    }
     const double PI = p.pi, R0 = p.radius, r = p.radius;
     const double ax = d.force[3 * c] / PI / (R0 * R0) / p.rho_solid;
     const double ay = d.force[3 * c + 1] / PI / (R0 * R0) / p.rho_solid;
@@ -398,17 +464,27 @@ __global__ void k2_refill(D2 d) {
                     return;
                 }
                 const int e0 = c_ex[ec], e1 = c_ey[ec];
-                for (int a = 0; a < 9; a++)
-                    F(d, a, i, j) = 3.0 * F(d, a, i + e0, j + e1) - 3.0 * F(d, a, i + 2 * e0, j + 2 * e1) +
-                                    F(d, a, i + 3 * e0, j + 3 * e1);
+                const int i1 = wxi(d, i + e0), i2 = wxi(d, i + 2 * e0), i3 = wxi(d, i + 3 * e0);
+                for (int a = 0; a < 9; a++) {
+                    if (p.linear)  // case1 particle_update.F90:115-119
+                        F(d, a, i, j) = 2.0 * F(d, a, i1, j + e1) - F(d, a, i2, j + 2 * e1);
+                    else
+                        F(d, a, i, j) = 3.0 * F(d, a, i1, j + e1) - 3.0 * F(d, a, i2, j + 2 * e1) +
+                                        F(d, a, i3, j + 3 * e1);
+                }
                 double G[9], m[9];
                 for (int a = 0; a < 9; a++) G[a] = F(d, a, i, j);
                 m[0] = G[0] + G[1] + G[2] + G[3] + G[4] + G[5] + G[6] + G[7] + G[8];
                 m[1] = -4.0 * G[0] - G[1] - G[2] - G[3] - G[4] + 2.0 * G[5] + 2.0 * G[6] + 2.0 * G[7] + 2.0 * G[8];
                 m[2] = 4.0 * G[0] - 2.0 * G[1] - 2.0 * G[2] - 2.0 * G[3] - 2.0 * G[4] + G[5] + G[6] + G[7] + G[8];
-                m[3] = ra * (d.uc[3 * c] - (j - yc) * d.om[3 * c + 2]);
+                if (p.variant == P2_SHEAR) {  // case1 :130,132: the first circle's (Uc, Vc)
+                    m[3] = ra * d.uc[0];
+                    m[5] = ra * d.uc[1];
+                } else {
+                    m[3] = ra * (d.uc[3 * c] - (j - yc) * d.om[3 * c + 2]);
+                    m[5] = ra * (d.uc[3 * c + 1] + (i - xc) * d.om[3 * c + 2]);
+                }
                 m[4] = -2.0 * G[1] + 2.0 * G[3] + G[5] - G[6] - G[7] + G[8];
-                m[5] = ra * (d.uc[3 * c + 1] + (i - xc) * d.om[3 * c + 2]);
                 m[6] = -2.0 * G[2] + 2.0 * G[4] + G[5] + G[6] - G[7] - G[8];
                 m[7] = G[1] - G[2] + G[3] - G[4];
                 m[8] = G[5] - G[6] + G[7] - G[8];
@@ -449,16 +525,23 @@ __global__ void k2_init_fields(D2 d) {
     if (interior) {
         const bool solid = d.ob[IX(d, i, j)] == 1;
         d.rho[IX(d, i, j)] = solid ? d.p.rho_solid : d.p.rho0;
-        d.u[IX(d, i, j)] = 0.0;
+        double uu = 0.0;
+        if (d.p.variant == P2_SHEAR) {  // case1 initial.F90:96-127
+            const bool mf = d.p.moving_frame;
+            uu = mf ? 0.0 : d.p.u0;
+            if (j == 1) uu = mf ? -d.p.uwall - d.p.u0 : -d.p.uwall;
+            if (j == ny) uu = mf ? d.p.uwall - d.p.u0 : d.p.uwall;
+        }
+        d.u[IX(d, i, j)] = uu;
         d.v[IX(d, i, j)] = 0.0;
         if (!solid) {
-            const double uu = 0.0, vv = 0.0, us2 = uu * uu + vv * vv;
+            const double vv = 0.0, us2 = uu * uu + vv * vv;
             for (int a = 0; a < 9; a++) {
                 const double un = uu * c_ex[a] + vv * c_ey[a];
                 F(d, a, i, j) = c_w[a] * (1.0 + 3.0 * un + 4.5 * un * un - 1.5 * us2);
             }
         }
-    } else if (ghost) {
+    } else if (ghost && d.p.variant != P2_SHEAR) {  // case1 ghosts stay 0 (initial.F90:140)
         for (int a = 0; a < 9; a++) {
             F(d, a, i, j) = c_w[a] * d.p.rho0;
             FP(d, a, i, j) = c_w[a] * d.p.rho0;
@@ -582,6 +665,14 @@ int p2d_initial(P2Ctx* c, std::string& err) {
         if ((rc = ck(cudaMemcpyAsync(d.xco, d.xc, sizeof(double) * 3 * d.p.np, cudaMemcpyDeviceToDevice,
                                      c->s), "centres", err)))
             return rc;
+    }
+    if (d.p.variant == P2_SHEAR && d.p.np > 0) {  // case1 initial.F90:61-70
+        std::vector<double> uc(3 * (size_t)d.p.np, 0.0);
+        for (int q = 0; q < d.p.np; q++) uc[3 * q] = d.p.moving_frame ? 0.0 : d.p.u0;
+        if ((rc = ck(cudaMemcpyAsync(d.uc, uc.data(), sizeof(double) * uc.size(),
+                                     cudaMemcpyHostToDevice, c->s), "velocities", err)))
+            return rc;
+        if ((rc = ck(cudaStreamSynchronize(c->s), "velocities", err))) return rc;
     }
     k2_mask<<<dim3((d.p.nx + 2 + 127) / 128, d.p.ny + 2), 128, 0, c->s>>>(d, d.ob, false);
     k2_init_fields<<<dim3((d.p.nx + 6 + 127) / 128, d.p.ny + 6), 128, 0, c->s>>>(d);

@@ -34,7 +34,7 @@ __device__ __forceinline__ int next_tile_warp(unsigned* counter) {
 }
 
 // lid tiles: [0, lid_tiles); heated tiles: [lid_tiles, total_tiles)
-template <typename S, bool THERMAL>
+template <typename S, bool THERMAL, bool SR>
 __global__ void __launch_bounds__(256, THERMAL ? 2 : 3)
     k_serve_step(const ServeTable* __restrict__ tab, int kstep, unsigned* counter) {
     const int parity = kstep & 1;
@@ -57,13 +57,13 @@ __global__ void __launch_bounds__(256, THERMAL ? 2 : 3)
             const int i = idx % nx, r = r0 + idx / nx;
             const int j = r % ny, k = r / ny;
             if (!THERMAL)
-                lid_cell<S, false, unsigned>(i, j, k, fin, fout, sv.K, sv.plane, nullptr, nullptr,
-                                             nullptr, nullptr, sv.step0 + (unsigned)kstep);
+                lid_cell<S, false, unsigned, SR>(i, j, k, fin, fout, sv.K, sv.plane, nullptr,
+                                                 nullptr, nullptr, nullptr,
+                                                 sv.step0 + (unsigned)kstep);
             else
-                thermal_cell<S, false, false, unsigned>(i, j, k, fin, fout, sv.g[parity],
-                                                        sv.g[parity ^ 1], sv.F, sv.K, sv.plane,
-                                                        nullptr, nullptr, nullptr, nullptr,
-                                                        nullptr, 0u, sv.step0 + (unsigned)kstep);
+                thermal_cell<S, false, false, unsigned, SR>(
+                    i, j, k, fin, fout, sv.g[parity], sv.g[parity ^ 1], sv.F, sv.K, sv.plane,
+                    nullptr, nullptr, nullptr, nullptr, nullptr, 0u, sv.step0 + (unsigned)kstep);
         }
     }
 }
@@ -160,18 +160,21 @@ __global__ void k_serve_fields(ServeSolve sv, float* out) {
     }
 }
 
-template <typename S>
+template <typename S, bool SR>
 static void serve_go(int thermal, const ServeTable* tab, int k, unsigned* counter, int grid,
                      int block, cudaStream_t st) {
-    if (thermal) k_serve_step<S, true><<<grid, block, 0, st>>>(tab, k, counter);
-    else k_serve_step<S, false><<<grid, block, 0, st>>>(tab, k, counter);
+    if (thermal) k_serve_step<S, true, SR><<<grid, block, 0, st>>>(tab, k, counter);
+    else k_serve_step<S, false, SR><<<grid, block, 0, st>>>(tab, k, counter);
 }
 
-cudaError_t launch_serve_step(int form, int thermal, const ServeTable* tab, int k,
+cudaError_t launch_serve_step(int form, int sr, int thermal, const ServeTable* tab, int k,
                               unsigned* counter, int grid, int block, cudaStream_t st) {
-    if (form == FORM_FP16) serve_go<__half>(thermal, tab, k, counter, grid, block, st);
-    else if (form == FORM_FP32) serve_go<float>(thermal, tab, k, counter, grid, block, st);
-    else if (form == FORM_BF16) serve_go<__nv_bfloat16>(thermal, tab, k, counter, grid, block, st);
+    if (form == FORM_FP16 && sr) serve_go<__half, true>(thermal, tab, k, counter, grid, block, st);
+    else if (form == FORM_FP16) serve_go<__half, false>(thermal, tab, k, counter, grid, block, st);
+    else if (form == FORM_FP32) serve_go<float, false>(thermal, tab, k, counter, grid, block, st);
+    else if (form == FORM_BF16 && sr)
+        serve_go<__nv_bfloat16, true>(thermal, tab, k, counter, grid, block, st);
+    else if (form == FORM_BF16) serve_go<__nv_bfloat16, false>(thermal, tab, k, counter, grid, block, st);
     else return cudaErrorInvalidValue;
     return cudaGetLastError();
 }

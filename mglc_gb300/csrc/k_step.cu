@@ -18,14 +18,15 @@
 
 namespace mglc {
 
-template <typename S, bool FIRST, typename IDX>
+template <typename S, bool FIRST, typename IDX, bool SR>
 __global__ void __launch_bounds__(128)
     k_lid_step(const S* __restrict__ fin, S* __restrict__ fout, StepK<typename St<S>::C> K,
                IDX P, const double* __restrict__ mrho, const double* __restrict__ mu,
                const double* __restrict__ mv, const double* __restrict__ mw) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= K.nx) return;
-    lid_cell<S, FIRST, IDX>(i, blockIdx.y, blockIdx.z, fin, fout, K, P, mrho, mu, mv, mw, K.seed);
+    lid_cell<S, FIRST, IDX, SR>(i, blockIdx.y, blockIdx.z, fin, fout, K, P, mrho, mu, mv, mw,
+                                K.seed);
 }
 
 template <bool FIRST, typename IDX>
@@ -53,7 +54,7 @@ __global__ void __launch_bounds__(128, 4)
                                      mrho, mu, mv, mw, mT);
 }
 
-template <typename S, bool FIRST, bool ROT, typename IDX>
+template <typename S, bool FIRST, bool ROT, typename IDX, bool SR>
 __global__ void __launch_bounds__(128)
     k_thermal_step(const S* __restrict__ fin, S* __restrict__ fout,
                    const typename St<S>::C* __restrict__ gin, typename St<S>::C* __restrict__ gout,
@@ -63,8 +64,8 @@ __global__ void __launch_bounds__(128)
                    const double* __restrict__ mT) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= K.nx) return;
-    thermal_cell<S, FIRST, ROT, IDX>(i, blockIdx.y, blockIdx.z, fin, fout, gin, gout, F, K, P,
-                                     mrho, mu, mv, mw, mT, (IDX)2 * P, K.seed);
+    thermal_cell<S, FIRST, ROT, IDX, SR>(i, blockIdx.y, blockIdx.z, fin, fout, gin, gout, F, K,
+                                         P, mrho, mu, mv, mw, mT, (IDX)2 * P, K.seed);
 }
 
 // --------------------------------------------------------------- launch --
@@ -86,14 +87,20 @@ static cudaError_t lid_go(bool first, const void* fin, void* fout, const LidStep
     K.sr = a.sr;
     dim3 b = step_block(a.g.nx), gr = step_grid(a.g, b);
     const bool small = (long long)Q19 * a.g.plane < (1ll << 31);
-#define LID_LAUNCH(FI, IT)                                                                    \
-    k_lid_step<S, FI, IT><<<gr, b, 0, s>>>((const S*)fin, (S*)fout, K, (IT)a.g.plane, a.rho, a.u, \
-                                           a.v, a.w)
+    // stochastic rounding exists for the 16-bit storage types only
+    constexpr bool kHalf = sizeof(S) == 2;
+#define LID_LAUNCH(FI, IT, SRV)                                                          \
+    k_lid_step<S, FI, IT, SRV><<<gr, b, 0, s>>>((const S*)fin, (S*)fout, K, (IT)a.g.plane, \
+                                                a.rho, a.u, a.v, a.w)
+#define LID_SR(FI, IT)                                  \
+    if (kHalf && a.sr) LID_LAUNCH(FI, IT, kHalf);        \
+    else LID_LAUNCH(FI, IT, false);
     if (small) {
-        if (first) LID_LAUNCH(true, unsigned); else LID_LAUNCH(false, unsigned);
+        if (first) { LID_SR(true, unsigned) } else { LID_SR(false, unsigned) }
     } else {
-        if (first) LID_LAUNCH(true, long long); else LID_LAUNCH(false, long long);
+        if (first) { LID_SR(true, long long) } else { LID_SR(false, long long) }
     }
+#undef LID_SR
 #undef LID_LAUNCH
     return cudaGetLastError();
 }
@@ -145,10 +152,16 @@ static cudaError_t th_go(bool first, const void* fin, void* fout, const void* gi
     dim3 b = step_block(a.g.nx), gr = step_grid(a.g, b);
     const bool rot = a.omega_rot != 0.0;
     const bool small = (long long)Q19 * a.g.plane < (1ll << 31);
-#define TH_LAUNCH(FI, RO, IT)                                                                  \
-    k_thermal_step<S, FI, RO, IT><<<gr, b, 0, s>>>((const S*)fin, (S*)fout, (const C*)gin,     \
-                                                   (C*)gout, (C*)F, K, (IT)a.g.plane, a.rho,  \
-                                                   a.u, a.v, a.w, a.T)
+    constexpr bool kHalf = sizeof(S) == 2;
+#define TH_LAUNCH2(FI, RO, IT, SRV)                                                            \
+    k_thermal_step<S, FI, RO, IT, SRV><<<gr, b, 0, s>>>((const S*)fin, (S*)fout, (const C*)gin, \
+                                                        (C*)gout, (C*)F, K, (IT)a.g.plane,     \
+                                                        a.rho, a.u, a.v, a.w, a.T)
+#define TH_LAUNCH(FI, RO, IT)                                   \
+    do {                                                        \
+        if (kHalf && a.sr) TH_LAUNCH2(FI, RO, IT, kHalf);       \
+        else TH_LAUNCH2(FI, RO, IT, false);                     \
+    } while (0)
 #define TH_ROT(IT)                                       \
     if (first && rot) TH_LAUNCH(true, true, IT);          \
     else if (first) TH_LAUNCH(true, false, IT);           \
@@ -161,6 +174,7 @@ static cudaError_t th_go(bool first, const void* fin, void* fout, const void* gi
     }
 #undef TH_ROT
 #undef TH_LAUNCH
+#undef TH_LAUNCH2
     return cudaGetLastError();
 }
 

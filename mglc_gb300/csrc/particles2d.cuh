@@ -16,12 +16,20 @@
 
 namespace mglc {
 
+enum { P2_SETTLING = 0, P2_SHEAR = 1 };
+
 struct P2Params {
     int nx, ny, np;
     int q_bisection;  // 1: calQ (bisection), 0: calQ2 (ray-circle root)
     double tauf, rho0, rho_solid, radius, gravity;  // gravity: magnitude along -y
     double threshold_wall, stiff_wall, threshold_particle, stiff_particle;
     double snu, sq, pi;
+    // P2_SHEAR (case1/mpi_complete): circles carried at u0 through the shear
+    // between walls moving at -/+uwall, periodic x, no springs or gravity
+    int variant;       // P2_SETTLING (case4) or P2_SHEAR (case1)
+    int moving_frame;  // case1 movingFrame (1) or stationaryFrame (0)
+    int linear;        // case1 linear (1) or quadratic (0) bounce-back and refill
+    double u0, uwall;
 };
 
 struct P2Ctx;  // device state (k_particle2d.cu)

@@ -109,7 +109,7 @@ struct mglc_server {
     Arena arena;
     ServeTable* tab_host = nullptr;  // pinned
     ServeTable* tab_dev = nullptr;
-    unsigned* counters = nullptr;   // K + 1
+    unsigned* counters = nullptr;   // 2K + 24: per-step queue counters (iteration, autotuner)
     unsigned* resid_dev = nullptr;  // SERVE_MAX_ACTIVE
     unsigned* resid_host = nullptr; // pinned
     float* fields_dev = nullptr;    // staging for retired solves' fields
@@ -245,6 +245,22 @@ int upload_table(mglc_server* s) {
     return MGLC_OK;
 }
 
+// one step of every resident solve as an iteration issues it: the heated
+// kernel on the side stream beside the lid kernel, joined before the next step
+cudaError_t issue_step(mglc_server* s, int k, unsigned* c_lid, unsigned* c_heat, int grid,
+                       int blk) {
+    const int sr = s->sr ? 1 : 0;
+    cudaError_t e = cudaEventRecord(s->fork, s->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s->side, s->fork, 0);
+    if (e == cudaSuccess)
+        e = launch_serve_step(s->p.precision, sr, 1, s->tab_dev, k, c_heat, grid, blk, s->side);
+    if (e == cudaSuccess)
+        e = launch_serve_step(s->p.precision, sr, 0, s->tab_dev, k, c_lid, grid, blk, s->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(s->join, s->side);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s->stream, s->join, 0);
+    return e;
+}
+
 int build_graph(mglc_server* s) {
     if (s->graph) {
         cudaGraphExecDestroy(s->graph);
@@ -257,17 +273,8 @@ int build_graph(mglc_server* s) {
     // counters: [0, K) lid steps, [K, 2K) heated steps, 2K residual
     cudaError_t e = cudaMemsetAsync(s->counters, 0, sizeof(unsigned) * (2 * K + 1), s->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(s->resid_dev, 0, sizeof(unsigned) * SERVE_MAX_ACTIVE, s->stream);
-    for (int k = 0; k < K && e == cudaSuccess; k++) {
-        // the heated branch runs beside the lid branch: fork and join per step
-        e = cudaEventRecord(s->fork, s->stream);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(s->side, s->fork, 0);
-        if (e == cudaSuccess)
-            e = launch_serve_step(s->p.precision, 1, s->tab_dev, k, s->counters + K + k, grid, s->block, s->side);
-        if (e == cudaSuccess)
-            e = launch_serve_step(s->p.precision, 0, s->tab_dev, k, s->counters + k, grid, s->block, s->stream);
-        if (e == cudaSuccess) e = cudaEventRecord(s->join, s->side);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(s->stream, s->join, 0);
-    }
+    for (int k = 0; k < K && e == cudaSuccess; k++)
+        e = issue_step(s, k, s->counters + k, s->counters + K + k, grid, s->block);
     if (e == cudaSuccess)
         e = launch_serve_resid(s->p.precision, s->tab_dev, s->counters + 2 * K, s->resid_dev, K, grid,
                                s->block, s->stream);
@@ -286,8 +293,10 @@ int build_graph(mglc_server* s) {
     return MGLC_OK;
 }
 
-// Choose threads per CTA, rows per tile and CTAs per SM by timing a few steps
-// of a synthetic mix (one solve of each size, lid and heated alternating).
+// Choose threads per CTA, rows per tile and CTAs per SM by timing steps of a
+// synthetic mix (one solve of each size, lid and heated alternating), issued
+// as an iteration issues them (heated beside lid): per candidate two warm-up
+// steps and eight timed ones, the best of two passes over all candidates.
 int autotune(mglc_server* s) {
     static const int sizes[] = {32, 48, 64, 96, 128};
     std::vector<Req> mix;
@@ -325,34 +334,33 @@ int autotune(mglc_server* s) {
     const int blocks[] = {128, 256};
     const int rowsv[] = {1, 2, 4, 8};
     const int ctas[] = {2, 4, 8};
-    for (int blk : blocks)
-        for (int rw : rowsv)
-            for (int cp : ctas) {
-                s->block = blk;
-                s->rows = rw;
-                s->ctas_per_sm = cp;
-                if (upload_table(s)) break;
-                cudaStreamSynchronize(s->stream);  // the pinned table is rewritten next round
-                const int grid = s->nsm * cp;
-                cudaMemsetAsync(s->counters, 0, sizeof(unsigned) * 10, s->stream);
-                launch_serve_step(s->p.precision, 0, s->tab_dev, 0, s->counters, grid, blk, s->stream);
-                launch_serve_step(s->p.precision, 1, s->tab_dev, 0, s->counters + 5, grid, blk, s->stream);
-                cudaEventRecord(a, s->stream);
-                for (int k = 0; k < 4; k++) {
-                    launch_serve_step(s->p.precision, 0, s->tab_dev, k + 1, s->counters + 1 + k, grid, blk, s->stream);
-                    launch_serve_step(s->p.precision, 1, s->tab_dev, k + 1, s->counters + 6 + k, grid, blk, s->stream);
+    constexpr int kWarm = 2, kTimed = 8, kSteps = kWarm + kTimed;  // counters: 2 * kSteps
+    for (int pass = 0; pass < 2; pass++)
+        for (int blk : blocks)
+            for (int rw : rowsv)
+                for (int cp : ctas) {
+                    s->block = blk;
+                    s->rows = rw;
+                    s->ctas_per_sm = cp;
+                    if (upload_table(s)) break;
+                    cudaStreamSynchronize(s->stream);  // the pinned table is rewritten next round
+                    const int grid = s->nsm * cp;
+                    cudaMemsetAsync(s->counters, 0, sizeof(unsigned) * 2 * kSteps, s->stream);
+                    for (int k = 0; k < kSteps; k++) {
+                        if (k == kWarm) cudaEventRecord(a, s->stream);
+                        issue_step(s, k, s->counters + k, s->counters + kSteps + k, grid, blk);
+                    }
+                    cudaEventRecord(b, s->stream);
+                    cudaEventSynchronize(b);
+                    float ms = 0;
+                    cudaEventElapsedTime(&ms, a, b);
+                    if (ms < best) {
+                        best = ms;
+                        bb = blk;
+                        br = rw;
+                        bc = cp;
+                    }
                 }
-                cudaEventRecord(b, s->stream);
-                cudaEventSynchronize(b);
-                float ms = 0;
-                cudaEventElapsedTime(&ms, a, b);
-                if (ms < best) {
-                    best = ms;
-                    bb = blk;
-                    br = rw;
-                    bc = cp;
-                }
-            }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     SCK(cudaStreamSynchronize(s->stream), "autotune");
@@ -422,7 +430,8 @@ int mglc_server_create(const mglc_server_params* p, mglc_server** out) {
     SCK(cudaMallocHost((void**)&s->tab_host, sizeof(ServeTable)), "pinned table");
     std::memset(s->tab_host, 0, sizeof(ServeTable));
     SCK(cudaMalloc((void**)&s->tab_dev, sizeof(ServeTable)), "device table");
-    SCK(cudaMalloc((void**)&s->counters, sizeof(unsigned) * (2 * p->steps_per_iteration + 8)), "counters");
+    SCK(cudaMalloc((void**)&s->counters, sizeof(unsigned) * (2 * p->steps_per_iteration + 24)),
+        "counters");
     SCK(cudaMalloc((void**)&s->resid_dev, sizeof(unsigned) * SERVE_MAX_ACTIVE), "residuals");
     SCK(cudaMallocHost((void**)&s->resid_host, sizeof(unsigned) * SERVE_MAX_ACTIVE), "pinned residuals");
     SCK(cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming), "event");

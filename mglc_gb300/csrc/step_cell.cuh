@@ -137,8 +137,10 @@ __device__ __forceinline__ unsigned sr_pop(unsigned h, int q) {
 // ------------------------------------------------------------ lid kernel --
 // IDX: 32-bit element indices when Q*cells < 2^31, 64-bit otherwise.
 // lid_cell_from: collide and push one cell whose 19 stored populations are
-// already in registers (raw); lid_cell: load them, then the same.
-template <typename S, bool FIRST, typename IDX>
+// already in registers (raw); lid_cell: load them, then the same.  SR: the
+// 16-bit stores round stochastically (a compile-time choice, so the
+// round-to-nearest kernels carry none of its code).
+template <typename S, bool FIRST, typename IDX, bool SR = false>
 __device__ __forceinline__ void lid_cell_from(int i, int j, int k, const S (&raw)[Q19],
                                               S* __restrict__ fout,
                                               const StepK<typename St<S>::C>& K, IDX P,
@@ -174,7 +176,7 @@ __device__ __forceinline__ void lid_cell_from(int i, int j, int k, const S (&raw
     const unsigned h0 = sr_cell((unsigned)cell, seed);
     // stochastic rounding for finite cells; a NaN or infinite cell rounds to
     // nearest so that the non-finite values propagate unchanged
-    const bool sr = K.sr && isfinite(rho + ux + uy + uz);
+    const bool sr = SR && isfinite(rho + ux + uy + uz);
     auto put = [&](S* p, C v, int q) {
         if (sr) St<S>::st_sr(p, v, K.scale, sr_pop(h0, q));
         else St<S>::st(p, v, K.scale);
@@ -212,7 +214,7 @@ __device__ __forceinline__ void lid_load(int i, int j, int k, const S* __restric
     for (int q = 0; q < Q19; q++) raw[q] = St<S>::raw(fin + ((IDX)q * P + cell));
 }
 
-template <typename S, bool FIRST, typename IDX>
+template <typename S, bool FIRST, typename IDX, bool SR = false>
 __device__ __forceinline__ void lid_cell(int i, int j, int k, const S* __restrict__ fin,
                                          S* __restrict__ fout, const StepK<typename St<S>::C>& K,
                                          IDX P, const double* __restrict__ mrho,
@@ -221,7 +223,7 @@ __device__ __forceinline__ void lid_cell(int i, int j, int k, const S* __restric
                                          const double* __restrict__ mw, unsigned seed) {
     S raw[Q19];  // every load is issued before the first conversion
     lid_load<S, IDX>(i, j, k, fin, K.nx, K.ny, P, raw);
-    lid_cell_from<S, FIRST, IDX>(i, j, k, raw, fout, K, P, mrho, mu, mv, mw, seed);
+    lid_cell_from<S, FIRST, IDX, SR>(i, j, k, raw, fout, K, P, mrho, mu, mv, mw, seed);
 }
 
 // ------------------------------------------------------ lid kernel, FX64 --
@@ -313,7 +315,7 @@ __device__ __forceinline__ void lid_cell_fx(int i, int j, int k, const double* _
 // Temperature populations are kept in the arithmetic type (FP64, or FP32 for
 // the reduced forms): g_0 ~ 0.7 T has a 16-bit ulp (~2e-4) far above the
 // per-step diffusive increments, so 16-bit g would stagnate.
-template <typename S, bool FIRST, bool ROT, typename IDX>
+template <typename S, bool FIRST, bool ROT, typename IDX, bool SR = false>
 __device__ __forceinline__ void thermal_cell(
     int i, int j, int k, const S* __restrict__ fin, S* __restrict__ fout,
     const typename St<S>::C* __restrict__ gin, typename St<S>::C* __restrict__ gout,
@@ -370,7 +372,7 @@ __device__ __forceinline__ void thermal_cell(
     const IDX sy = (IDX)nx, sz = (IDX)nx * (IDX)ny;
     const unsigned bm = face_mask(i, j, k, nx, ny, nz);
     const unsigned h0 = sr_cell((unsigned)cell, seed);
-    const bool sr = K.sr && isfinite(rho + ux + uy + uz + temp);
+    const bool sr = SR && isfinite(rho + ux + uy + uz + temp);
     auto put = [&](S* p, C v, int q) {
         if (sr) St<S>::st_sr(p, v, K.scale, sr_pop(h0, q));
         else St<S>::st(p, v, K.scale);

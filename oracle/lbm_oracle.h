@@ -129,6 +129,24 @@ void orc_pt_get(const orc_particles* s, double* f, double* f_post, double* rho, 
                 double* force, double* torque, double* rho_avg);
 void orc_pt_destroy(orc_particles* s);
 
+/* ---- circles in shear flow, periodic x (MPI/Micro_particles/fortran/case1/mpi_complete),
+ * shear2d_oracle.c.  centers = np x (x, y); outputs (ny, nx) fields, np x 2 vectors. ---- */
+typedef struct {
+    int nx, ny, np;
+    int moving_frame; /* 0: stationaryFrame (the shipped build), 1: movingFrame */
+    int linear;       /* 0: quadratic IBB and refill (shipped), 1: linear */
+    double tauf, rho0, rho_solid, radius;
+    double u0;        /* carrier speed of the circles (stationary frame) */
+    double uwall;     /* wall speeds -uwall (j = 1) and +uwall (j = ny) */
+} orc_shear_params;
+typedef struct orc_shear orc_shear;
+orc_shear* orc_shear_create(const orc_shear_params* p, const double* centers);
+/* returns 0, or 1 no owning circle, 2 q out of range, 5 no refill direction */
+int orc_shear_step(orc_shear* s, int nsteps);
+void orc_shear_get(const orc_shear* s, double* f, double* rho, double* u, double* v, int* obst,
+                   double* xc, double* uc, double* force, double* torque, double* rho_avg);
+void orc_shear_destroy(orc_shear* s);
+
 #ifdef __cplusplus
 }
 #endif

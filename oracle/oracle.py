@@ -26,7 +26,7 @@ LIB = os.path.join(BUILD, "liboracle.so")
 
 def build(force: bool = False) -> str:
     """Compile the oracle with gcc (-O2 -ffp-contract=off, OpenMP for the timed baseline)."""
-    srcs = [os.path.join(HERE, f) for f in ("lbm_oracle.c", "particle_oracle.c", "lid2d_oracle.c")]
+    srcs = [os.path.join(HERE, f) for f in ("lbm_oracle.c", "particle_oracle.c", "lid2d_oracle.c", "shear2d_oracle.c")]
     hdr = os.path.join(HERE, "lbm_oracle.h")
     os.makedirs(BUILD, exist_ok=True)
     newest = max(os.path.getmtime(x) for x in srcs + [hdr])
@@ -60,6 +60,12 @@ class ThConsts(ctypes.Structure):
                  "snu", "sq", "qd", "qnu")]
 
 
+class ShearParams(ctypes.Structure):
+    _fields_ = [("nx", _I), ("ny", _I), ("np", _I), ("moving_frame", _I), ("linear", _I),
+                ("tauf", _D), ("rho0", _D), ("rho_solid", _D), ("radius", _D), ("u0", _D),
+                ("uwall", _D)]
+
+
 def _declare(L):
     L.orc_lid_params.argtypes = [_I, _D, _D, _P, _P, _P]
     L.orc_lid_initial.argtypes = [_I, _I, _I, _D, _D, _I, _P, _P, _P, _P, _P]
@@ -77,6 +83,11 @@ def _declare(L):
     L.orc_lid2d_check.restype = _D
     L.orc_lid2d_run.argtypes = [_I, _I, _D, _D, _D, _I, _I, _I] + [_P] * 7
     L.orc_lid2d_run.restype = _D
+    L.orc_shear_create.argtypes = [ctypes.POINTER(ShearParams), _P]
+    L.orc_shear_create.restype = ctypes.c_void_p
+    L.orc_shear_step.argtypes = [ctypes.c_void_p, _I]
+    L.orc_shear_get.argtypes = [ctypes.c_void_p, _P, _P, _P, _P, ctypes.c_void_p, _P, _P, _P, _P, _P]
+    L.orc_shear_destroy.argtypes = [ctypes.c_void_p]
     TP = ctypes.POINTER(ThConsts)
     L.orc_th_params.argtypes = [_I, _D, _D, _D, _D, TP]
     L.orc_th_initial.argtypes = [_I, _I, _I, TP, _D, _D, _I, _I] + [_P] * 7
@@ -277,5 +288,41 @@ class ParticleOracle:
     def __del__(self):
         try:
             lib().orc_pt_destroy(self._s)
+        except Exception:
+            pass
+
+
+class ShearOracle:
+    """case1 (circles in shear flow, periodic x) on one rank.  Fields (ny, nx),
+    f (ny, nx, 9), per-circle vectors (np, 2)."""
+
+    def __init__(self, centers, nx, ny, radius, tauf=3.0 * (1.0 / 9.0) + 0.5, rho0=1.0,
+                 rho_solid=2.0, u0=0.02, uwall=0.1, moving_frame=False, linear=False):
+        c = np.ascontiguousarray(np.asarray(centers, dtype=np.float64).reshape(-1, 2))
+        self.nx, self.ny, self.np = nx, ny, len(c)
+        self.p = ShearParams(nx, ny, len(c), int(bool(moving_frame)), int(bool(linear)),
+                             float(tauf), float(rho0), float(rho_solid), float(radius), float(u0),
+                             float(uwall))
+        self.h = lib().orc_shear_create(ctypes.byref(self.p), _p(c))
+
+    def step(self, n=1) -> int:
+        return lib().orc_shear_step(self.h, n)
+
+    def get(self):
+        nx, ny, k = self.nx, self.ny, max(self.np, 1)
+        o = {"f": np.zeros((ny, nx, 9)), "rho": np.zeros((ny, nx)), "u": np.zeros((ny, nx)),
+             "v": np.zeros((ny, nx)), "obst": np.zeros((ny, nx), dtype=np.int32),
+             "xc": np.zeros((k, 2)), "uc": np.zeros((k, 2)), "force": np.zeros((k, 2)),
+             "torque": np.zeros(k)}
+        ra = ctypes.c_double()
+        lib().orc_shear_get(self.h, _p(o["f"]), _p(o["rho"]), _p(o["u"]), _p(o["v"]),
+                            o["obst"].ctypes.data, _p(o["xc"]), _p(o["uc"]), _p(o["force"]),
+                            _p(o["torque"]), ctypes.byref(ra))
+        o["rho_avg"] = ra.value
+        return o
+
+    def __del__(self):
+        try:
+            lib().orc_shear_destroy(self.h)
         except Exception:
             pass

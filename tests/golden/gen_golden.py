@@ -31,6 +31,7 @@ LID_DIR = "MPI/Lid_driven_cavity/fortran/3d/mpi_3d_blocked"
 PART_DIR = "MPI/Micro_particles/fortran/case4/mpi_particle"
 THERMAL_FILE = "MPI/Buoyancy_driven_cavity/fortran/3d/bouyancy3d_mpi.F90"
 LID2D_DIR = "MPI/Lid_driven_cavity/fortran/2d/2d_revised/mpi_blocked"
+SHEAR_DIR = "MPI/Micro_particles/fortran/case1/mpi_complete"
 
 
 def _mpi_single_rank(ndim=3):
@@ -177,6 +178,64 @@ def lid2d_case(ref, nx, ny, reynolds, nsteps, check_every, u0=0.1):
     return out
 
 
+def shear2d_case(ref, nx, ny, radius0, xc, yc, nsteps, frame="stationaryFrame",
+                 interp="quadratic", u0=None, uwall=None):
+    """case1: one circle carried through a shear flow between walls moving at
+    -/+Uwall, periodic in x, on one rank (main.F90:36-72 order).  The centre
+    (initial.F90:59-60) is replaced by (xc, yc) for the smaller grid."""
+    p = Program()
+    p.defines |= {frame, interp}
+    ov = {"total_nx": nx, "total_ny": ny, "radius0": float(radius0), "rank": 0, "rank2d": 0,
+          "num_process": 1, "comm2d": 0,
+          "dims": FArr([(0, 1)], np.int64, 1), "coords": FArr([(0, 1)], np.int64, 0),
+          "periods": FArr([(0, 1)], np.int64, 0)}
+    if u0 is not None:
+        ov["u0"] = float(u0)
+    if uwall is not None:
+        ov["uwall"] = float(uwall)
+    p.overrides = ov
+    src = open(os.path.join(ref, SHEAR_DIR, "commondata.F90")).read()
+    src = src.replace("data periods/.true., .false./", "")  # overridden; MPI topology only
+    p.load_module(preprocess(src, p.defines))
+    p.ns.update({"nx": nx, "ny": ny, "i_start_global": 0, "j_start_global": 0})
+    ini = open(os.path.join(ref, SHEAR_DIR, "initial.F90")).read()
+    lit = lambda x: repr(float(x)) + "d0"  # plain decimals (no exponent) for these centres
+    ini = ini.replace("xCenter(1) = 30.0d0", "xCenter(1) = " + lit(xc))
+    ini = ini.replace("yCenter(1) = 54.0d0", "yCenter(1) = " + lit(yc))
+    for text in (open(os.path.join(ref, SHEAR_DIR, "freeall.F90")).read(), ini,
+                 *(open(os.path.join(ref, SHEAR_DIR, fn)).read() for fn in
+                   ("fluid.F90", "particle_bounceback.F90", "particle_force.F90",
+                    "particle_update.F90"))):
+        p.load_subroutines(preprocess(text, p.defines))
+    names = ["allocate_all", "initial", "collision", "streaming", "bounceback",
+             "bounceback_particle", "calq", "macro", "calforce", "updatecenter"]
+    p.build(names)
+    p.call("allocate_all")
+    p.call("initial")
+    ns = p.ns
+    out = {"nx": nx, "ny": ny, "radius0": float(radius0), "nsteps": nsteps, "frame": frame,
+           "interp": interp, "tauf": ns["tauf"], "rhosolid": ns["rhosolid"], "u0": ns["u0"],
+           "uwall": ns["uwall"], "xc0": np.array([[float(xc), float(yc)]])}
+    for itc in range(nsteps):
+        p.call("collision")
+        p.call("streaming")
+        p.call("bounceback")
+        p.call("bounceback_particle")
+        p.call("macro")
+        p.call("calforce")
+        ns["itc"] = ns["itc"] + 1
+        p.call("updatecenter")
+    f = ns["f"].numpy()            # (ny+6, nx+6, 9) with lower bound -2
+    out.update(f=f[3:3 + ny, 3:3 + nx, :], rho=ns["rho"].numpy(), u=ns["u"].numpy(),
+               v=ns["v"].numpy(), obst=ns["obst"].numpy()[1:1 + ny, 1:1 + nx],
+               xc=np.stack([ns["xcenter"].numpy(), ns["ycenter"].numpy()], axis=1),
+               uc=np.stack([ns["uc"].numpy(), ns["vc"].numpy()], axis=1),
+               force=np.stack([ns["walltotalforcex"].numpy(), ns["walltotalforcey"].numpy()], axis=1),
+               torque=ns["totaltorque"].numpy(), rho_avg=ns["rhoavg"])
+    assert not np.isnan(out["f"]).any()
+    return out
+
+
 def particle2d_case(ref, nx, ny, radius0, gravity, rnd, nsteps):
     """case4 (D2Q9 moving circles) on one rank, main.F90:35-73 order.
 
@@ -237,6 +296,13 @@ CASES = {
     "lid2d_9x7": lambda ref: lid2d_case(ref, 9, 7, reynolds=30.0, nsteps=40, check_every=10),
     "lid2d_12x10_re1000": lambda ref: lid2d_case(ref, 12, 10, reynolds=1000.0, nsteps=25,
                                                  check_every=5),
+    # case1 circle in shear flow: the shipped build (stationary frame, quadratic
+    # IBB), linear IBB/refill with a faster carrier (more refills), moving frame
+    "shear2d_64x40_sq": lambda ref: shear2d_case(ref, 64, 40, 6.25, 24.0, 20.6, nsteps=40),
+    "shear2d_56x36_sl": lambda ref: shear2d_case(ref, 56, 36, 5.5, 20.0, 17.3, nsteps=40,
+                                                 interp="linear", u0=0.05),
+    "shear2d_48x32_mq": lambda ref: shear2d_case(ref, 48, 32, 5.0, 18.0, 15.7, nsteps=30,
+                                                 frame="movingFrame"),
     # lid: non-cubic grid to catch axis mix-ups; Re chosen for tau ~ 0.6
     "lid_7x6x5": lambda ref: lid_case(ref, 7, 6, 5, reynolds=21.0, nsteps=12, check_every=4),
     "lid_6x6x6_re400": lambda ref: lid_case(ref, 6, 6, 6, reynolds=400.0, nsteps=6,

@@ -71,3 +71,17 @@ def test_lid2d_parameters_are_rejected_without_a_gpu(lib):
         assert lib.mglc_lid2d_create(ctypes.byref(p), ctypes.byref(ctx)) == rc_want
         assert msg in lib.mglc_last_error(ctx)
         lib.mglc_destroy(ctx)
+
+
+def test_shear2d_parameters_are_rejected_without_a_gpu(lib):
+    import numpy as np
+    for args, centers, msg in (((4, 40, 0.8, 1.0, 2.0, 5.0, 0.02, 0.1, 0, 0), [[20.0, 20.0]], b"nx, ny"),
+                               ((64, 40, 0.5, 1.0, 2.0, 5.0, 0.02, 0.1, 0, 0), [[20.0, 20.0]], b"tauf"),
+                               ((64, 40, 0.8, 1.0, 2.0, 5.0, 0.02, 0.1, 0, 0), [[4.0, 20.0]],
+                                b"periodic boundary")):
+        ctx = ctypes.c_void_p()
+        c = np.ascontiguousarray(centers, dtype=np.float64)
+        p = capi.Shear2DParams(*args)
+        assert lib.mglc_shear2d_create(ctypes.byref(p), c.ctypes.data, len(c), ctypes.byref(ctx)) == 1
+        assert msg in lib.mglc_last_error(ctx)
+        lib.mglc_destroy(ctx)

@@ -113,3 +113,23 @@ def test_lid2d_oracle_threads_and_run_checks_agree():
     ea = a.run(60, check_every=20, nthreads=1)
     eb = b.run(60, check_every=20, nthreads=4)
     assert np.array_equal(a.f, b.f) and ea == eb and 0 < ea < 1
+
+
+def _shear_oracle(d):
+    return O.ShearOracle(d["xc0"], int(d["nx"]), int(d["ny"]), float(d["radius0"]),
+                         tauf=float(d["tauf"]), rho_solid=float(d["rhosolid"]), u0=float(d["u0"]),
+                         uwall=float(d["uwall"]), moving_frame=str(d["frame"]) == "movingFrame",
+                         linear=str(d["interp"]) == "linear")
+
+
+@pytest.mark.parametrize("case", _cases("shear2d_"))
+def test_shear2d_oracle_matches_reference_statements(case):
+    """case1 circle in shear flow (stationary/moving frame, quadratic/linear):
+    populations, fields, mask, centre, velocity, force and torque bit for bit."""
+    d = np.load(os.path.join(GOLD, case + ".npz"))
+    o = _shear_oracle(d)
+    assert o.step(int(d["nsteps"])) == 0
+    g = o.get()
+    for k in ("f", "rho", "u", "v", "obst", "xc", "uc", "force", "torque"):
+        assert np.array_equal(g[k], d[k]), k
+    assert g["rho_avg"] == float(d["rho_avg"])
