@@ -44,6 +44,12 @@ module mglc_iface
         integer(c_int) :: q_bisection
     end type
 
+    type, bind(C) :: mglc_shear2d_params
+        integer(c_int) :: total_nx, total_ny
+        real(c_double) :: tauf, rho0, rho_solid, radius, u0, uwall
+        integer(c_int) :: moving_frame, linear
+    end type
+
     type, bind(C) :: mglc_lid2d_params
         integer(c_int) :: total_nx, total_ny
         real(c_double) :: reynolds, rho0, u0
@@ -133,6 +139,15 @@ module mglc_iface
                 bind(C, name="mglc_particle2d_create")
             import :: c_int, c_ptr, c_double, mglc_particle2d_params
             type(mglc_particle2d_params), intent(in) :: p
+            real(c_double), intent(in) :: centers(*)
+            integer(c_int), value :: np
+            type(c_ptr), intent(out) :: ctx
+        end function
+        !! case1 (D2Q9) circles in shear flow, periodic x: centers(2, np)
+        integer(c_int) function mglc_shear2d_create(p, centers, np, ctx) &
+                bind(C, name="mglc_shear2d_create")
+            import :: c_int, c_ptr, c_double, mglc_shear2d_params
+            type(mglc_shear2d_params), intent(in) :: p
             real(c_double), intent(in) :: centers(*)
             integer(c_int), value :: np
             type(c_ptr), intent(out) :: ctx
