@@ -375,7 +375,7 @@ def serve_bench(torch, mg, n_req=24, rate=50.0, seed=1234, max_steps=2000, tol=1
                      "ctas_per_sm": st["ctas_per_sm"]}}
 
 
-def lid2d_bench(torch, mg, n=1024, steps=400, warmup=20, cpu_s=3.0):
+def lid2d_bench(torch, mg, n=1024, steps=400, warmup=20, cpu_s=3.0, cpu=True):
     """The D2Q9 lid cavity (the reference's 2-D code; FP64, bitwise the
     reference's statements) at n^2: device MLUPS between CUDA events on the
     context's stream, and the oracle on all host cores for a bounded sample.
@@ -400,6 +400,8 @@ def lid2d_bench(torch, mg, n=1024, steps=400, warmup=20, cpu_s=3.0):
            "ms_per_step": round(ms / steps, 4), "bound": "fp64 pipe",
            "hbm_gbs": round(144.0 * n * n / (ms / steps * 1e-3) / 1e9, 1),
            "gpu_launches": steps}
+    if not cpu:
+        return out
     from oracle import oracle as O
     threads = os.cpu_count() or 1
     o = O.Lid2DOracle(n, n, 1000.0, 0.1)
@@ -533,6 +535,8 @@ def main():
     ap.add_argument("--error-steps", type=int, default=0,
                     help="steps for the error runs (default: the workload's own count)")
     ap.add_argument("--no-lid2d", action="store_true", help="skip the D2Q9 lid cavity line")
+    ap.add_argument("--only-lid2d", type=int, default=0, metavar="N",
+                    help="time only the D2Q9 lid cavity at N^2 (--steps/--warmup; profiling runs)")
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-max-steps", type=int, default=2000)
     args = ap.parse_args()
@@ -561,6 +565,11 @@ def main():
     B.build()
     mglc_gb300.lib()
 
+    if args.only_lid2d:
+        print(json.dumps({"lid2d": lid2d_bench(torch, mglc_gb300, n=args.only_lid2d,
+                                               steps=args.steps, warmup=args.warmup,
+                                               cpu=not args.no_cpu)}))
+        return 0
     cells = cells_of(wl)
     peak, peak_kind = load_peaks()
     with ClockSampler(local) as clk:
