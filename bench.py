@@ -153,7 +153,7 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_solve(mg, wl, form):
+def make_solve(mg, wl, form, in_place=False):
     n = wl["n"]
     if wl["kind"] == "particle":
         nx, ny, nz = n
@@ -165,7 +165,7 @@ def make_solve(mg, wl, form):
                                spring_scale_particle=1.0, precision=form)
     if wl["kind"] == "lid":
         return mg.LidDrivenCavity(n, reynolds=wl["reynolds"], u0=wl["u0"], top_layer_u0=False,
-                                  precision=form)
+                                  precision=form, in_place=in_place)
     return mg.BuoyancyCavity(n, rayleigh=wl["rayleigh"], prandtl=wl["prandtl"], mach=wl["mach"],
                              t_hot=0.5, t_cold=-0.5, ekman=0.0, precision=form)
 
@@ -188,9 +188,9 @@ def max_over_ranks(torch, dist, x, device="cuda"):
     return float(t.item())
 
 
-def time_device(torch, mg, wl, form, steps, warmup, dist=None):
+def time_device(torch, mg, wl, form, steps, warmup, dist=None, in_place=False):
     """Device-resident MLUPS: state in HBM, K fused steps between CUDA events."""
-    s = make_solve(mg, wl, form)
+    s = make_solve(mg, wl, form, in_place)
     # the context runs on a dedicated (non-default) stream; the CUDA events
     # are recorded on that same stream
     stream = torch.cuda.Stream()
@@ -623,6 +623,20 @@ def main():
                              "achieved_gbs": round(a2, 1), "frac": round(a2 / peak, 4)}
             except Exception as e:  # report, never hide
                 forms[fm] = {"error": str(e)}
+        if wl["kind"] == "lid":  # the in-place (AA-pattern, one buffer) kernels
+            for fm in ("fp64", "fp32", "fp16", "fp16s"):
+                try:
+                    m2, inf2 = time_device(torch, mglc_gb300, wl, fm, args.steps, args.warmup,
+                                           in_place=True)
+                    v2 = cells * args.steps / (m2 * 1e-3) / 1e6
+                    a2 = inf2.bytes_per_cell_step * cells / (m2 / args.steps * 1e-3) / 1e9
+                    forms[fm + "_in_place"] = {"value": round(v2, 3),
+                                               "ms_per_step": round(m2 / args.steps, 4),
+                                               "achieved_gbs": round(a2, 1),
+                                               "frac": round(a2 / peak, 4),
+                                               "device_bytes": inf2.device_bytes}
+                except Exception as e:  # report, never hide
+                    forms[fm + "_in_place"] = {"error": str(e)}
         if not args.no_error and wl["kind"] in ("lid", "thermal"):
             esteps = args.error_steps or wl.get("error_steps", 1000)
             errs = form_errors(mglc_gb300, wl, [f for f in fms if f != "fp64"], esteps)

@@ -18,6 +18,7 @@ module mglc_iface
         integer(c_int) :: total_nx, total_ny, total_nz
         real(c_double) :: reynolds, rho0, u0
         integer(c_int) :: top_layer_u0, precision
+        integer(c_int) :: in_place = 0   !! 1: AA-pattern streaming on one buffer
     end type
 
     type, bind(C) :: mglc_thermal_params

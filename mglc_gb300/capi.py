@@ -25,7 +25,8 @@ _VP = ctypes.c_void_p
 
 class LidParams(ctypes.Structure):
     _fields_ = [("total_nx", _I), ("total_ny", _I), ("total_nz", _I), ("reynolds", _D),
-                ("rho0", _D), ("u0", _D), ("top_layer_u0", _I), ("precision", _I)]
+                ("rho0", _D), ("u0", _D), ("top_layer_u0", _I), ("precision", _I),
+                ("in_place", _I)]
 
 
 class ThermalParams(ctypes.Structure):

@@ -161,11 +161,12 @@ class LidDrivenCavity(_Solve):
     """D3Q19 MRT lid-driven cavity (reference: Lid_driven_cavity/fortran/3d)."""
 
     def __init__(self, total_nx, total_ny=None, total_nz=None, reynolds=1000.0, u0=0.1,
-                 rho0=1.0, top_layer_u0=True, precision="fp64"):
+                 rho0=1.0, top_layer_u0=True, precision="fp64", in_place=False):
         super().__init__()
         self.u0 = float(u0)
         p = capi.LidParams(total_nx, total_ny or total_nx, total_nz or total_nx, float(reynolds),
-                           float(rho0), float(u0), int(bool(top_layer_u0)), capi.FORMS[precision])
+                           float(rho0), float(u0), int(bool(top_layer_u0)), capi.FORMS[precision],
+                           int(bool(in_place)))
         ctx = _P()
         rc = capi.lib().mglc_lid_create(ctypes.byref(p), ctypes.byref(ctx))
         self._ctx = ctx

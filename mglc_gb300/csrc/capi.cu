@@ -28,6 +28,8 @@ struct mglc_ctx {
     P2Ctx* p2d = nullptr;  // MGLC_KIND_PARTICLE2D: the D2Q9 case4 state
     L2Ctx* l2d = nullptr;  // MGLC_KIND_LID2D: the D2Q9 lid-driven cavity
     bool sr = false;       // MGLC_FP16S / MGLC_BF16S: stochastic rounding of the 16-bit stores
+    bool in_place = false; // lid: AA pattern on one population buffer (f[1] unused)
+    bool swapped = false;  // in place: the buffer holds an even step's output (swap pending)
     Geom geom{};
     long long n = 0;
     cudaStream_t stream = nullptr;
@@ -126,7 +128,7 @@ int alloc_common(mglc_ctx* c, bool thermal) {
     const long long n = c->n;
     const size_t pb = form_bytes(c->form);
     int rc;
-    for (int b = 0; b < 2; b++)
+    for (int b = 0; b < (c->in_place ? 1 : 2); b++)
         if ((rc = dalloc(c, &c->f[b], (size_t)Q19 * n * pb, "populations f"))) return rc;
     if (thermal) {
         // temperature populations in the arithmetic type (FP64 or FP32)
@@ -221,9 +223,19 @@ int download_pops(mglc_ctx* c, int Q, const void* dev, double* host, bool shifte
 
 bool thermal(const mglc_ctx* c) { return c->kind == MGLC_KIND_THERMAL; }
 
+// in place: restore the post-stream layout after an even step (pairwise swap)
+int natural_layout(mglc_ctx* c) {
+    if (!c->in_place || !c->swapped) return MGLC_OK;
+    CK(launch_aa_swap(c->form, c->geom, c->f[0], c->stream), "in-place layout swap");
+    c->swapped = false;
+    return MGLC_OK;
+}
+
 // bring rho,u,v,w(,T) up to date with the current populations
 int refresh_macros(mglc_ctx* c) {
     if (c->macros_valid) return MGLC_OK;
+    int rc0 = natural_layout(c);
+    if (rc0) return rc0;
     if (c->kind == MGLC_KIND_PARTICLE) {
         CK(launch_particle_macro(c->form, c->first_pending, c->f[c->cur], c->pp, c->pd, c->rho,
                                  c->u, c->v, c->w, c->stream),
@@ -262,7 +274,12 @@ int mglc_lid_create(const mglc_lid_params* p, mglc_ctx** out) {
         *out = c;  // caller reads the message, then destroys
         return rc;
     }
+    if (p->in_place && p->precision == MGLC_FX64) {
+        *out = c;
+        return fail(c, MGLC_ERR_UNSUPPORTED, "the in-place pattern is built for FP64/FP32/FP16/BF16");
+    }
     c->kind = MGLC_KIND_LID;
+    c->in_place = p->in_place != 0;
     c->fx64 = p->precision == MGLC_FX64;
     c->sr = sr_form(p->precision);
     c->form = c->fx64 ? FORM_FP64 : storage_of(p->precision);
@@ -468,6 +485,7 @@ int mglc_initial(mglc_ctx* c) {
        "equilibrium");
     CK(cudaStreamSynchronize(c->stream), "synchronize");  // host vectors go out of scope
     c->cur = 0;
+    c->swapped = false;
     c->itc = 0;
     c->first_pending = true;
     c->macros_valid = true;
@@ -487,6 +505,7 @@ int mglc_load_state(mglc_ctx* c, const double* f, const double* g, const double*
     if (thermal(c) && !g) return fail(c, MGLC_ERR_INVALID, "thermal contexts need g");
     const bool shifted = c->form != FORM_FP64;
     int rc;
+    c->swapped = false;  // the upload writes the post-stream layout
     if ((rc = upload_pops(c, Q19, f, c->f[0], shifted))) return rc;
     if (thermal(c) && (rc = upload_pops(c, Q7, g, c->g[0], false))) return rc;
     const size_t b = c->n * sizeof(double);
@@ -535,6 +554,7 @@ int mglc_get_f(mglc_ctx* c, double* f, double* g) {
     if (c->l2d) return f ? l2d_get_f(c->l2d, f, c->err) : MGLC_OK;
     const bool shifted = c->form != FORM_FP64;
     int rc;
+    if ((rc = natural_layout(c))) return rc;
     if (f && (rc = download_pops(c, Q19, c->f[c->cur], f, shifted))) return rc;
     if (g && thermal(c) && (rc = download_pops(c, Q7, c->g[c->cur], g, false))) return rc;
     return MGLC_OK;
@@ -589,6 +609,15 @@ int mglc_step(mglc_ctx* c, int nsteps) {
             a.seed = (unsigned)c->itc;
             a.sr = c->sr ? 1 : 0;
             a.rho = c->rho; a.u = c->u; a.v = c->v; a.w = c->w;
+            if (c->in_place) {
+                e = launch_lid_step_aa(c->form, c->first_pending, c->swapped, c->f[0], a, c->stream);
+                if (e != cudaSuccess) return cuda_fail(c, e, "step kernel launch");
+                c->swapped = !c->swapped;
+                c->first_pending = false;
+                c->macros_valid = false;
+                c->itc++;
+                continue;
+            }
             e = launch_lid_step(c->fx64 ? FORM_FX64 : c->form, c->first_pending, c->f[c->cur],
                                 c->f[nxt], a, c->stream);
         } else {

@@ -45,6 +45,11 @@ struct ThermalStepArgs {
 };
 
 // fused step launchers (fin/fout are the population buffers in the context's form)
+// in place (AA pattern, k_step_aa.cu): even/odd step kernels on one buffer,
+// and the pairwise swap that restores the post-stream layout after an even step
+cudaError_t launch_lid_step_aa(int form, bool first, bool odd, void* f, const LidStepArgs& a,
+                               cudaStream_t s);
+cudaError_t launch_aa_swap(int form, const Geom& g, void* f, cudaStream_t s);
 cudaError_t launch_lid_step(int form, bool first, const void* fin, void* fout,
                             const LidStepArgs& a, cudaStream_t s);
 cudaError_t launch_thermal_step(int form, bool first, const void* fin, void* fout,

@@ -19,6 +19,8 @@ struct St<double> {
     static constexpr bool SHIFT = false;
     __device__ static C ld(const double* p, float) { return __ldg(p); }
     __device__ static double raw(const double* p) { return __ldg(p); }
+    // raw_rw: plain load, for a buffer that the same kernel also writes
+    __device__ static double raw_rw(const double* p) { return *p; }
     __device__ static void st_sr(double* p, C v, float, unsigned) { *p = v; }
     __device__ static C cvt(double v, float) { return v; }
     __device__ static void st(double* p, C v, float) { *p = v; }
@@ -29,6 +31,7 @@ struct St<float> {
     static constexpr bool SHIFT = true;
     __device__ static C ld(const float* p, float) { return __ldg(p); }
     __device__ static float raw(const float* p) { return __ldg(p); }
+    __device__ static float raw_rw(const float* p) { return *p; }
     __device__ static void st_sr(float* p, C v, float, unsigned) { *p = v; }
     __device__ static C cvt(float v, float) { return v; }
     __device__ static void st(float* p, C v, float) { *p = v; }
@@ -39,6 +42,7 @@ struct St<__half> {
     static constexpr bool SHIFT = true;
     __device__ static C ld(const __half* p, float inv) { return __half2float(__ldg(p)) * inv; }
     __device__ static __half raw(const __half* p) { return __ldg(p); }
+    __device__ static __half raw_rw(const __half* p) { return *p; }
     // stochastic rounding: 13 uniform bits added below the 10 kept mantissa
     // bits, then truncation (unbiased; rounding errors do not correlate from
     // step to step, so they do not accumulate into a drift)
@@ -58,6 +62,7 @@ struct St<__nv_bfloat16> {
         return __bfloat162float(__ldg(p)) * inv;
     }
     __device__ static __nv_bfloat16 raw(const __nv_bfloat16* p) { return __ldg(p); }
+    __device__ static __nv_bfloat16 raw_rw(const __nv_bfloat16* p) { return *p; }
     __device__ static void st_sr(__nv_bfloat16* p, C v, float sc, unsigned r) {
         *p = __float2bfloat16_rz(__uint_as_float(__float_as_uint(v * sc) + (r >> 16)));
     }
@@ -140,7 +145,21 @@ __device__ __forceinline__ unsigned sr_pop(unsigned h, int q) {
 // already in registers (raw); lid_cell: load them, then the same.  SR: the
 // 16-bit stores round stochastically (a compile-time choice, so the
 // round-to-nearest kernels carry none of its code).
-template <typename S, bool FIRST, typename IDX, bool SR = false>
+//
+// In-place (AA) pattern, one population buffer: an even step reads the
+// cell's own slots and writes each post-collision population q into the
+// cell's own slot opp(q) (SWAP_STORE); an odd step reads population q from
+// slot opp(q) of the upstream cell x - e_q (or, when that cell is outside,
+// from the cell's own slot q, which the even step filled with the reflected
+// value) and writes like the push kernel, into slot q of x + e_q or, at a
+// wall, into the cell's own slot opp(q).  Every slot is read and then written
+// by one thread only, so a step needs no second buffer.  Wall reflections
+// and the lid term are applied when a population is written, with that
+// step's rho, exactly as in the push kernel: the arithmetic, and so every
+// bit of the result, is the push kernel's.  After an odd step the buffer
+// holds the post-stream populations (the push layout); after an even step a
+// pairwise swap (k_aa_swap) restores that layout.
+template <typename S, bool FIRST, typename IDX, bool SR = false, bool SWAP_STORE = false>
 __device__ __forceinline__ void lid_cell_from(int i, int j, int k, const S (&raw)[Q19],
                                               S* __restrict__ fout,
                                               const StepK<typename St<S>::C>& K, IDX P,
@@ -181,6 +200,18 @@ __device__ __forceinline__ void lid_cell_from(int i, int j, int k, const S (&raw
         if (sr) St<S>::st_sr(p, v, K.scale, sr_pop(h0, q));
         else St<S>::st(p, v, K.scale);
     };
+    if (SWAP_STORE) {  // in-place even step: own cell, slot opp(q)
+        C lid = C(0);
+        if (k == nz - 1) lid = rho / C(6) * K.u0;
+#pragma unroll
+        for (int q = 0; q < Q19; q++) {
+            const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
+            C val = f[q];
+            if ((bm & leave_bits(dx, dy, dz)) != 0 && dz > 0 && dx != 0) val = val - C(dx) * lid;
+            put(fout + ((IDX)opp19(q) * P + cell), val, q);
+        }
+        return;
+    }
     if (bm == 0) {  // interior cell: every population streams
 #pragma unroll
         for (int q = 0; q < Q19; q++) {
@@ -212,6 +243,31 @@ __device__ __forceinline__ void lid_load(int i, int j, int k, const S* __restric
     const IDX cell = (IDX)i + (IDX)nx * ((IDX)j + (IDX)ny * (IDX)k);
 #pragma unroll
     for (int q = 0; q < Q19; q++) raw[q] = St<S>::raw(fin + ((IDX)q * P + cell));
+}
+
+// in-place pattern loads (plain loads: the buffer is written by the same kernel).
+// ODD: population q from slot opp(q) of the upstream cell, or from the cell's
+// own slot q where the upstream cell is outside the domain.
+template <typename S, typename IDX, bool ODD>
+__device__ __forceinline__ void lid_load_aa(int i, int j, int k, const S* f, int nx, int ny,
+                                            int nz, IDX P, S (&raw)[Q19]) {
+    const IDX cell = (IDX)i + (IDX)nx * ((IDX)j + (IDX)ny * (IDX)k);
+    if (!ODD) {
+#pragma unroll
+        for (int q = 0; q < Q19; q++) raw[q] = St<S>::raw_rw(f + ((IDX)q * P + cell));
+        return;
+    }
+    const IDX sy = (IDX)nx, sz = (IDX)nx * (IDX)ny;
+    const unsigned bm = face_mask(i, j, k, nx, ny, nz);
+#pragma unroll
+    for (int q = 0; q < Q19; q++) {
+        const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
+        if ((bm & leave_bits(-dx, -dy, -dz)) != 0)
+            raw[q] = St<S>::raw_rw(f + ((IDX)q * P + cell));
+        else
+            raw[q] = St<S>::raw_rw(f + ((IDX)opp19(q) * P + cell - (IDX)(dx + dy * (int)sy) -
+                                        (IDX)dz * sz));
+    }
 }
 
 template <typename S, bool FIRST, typename IDX, bool SR = false>
