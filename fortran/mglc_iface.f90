@@ -27,6 +27,7 @@ module mglc_iface
         real(c_double) :: t_hot, t_cold, t_ref
         real(c_double) :: ekman
         integer(c_int) :: bc_y_const_t, bc_z_const_t, precision
+        integer(c_int) :: in_place = 0   !! 1: AA-pattern streaming of f and g
     end type
 
     type, bind(C) :: mglc_particle_params

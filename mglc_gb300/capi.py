@@ -32,7 +32,8 @@ class LidParams(ctypes.Structure):
 class ThermalParams(ctypes.Structure):
     _fields_ = [("total_nx", _I), ("total_ny", _I), ("total_nz", _I), ("rayleigh", _D),
                 ("prandtl", _D), ("mach", _D), ("t_hot", _D), ("t_cold", _D), ("t_ref", _D),
-                ("ekman", _D), ("bc_y_const_t", _I), ("bc_z_const_t", _I), ("precision", _I)]
+                ("ekman", _D), ("bc_y_const_t", _I), ("bc_z_const_t", _I), ("precision", _I),
+                ("in_place", _I)]
 
 
 class ParticleParams(ctypes.Structure):

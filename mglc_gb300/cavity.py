@@ -205,12 +205,12 @@ class BuoyancyCavity(_Solve):
 
     def __init__(self, total_nx, total_ny=None, total_nz=None, rayleigh=1e5, prandtl=0.71,
                  mach=0.1, t_hot=0.5, t_cold=-0.5, t_ref=0.0, ekman=0.0, bc_y_const_t=True,
-                 bc_z_const_t=False, precision="fp64"):
+                 bc_z_const_t=False, precision="fp64", in_place=False):
         super().__init__()
         p = capi.ThermalParams(total_nx, total_ny or total_nx, total_nz or total_nx,
                                float(rayleigh), float(prandtl), float(mach), float(t_hot),
                                float(t_cold), float(t_ref), float(ekman), int(bool(bc_y_const_t)),
-                               int(bool(bc_z_const_t)), capi.FORMS[precision])
+                               int(bool(bc_z_const_t)), capi.FORMS[precision], int(bool(in_place)))
         ctx = _P()
         rc = capi.lib().mglc_thermal_create(ctypes.byref(p), ctypes.byref(ctx))
         self._ctx = ctx

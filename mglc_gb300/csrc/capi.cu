@@ -133,7 +133,7 @@ int alloc_common(mglc_ctx* c, bool thermal) {
     if (thermal) {
         // temperature populations in the arithmetic type (FP64 or FP32)
         const size_t gb = c->form == FORM_FP64 ? 8 : 4;
-        for (int b = 0; b < 2; b++)
+        for (int b = 0; b < (c->in_place ? 1 : 2); b++)
             if ((rc = dalloc(c, &c->g[b], (size_t)Q7 * n * gb, "populations g"))) return rc;
         const size_t cb = c->form == FORM_FP64 ? 8 : 4;
         if ((rc = dalloc(c, &c->F, 3 * n * cb, "carried force"))) return rc;
@@ -226,7 +226,8 @@ bool thermal(const mglc_ctx* c) { return c->kind == MGLC_KIND_THERMAL; }
 // in place: restore the post-stream layout after an even step (pairwise swap)
 int natural_layout(mglc_ctx* c) {
     if (!c->in_place || !c->swapped) return MGLC_OK;
-    CK(launch_aa_swap(c->form, c->geom, c->f[0], c->stream), "in-place layout swap");
+    CK(launch_aa_swap(c->form, c->geom, c->f[0], thermal(c) ? c->g[0] : nullptr, c->stream),
+       "in-place layout swap");
     c->swapped = false;
     return MGLC_OK;
 }
@@ -314,11 +315,14 @@ int mglc_thermal_create(const mglc_thermal_params* p, mglc_ctx** out) {
         rc = fail(c, MGLC_ERR_INVALID, "unknown precision %d", p->precision);
     if (!rc && !(p->rayleigh > 0.0 && p->prandtl > 0.0 && p->mach > 0.0))
         rc = fail(c, MGLC_ERR_INVALID, "rayleigh, prandtl and mach must be positive");
+    if (!rc && p->in_place && p->precision == MGLC_FX64)
+        rc = fail(c, MGLC_ERR_UNSUPPORTED, "the in-place pattern is built for FP64/FP32/FP16/BF16");
     if (rc) {
         *out = c;
         return rc;
     }
     c->kind = MGLC_KIND_THERMAL;
+    c->in_place = p->in_place != 0;
     c->sr = sr_form(p->precision);
     c->fx64 = p->precision == MGLC_FX64;
     c->form = c->fx64 ? FORM_FP64 : storage_of(p->precision);
@@ -632,6 +636,16 @@ int mglc_step(mglc_ctx* c, int nsteps) {
             a.seed = (unsigned)c->itc;
             a.sr = c->sr ? 1 : 0;
             a.rho = c->rho; a.u = c->u; a.v = c->v; a.w = c->w; a.T = c->T;
+            if (c->in_place) {
+                e = launch_thermal_step_aa(c->form, c->first_pending, c->swapped, c->f[0], c->g[0],
+                                           c->F, a, c->stream);
+                if (e != cudaSuccess) return cuda_fail(c, e, "step kernel launch");
+                c->swapped = !c->swapped;
+                c->first_pending = false;
+                c->macros_valid = false;
+                c->itc++;
+                continue;
+            }
             e = launch_thermal_step(c->fx64 ? FORM_FX64 : c->form, c->first_pending, c->f[c->cur], c->f[nxt], c->g[c->cur],
                                     c->g[nxt], c->F, a, c->stream);
         }

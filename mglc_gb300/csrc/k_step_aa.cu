@@ -25,11 +25,30 @@ __global__ void __launch_bounds__(128)
     lid_cell_from<S, FIRST, IDX, SR, !ODD>(i, j, k, raw, f, K, P, mrho, mu, mv, mw, K.seed);
 }
 
-// Pairwise exchange (q, x) <-> (opp(q), x - e_q) for the nine directions with
-// opp(q) > q: the streaming half of a step, without collision.  The pair is
-// owned by the thread of x, so the exchange is race-free; where x - e_q is
-// outside, slot q of x already holds the reflected population.
-template <typename S, typename IDX>
+// Heated cavity in place: flow and temperature populations each on one
+// buffer; the carried force is the cell's own (read, then written).
+template <typename S, bool FIRST, bool ROT, typename IDX, bool SR, bool ODD>
+__global__ void __launch_bounds__(128)
+    k_thermal_step_aa(S* f, typename St<S>::C* g, typename St<S>::C* __restrict__ F,
+                      StepK<typename St<S>::C> K, IDX P, const double* __restrict__ mrho,
+                      const double* __restrict__ mu, const double* __restrict__ mv,
+                      const double* __restrict__ mw, const double* __restrict__ mT) {
+    using C = typename St<S>::C;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= K.nx) return;
+    const int j = blockIdx.y, k = blockIdx.z;
+    C fv[Q19], gv[Q7];  // every load is issued before the first store
+    thermal_load_aa<S, IDX, ODD>(i, j, k, f, g, K, P, fv, gv);
+    thermal_cell_from<S, FIRST, ROT, IDX, SR, !ODD>(i, j, k, fv, gv, f, g, F, K, P, mrho, mu, mv,
+                                                    mw, mT, (IDX)2 * P, K.seed);
+}
+
+// Pairwise exchange (q, x) <-> (opp(q), x - e_q) for the directions with
+// opp(q) > q (nine of D3Q19, three of D3Q7): the streaming half of a step,
+// without collision.  The pair is owned by the thread of x, so the exchange
+// is race-free; where x - e_q is outside, slot q of x already holds the
+// reflected population.
+template <typename S, int Q, typename IDX>
 __global__ void __launch_bounds__(128) k_aa_swap(S* f, int nx, int ny, int nz, IDX P) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nx) return;
@@ -38,7 +57,7 @@ __global__ void __launch_bounds__(128) k_aa_swap(S* f, int nx, int ny, int nz, I
     const IDX sy = (IDX)nx, sz = (IDX)nx * (IDX)ny;
     const unsigned bm = face_mask(i, j, k, nx, ny, nz);
 #pragma unroll
-    for (int q = 1; q < Q19; q++) {
+    for (int q = 1; q < Q; q++) {
         if (opp19(q) < q) continue;
         const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
         if ((bm & leave_bits(-dx, -dy, -dz)) != 0) continue;
@@ -92,13 +111,56 @@ cudaError_t lid_go_aa(bool first, bool odd, void* f, const LidStepArgs& a, cudaS
     return cudaGetLastError();
 }
 
-template <typename S>
+template <typename S, int Q>
 cudaError_t swap_go(const Geom& g, void* f, cudaStream_t s) {
     const dim3 b = aa_block(g.nx), gr((g.nx + b.x - 1) / b.x, g.ny, g.nz);
     if ((long long)Q19 * g.plane < (1ll << 31))
-        k_aa_swap<S, unsigned><<<gr, b, 0, s>>>((S*)f, g.nx, g.ny, g.nz, (unsigned)g.plane);
+        k_aa_swap<S, Q, unsigned><<<gr, b, 0, s>>>((S*)f, g.nx, g.ny, g.nz, (unsigned)g.plane);
     else
-        k_aa_swap<S, long long><<<gr, b, 0, s>>>((S*)f, g.nx, g.ny, g.nz, (long long)g.plane);
+        k_aa_swap<S, Q, long long><<<gr, b, 0, s>>>((S*)f, g.nx, g.ny, g.nz, (long long)g.plane);
+    return cudaGetLastError();
+}
+
+template <typename S>
+cudaError_t th_go_aa(bool first, bool odd, void* f, void* g, void* F, const ThermalStepArgs& a,
+                     cudaStream_t s) {
+    using C = typename St<S>::C;
+    StepK<C> K = make_k<C>(a.g, a.cd, 0.0, a.rho0, a.scale, a.inv_scale);
+    K.seed = a.seed;
+    K.sr = a.sr;
+    K.gbeta = (C)a.gbeta; K.omega_rot = (C)a.omega_rot; K.t_ref = (C)a.t_ref;
+    K.para_a = (C)a.para_a; K.qd = (C)a.qd; K.qnu = (C)a.qnu;
+    K.chot = (C)((6.0 + a.para_a) / 21.0 * a.t_hot);
+    K.ccold = (C)((6.0 + a.para_a) / 21.0 * a.t_cold);
+    K.bc_y = a.bc_y; K.bc_z = a.bc_z;
+    const dim3 b = aa_block(a.g.nx), gr((a.g.nx + b.x - 1) / b.x, a.g.ny, a.g.nz);
+    const bool rot = a.omega_rot != 0.0;
+    const bool small = (long long)Q19 * a.g.plane < (1ll << 31);
+    constexpr bool kHalf = sizeof(S) == 2;
+    const bool sr = kHalf && a.sr;
+    S* fp = (S*)f;
+    C* gp = (C*)g;
+    C* Fp = (C*)F;
+#define TA_LAUNCH(FI, RO, IT, SRV, OD)                                                       \
+    k_thermal_step_aa<S, FI, RO, IT, SRV, OD><<<gr, b, 0, s>>>(fp, gp, Fp, K, (IT)a.g.plane, \
+                                                               a.rho, a.u, a.v, a.w, a.T)
+#define TA_SR(FI, RO, IT, OD)                        \
+    do {                                             \
+        if (sr) TA_LAUNCH(FI, RO, IT, kHalf, OD);    \
+        else TA_LAUNCH(FI, RO, IT, false, OD);       \
+    } while (0)
+#define TA_PICK(RO, IT)                              \
+    if (odd) TA_SR(false, RO, IT, true);             \
+    else if (first) TA_SR(true, RO, IT, false);      \
+    else TA_SR(false, RO, IT, false);
+    if (small) {
+        if (rot) { TA_PICK(true, unsigned) } else { TA_PICK(false, unsigned) }
+    } else {
+        if (rot) { TA_PICK(true, long long) } else { TA_PICK(false, long long) }
+    }
+#undef TA_PICK
+#undef TA_SR
+#undef TA_LAUNCH
     return cudaGetLastError();
 }
 
@@ -118,14 +180,29 @@ cudaError_t launch_lid_step_aa(int form, bool first, bool odd, void* f, const Li
     return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_aa_swap(int form, const Geom& g, void* f, cudaStream_t s) {
+cudaError_t launch_thermal_step_aa(int form, bool first, bool odd, void* f, void* g, void* F,
+                                   const ThermalStepArgs& a, cudaStream_t s) {
+    if (first && odd) return cudaErrorInvalidValue;
     switch (form) {
-        case FORM_FP64: return swap_go<double>(g, f, s);
-        case FORM_FP32: return swap_go<float>(g, f, s);
-        case FORM_FP16: return swap_go<__half>(g, f, s);
-        case FORM_BF16: return swap_go<__nv_bfloat16>(g, f, s);
+        case FORM_FP64: return th_go_aa<double>(first, odd, f, g, F, a, s);
+        case FORM_FP32: return th_go_aa<float>(first, odd, f, g, F, a, s);
+        case FORM_FP16: return th_go_aa<__half>(first, odd, f, g, F, a, s);
+        case FORM_BF16: return th_go_aa<__nv_bfloat16>(first, odd, f, g, F, a, s);
     }
     return cudaErrorInvalidValue;
+}
+
+// g (heated cavity): D3Q7 populations in the arithmetic type (FP64 or FP32)
+cudaError_t launch_aa_swap(int form, const Geom& g, void* f, void* gt, cudaStream_t s) {
+    cudaError_t e = cudaErrorInvalidValue;
+    switch (form) {
+        case FORM_FP64: e = swap_go<double, Q19>(g, f, s); break;
+        case FORM_FP32: e = swap_go<float, Q19>(g, f, s); break;
+        case FORM_FP16: e = swap_go<__half, Q19>(g, f, s); break;
+        case FORM_BF16: e = swap_go<__nv_bfloat16, Q19>(g, f, s); break;
+    }
+    if (e != cudaSuccess || !gt) return e;
+    return form == FORM_FP64 ? swap_go<double, Q7>(g, gt, s) : swap_go<float, Q7>(g, gt, s);
 }
 
 }  // namespace mglc

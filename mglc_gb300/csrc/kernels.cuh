@@ -49,7 +49,10 @@ struct ThermalStepArgs {
 // and the pairwise swap that restores the post-stream layout after an even step
 cudaError_t launch_lid_step_aa(int form, bool first, bool odd, void* f, const LidStepArgs& a,
                                cudaStream_t s);
-cudaError_t launch_aa_swap(int form, const Geom& g, void* f, cudaStream_t s);
+cudaError_t launch_thermal_step_aa(int form, bool first, bool odd, void* f, void* g, void* F,
+                                   const ThermalStepArgs& a, cudaStream_t s);
+// gt: the heated cavity's temperature populations (NULL for the lid cavity)
+cudaError_t launch_aa_swap(int form, const Geom& g, void* f, void* gt, cudaStream_t s);
 cudaError_t launch_lid_step(int form, bool first, const void* fin, void* fout,
                             const LidStepArgs& a, cudaStream_t s);
 cudaError_t launch_thermal_step(int form, bool first, const void* fin, void* fout,

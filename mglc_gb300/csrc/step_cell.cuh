@@ -371,10 +371,14 @@ __device__ __forceinline__ void lid_cell_fx(int i, int j, int k, const double* _
 // Temperature populations are kept in the arithmetic type (FP64, or FP32 for
 // the reduced forms): g_0 ~ 0.7 T has a 16-bit ulp (~2e-4) far above the
 // per-step diffusive increments, so 16-bit g would stagnate.
-template <typename S, bool FIRST, bool ROT, typename IDX, bool SR = false>
-__device__ __forceinline__ void thermal_cell(
-    int i, int j, int k, const S* __restrict__ fin, S* __restrict__ fout,
-    const typename St<S>::C* __restrict__ gin, typename St<S>::C* __restrict__ gout,
+// thermal_cell_from: collide and push one cell whose populations are already
+// loaded (f converted to the arithmetic type, g); SWAP_STORE: the in-place
+// even step (own cell, slot opp(q), reflected and anti-bounce-back values
+// formed as the push kernel forms them).  thermal_cell: load, then the same.
+template <typename S, bool FIRST, bool ROT, typename IDX, bool SR = false, bool SWAP_STORE = false>
+__device__ __forceinline__ void thermal_cell_from(
+    int i, int j, int k, typename St<S>::C (&f)[Q19], typename St<S>::C (&g)[Q7],
+    S* __restrict__ fout, typename St<S>::C* __restrict__ gout,
     typename St<S>::C* __restrict__ F, const StepK<typename St<S>::C>& K, IDX P,
     const double* __restrict__ mrho, const double* __restrict__ mu, const double* __restrict__ mv,
     const double* __restrict__ mw, const double* __restrict__ mT, IDX fz_off, unsigned seed) {
@@ -382,11 +386,6 @@ __device__ __forceinline__ void thermal_cell(
     using C = typename St<S>::C;
     const int nx = K.nx, ny = K.ny, nz = K.nz;
     const IDX cell = (IDX)i + (IDX)nx * ((IDX)j + (IDX)ny * (IDX)k);
-    C f[Q19], g[Q7];
-#pragma unroll
-    for (int q = 0; q < Q19; q++) f[q] = St<S>::ld(fin + ((IDX)q * P + cell), K.inv_scale);
-#pragma unroll
-    for (int q = 0; q < Q7; q++) g[q] = gin[(IDX)q * P + cell];
     C rho_m, rho, ux, uy, uz, temp;
     if (FIRST) {
         rho = (C)mrho[cell];
@@ -433,6 +432,21 @@ __device__ __forceinline__ void thermal_cell(
         if (sr) St<S>::st_sr(p, v, K.scale, sr_pop(h0, q));
         else St<S>::st(p, v, K.scale);
     };
+    if (SWAP_STORE) {  // in-place even step: own cell, slot opp(q)
+#pragma unroll
+        for (int q = 0; q < Q19; q++) put(fout + ((IDX)opp19(q) * P + cell), f[q], q);
+#pragma unroll
+        for (int q = 0; q < Q7; q++) {
+            const int dy = ey19(q), dz = ez19(q);
+            C val = g[q];
+            if ((bm & leave_bits(ex19(q), dy, dz)) != 0) {
+                if (dy != 0 && K.bc_y) val = -val + (dy < 0 ? K.chot : K.ccold);
+                if (dz != 0 && K.bc_z) val = -val + (dz < 0 ? K.chot : K.ccold);
+            }
+            gout[(IDX)opp19(q) * P + cell] = val;
+        }
+        return;
+    }
     if (bm == 0) {
 #pragma unroll
         for (int q = 0; q < Q19; q++) {
@@ -470,6 +484,52 @@ __device__ __forceinline__ void thermal_cell(
     }
 }
 
+
+template <typename S, bool FIRST, bool ROT, typename IDX, bool SR = false>
+__device__ __forceinline__ void thermal_cell(
+    int i, int j, int k, const S* __restrict__ fin, S* __restrict__ fout,
+    const typename St<S>::C* __restrict__ gin, typename St<S>::C* __restrict__ gout,
+    typename St<S>::C* __restrict__ F, const StepK<typename St<S>::C>& K, IDX P,
+    const double* __restrict__ mrho, const double* __restrict__ mu, const double* __restrict__ mv,
+    const double* __restrict__ mw, const double* __restrict__ mT, IDX fz_off, unsigned seed) {
+    using C = typename St<S>::C;
+    const IDX cell = (IDX)i + (IDX)K.nx * ((IDX)j + (IDX)K.ny * (IDX)k);
+    C f[Q19], g[Q7];
+#pragma unroll
+    for (int q = 0; q < Q19; q++) f[q] = St<S>::ld(fin + ((IDX)q * P + cell), K.inv_scale);
+#pragma unroll
+    for (int q = 0; q < Q7; q++) g[q] = gin[(IDX)q * P + cell];
+    thermal_cell_from<S, FIRST, ROT, IDX, SR>(i, j, k, f, g, fout, gout, F, K, P, mrho, mu, mv,
+                                              mw, mT, fz_off, seed);
+}
+
+// in-place pattern loads of a heated-cavity cell (plain loads; ODD: from the
+// upstream cells' opposite slots, or the own slot where upstream is outside)
+template <typename S, typename IDX, bool ODD>
+__device__ __forceinline__ void thermal_load_aa(int i, int j, int k, const S* f,
+                                                const typename St<S>::C* g,
+                                                const StepK<typename St<S>::C>& K, IDX P,
+                                                typename St<S>::C (&fv)[Q19],
+                                                typename St<S>::C (&gv)[Q7]) {
+    const int nx = K.nx, ny = K.ny, nz = K.nz;
+    const IDX cell = (IDX)i + (IDX)nx * ((IDX)j + (IDX)ny * (IDX)k);
+    const IDX sy = (IDX)nx, sz = (IDX)nx * (IDX)ny;
+    const unsigned bm = face_mask(i, j, k, nx, ny, nz);
+    auto src = [&](int q) -> IDX {
+        const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
+        if (!ODD || (bm & leave_bits(-dx, -dy, -dz)) != 0) return (IDX)q * P + cell;
+        return (IDX)opp19(q) * P + cell - (IDX)(dx + dy * (int)sy) - (IDX)dz * sz;
+    };
+    S raw[Q19];
+#pragma unroll
+    for (int q = 0; q < Q19; q++) raw[q] = St<S>::raw_rw(f + src(q));
+    // g through L2 only (ld.global.cg, coherent): measured 1.3x faster for the
+    // stochastically rounded 16-bit form, neutral for the others
+#pragma unroll
+    for (int q = 0; q < Q7; q++) gv[q] = __ldcg(g + src(q));
+#pragma unroll
+    for (int q = 0; q < Q19; q++) fv[q] = St<S>::cvt(raw[q], K.inv_scale);
+}
 
 // -------------------------------------------------- heated cavity, FX64 --
 // FP64 storage (f, g and the carried force as in the FP64 form); forced

@@ -93,3 +93,10 @@ def test_in_place_fx64_is_rejected_without_a_gpu(lib):
     assert lib.mglc_lid_create(ctypes.byref(p), ctypes.byref(ctx)) == 6
     assert b"in-place" in lib.mglc_last_error(ctx)
     lib.mglc_destroy(ctx)
+
+
+def test_in_place_fx64_heated_is_rejected_without_a_gpu(lib):
+    ctx = ctypes.c_void_p()
+    t = capi.ThermalParams(8, 8, 8, 1e4, 0.71, 0.1, 0.5, -0.5, 0.0, 0.0, 1, 0, capi.FORMS["fx64"], 1)
+    assert lib.mglc_thermal_create(ctypes.byref(t), ctypes.byref(ctx)) == 6
+    lib.mglc_destroy(ctx)

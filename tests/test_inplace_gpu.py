@@ -84,3 +84,39 @@ def test_64bit_index_path(mg):
         ra, ua = a.macro()[:2]
         rb, ub = b.macro()[:2]
     assert np.array_equal(ra, rb) and np.array_equal(ua, ub)
+
+
+@pytest.mark.parametrize("form", ["fp64", "fp32", "fp16", "fp16s", "bf16"])
+@pytest.mark.parametrize("ekman", [0.0, 1e-3])
+def test_heated_cavity_matches_two_buffer_kernel_bitwise(mg, form, ekman):
+    """Heated cavity in place (f and g on one buffer each, anti-bounce-back
+    walls, carried force, with and without rotation) against two buffers."""
+    kw = dict(rayleigh=1e4, t_hot=0.5, t_cold=-0.5, ekman=ekman, precision=form)
+    a = mg.BuoyancyCavity(21, 18, 16, **kw)
+    b = mg.BuoyancyCavity(21, 18, 16, in_place=True, **kw)
+    with a, b:
+        assert b.info().device_bytes < a.info().device_bytes
+        a.initial()
+        b.initial()
+        for steps in (1, 30, 3):
+            a.step(steps)
+            b.step(steps)
+            fa, ga = a.get_f()
+            fb, gb = b.get_f()
+            assert np.array_equal(fa, fb) and np.array_equal(ga, gb)
+            for x, y in zip(a.macro(), b.macro()):
+                assert np.array_equal(x, y)
+        assert a.nusselt() == b.nusselt()
+
+
+def test_heated_cavity_rayleigh_benard_walls_in_place(mg):
+    kw = dict(rayleigh=2e4, t_hot=0.5, t_cold=-0.5, bc_y_const_t=False, bc_z_const_t=True,
+              precision="fp32")
+    a = mg.BuoyancyCavity(16, 15, 14, **kw)
+    b = mg.BuoyancyCavity(16, 15, 14, in_place=True, **kw)
+    with a, b:
+        a.initial()
+        b.initial()
+        a.step(25)
+        b.step(25)
+        assert np.array_equal(a.get_f()[1], b.get_f()[1])
