@@ -312,6 +312,8 @@ typedef struct mglc_server_params {
     long long max_steps;        /* step cap of one solve */
     int autotune;               /* 1: time tile shapes on the first run and keep the fastest */
     int keep_results;           /* 1: keep rho,u,v,w(,T) of each retired solve on the host */
+    int in_place;               /* 1: AA-pattern streaming, one population buffer per solve
+                                   (about twice the solves per budget; identical results) */
 } mglc_server_params;
 typedef struct mglc_request {
     int kind;         /* MGLC_KIND_LID or MGLC_KIND_THERMAL */

@@ -54,7 +54,7 @@ class Info(ctypes.Structure):
 class ServerParams(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", _LL), ("max_active", _I), ("precision", _I),
                 ("steps_per_iteration", _I), ("tol", _D), ("max_steps", _LL), ("autotune", _I),
-                ("keep_results", _I)]
+                ("keep_results", _I), ("in_place", _I)]
 
 
 class Request(ctypes.Structure):

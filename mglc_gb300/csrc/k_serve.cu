@@ -34,7 +34,11 @@ __device__ __forceinline__ int next_tile_warp(unsigned* counter) {
 }
 
 // lid tiles: [0, lid_tiles); heated tiles: [lid_tiles, total_tiles)
-template <typename S, bool THERMAL, bool SR>
+// AA: solves stream in place on one buffer (step_cell.cuh: even steps read and
+// write each cell's own slots, odd steps read upstream and write downstream;
+// iterations have an even step count, so a solve is in the post-stream layout
+// whenever the residual or the field readers see it).
+template <typename S, bool THERMAL, bool SR, bool AA>
 __global__ void __launch_bounds__(256, THERMAL ? 2 : 3)
     k_serve_step(const ServeTable* __restrict__ tab, int kstep, unsigned* counter) {
     const int parity = kstep & 1;
@@ -53,17 +57,45 @@ __global__ void __launch_bounds__(256, THERMAL ? 2 : 3)
         const int ncell = (r1 - r0) * nx;
         const S* fin = (const S*)sv.f[parity];
         S* fout = (S*)sv.f[parity ^ 1];
+        const unsigned seed = sv.step0 + (unsigned)kstep;
         for (int idx = lane; idx < ncell; idx += 32) {
             const int i = idx % nx, r = r0 + idx / nx;
             const int j = r % ny, k = r / ny;
-            if (!THERMAL)
+            if (AA) {
+                S* f = (S*)sv.f[0];
+                if (!THERMAL) {
+                    S raw[Q19];
+                    if (parity) {
+                        lid_load_aa<S, unsigned, true>(i, j, k, f, nx, ny, nz, sv.plane, raw);
+                        lid_cell_from<S, false, unsigned, SR, false>(
+                            i, j, k, raw, f, sv.K, sv.plane, nullptr, nullptr, nullptr, nullptr, seed);
+                    } else {
+                        lid_load_aa<S, unsigned, false>(i, j, k, f, nx, ny, nz, sv.plane, raw);
+                        lid_cell_from<S, false, unsigned, SR, true>(
+                            i, j, k, raw, f, sv.K, sv.plane, nullptr, nullptr, nullptr, nullptr, seed);
+                    }
+                } else {
+                    float fv[Q19], gv[Q7];
+                    if (parity) {
+                        thermal_load_aa<S, unsigned, true>(i, j, k, f, sv.g[0], sv.K, sv.plane, fv, gv);
+                        thermal_cell_from<S, false, false, unsigned, SR, false>(
+                            i, j, k, fv, gv, f, sv.g[0], sv.F, sv.K, sv.plane, nullptr, nullptr,
+                            nullptr, nullptr, nullptr, 0u, seed);
+                    } else {
+                        thermal_load_aa<S, unsigned, false>(i, j, k, f, sv.g[0], sv.K, sv.plane, fv, gv);
+                        thermal_cell_from<S, false, false, unsigned, SR, true>(
+                            i, j, k, fv, gv, f, sv.g[0], sv.F, sv.K, sv.plane, nullptr, nullptr,
+                            nullptr, nullptr, nullptr, 0u, seed);
+                    }
+                }
+            } else if (!THERMAL) {
                 lid_cell<S, false, unsigned, SR>(i, j, k, fin, fout, sv.K, sv.plane, nullptr,
-                                                 nullptr, nullptr, nullptr,
-                                                 sv.step0 + (unsigned)kstep);
-            else
+                                                 nullptr, nullptr, nullptr, seed);
+            } else {
                 thermal_cell<S, false, false, unsigned, SR>(
                     i, j, k, fin, fout, sv.g[parity], sv.g[parity ^ 1], sv.F, sv.K, sv.plane,
-                    nullptr, nullptr, nullptr, nullptr, nullptr, 0u, sv.step0 + (unsigned)kstep);
+                    nullptr, nullptr, nullptr, nullptr, nullptr, 0u, seed);
+            }
         }
     }
 }
@@ -161,20 +193,23 @@ __global__ void k_serve_fields(ServeSolve sv, float* out) {
 }
 
 template <typename S, bool SR>
-static void serve_go(int thermal, const ServeTable* tab, int k, unsigned* counter, int grid,
-                     int block, cudaStream_t st) {
-    if (thermal) k_serve_step<S, true, SR><<<grid, block, 0, st>>>(tab, k, counter);
-    else k_serve_step<S, false, SR><<<grid, block, 0, st>>>(tab, k, counter);
+static void serve_go(int thermal, int aa, const ServeTable* tab, int k, unsigned* counter,
+                     int grid, int block, cudaStream_t st) {
+    if (thermal && aa) k_serve_step<S, true, SR, true><<<grid, block, 0, st>>>(tab, k, counter);
+    else if (thermal) k_serve_step<S, true, SR, false><<<grid, block, 0, st>>>(tab, k, counter);
+    else if (aa) k_serve_step<S, false, SR, true><<<grid, block, 0, st>>>(tab, k, counter);
+    else k_serve_step<S, false, SR, false><<<grid, block, 0, st>>>(tab, k, counter);
 }
 
-cudaError_t launch_serve_step(int form, int sr, int thermal, const ServeTable* tab, int k,
+cudaError_t launch_serve_step(int form, int sr, int aa, int thermal, const ServeTable* tab, int k,
                               unsigned* counter, int grid, int block, cudaStream_t st) {
-    if (form == FORM_FP16 && sr) serve_go<__half, true>(thermal, tab, k, counter, grid, block, st);
-    else if (form == FORM_FP16) serve_go<__half, false>(thermal, tab, k, counter, grid, block, st);
-    else if (form == FORM_FP32) serve_go<float, false>(thermal, tab, k, counter, grid, block, st);
+    if (form == FORM_FP16 && sr) serve_go<__half, true>(thermal, aa, tab, k, counter, grid, block, st);
+    else if (form == FORM_FP16) serve_go<__half, false>(thermal, aa, tab, k, counter, grid, block, st);
+    else if (form == FORM_FP32) serve_go<float, false>(thermal, aa, tab, k, counter, grid, block, st);
     else if (form == FORM_BF16 && sr)
-        serve_go<__nv_bfloat16, true>(thermal, tab, k, counter, grid, block, st);
-    else if (form == FORM_BF16) serve_go<__nv_bfloat16, false>(thermal, tab, k, counter, grid, block, st);
+        serve_go<__nv_bfloat16, true>(thermal, aa, tab, k, counter, grid, block, st);
+    else if (form == FORM_BF16)
+        serve_go<__nv_bfloat16, false>(thermal, aa, tab, k, counter, grid, block, st);
     else return cudaErrorInvalidValue;
     return cudaGetLastError();
 }

@@ -117,6 +117,7 @@ struct mglc_server {
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t done = nullptr;
     bool sr = false;  // stochastic rounding of the 16-bit stores
+    bool in_place = false;  // AA pattern: one population buffer per solve
     cudaStream_t side = nullptr;        // heated-solve branch of the captured step
     cudaEvent_t fork = nullptr, join = nullptr;
     int block = 256, rows = 2, ctas_per_sm = 4, nsm = 152;
@@ -151,8 +152,9 @@ size_t pop_bytes(const mglc_server* s) { return s->p.precision == MGLC_FP32 ? 4 
 // device footprint of a solve of n^3 cells
 size_t footprint(const mglc_server* s, int kind, int n) {
     const size_t c = (size_t)n * n * n;
-    size_t b = 2 * 19 * c * pop_bytes(s) + 3 * c * 4 + 5 * 256;  // f ping-pong, uprev
-    if (kind == MGLC_KIND_THERMAL) b += 2 * 7 * c * 4 + c * 4;    // g ping-pong, F_z
+    const size_t nb = s->in_place ? 1 : 2;                          // buffers per population set
+    size_t b = nb * 19 * c * pop_bytes(s) + 3 * c * 4 + 5 * 256;    // f, uprev
+    if (kind == MGLC_KIND_THERMAL) b += nb * 7 * c * 4 + c * 4;     // g, F_z
     return b;
 }
 
@@ -205,11 +207,11 @@ void place(mglc_server* s, Req& q) {
     const size_t c = q.sv.plane, pb = pop_bytes(s);
     auto take = [&](size_t n) { char* p = b; b += Arena::round(n); return p; };
     q.sv.f[0] = take(19 * c * pb);
-    q.sv.f[1] = take(19 * c * pb);
+    q.sv.f[1] = s->in_place ? q.sv.f[0] : take(19 * c * pb);
     q.sv.uprev = (float*)take(3 * c * 4);
     if (q.sv.kind == MGLC_KIND_THERMAL) {
         q.sv.g[0] = (float*)take(7 * c * 4);
-        q.sv.g[1] = (float*)take(7 * c * 4);
+        q.sv.g[1] = s->in_place ? q.sv.g[0] : (float*)take(7 * c * 4);
         q.sv.F = (float*)take(c * 4);
     } else {
         q.sv.g[0] = q.sv.g[1] = nullptr;
@@ -253,9 +255,9 @@ cudaError_t issue_step(mglc_server* s, int k, unsigned* c_lid, unsigned* c_heat,
     cudaError_t e = cudaEventRecord(s->fork, s->stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s->side, s->fork, 0);
     if (e == cudaSuccess)
-        e = launch_serve_step(s->p.precision, sr, 1, s->tab_dev, k, c_heat, grid, blk, s->side);
+        e = launch_serve_step(s->p.precision, sr, s->in_place ? 1 : 0, 1, s->tab_dev, k, c_heat, grid, blk, s->side);
     if (e == cudaSuccess)
-        e = launch_serve_step(s->p.precision, sr, 0, s->tab_dev, k, c_lid, grid, blk, s->stream);
+        e = launch_serve_step(s->p.precision, sr, s->in_place ? 1 : 0, 0, s->tab_dev, k, c_lid, grid, blk, s->stream);
     if (e == cudaSuccess) e = cudaEventRecord(s->join, s->side);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s->stream, s->join, 0);
     return e;
@@ -411,6 +413,7 @@ int mglc_server_create(const mglc_server_params* p, mglc_server** out) {
     // FP16S / BF16S: 16-bit storage with stochastic rounding; from here on the
     // precision field holds the storage form
     s->sr = p->precision == MGLC_FP16S || p->precision == MGLC_BF16S;
+    s->in_place = p->in_place != 0;
     if (p->precision == MGLC_FP16S) s->p.precision = MGLC_FP16;
     if (p->precision == MGLC_BF16S) s->p.precision = MGLC_BF16;
     if (p->steps_per_iteration < 2 || p->steps_per_iteration % 2)

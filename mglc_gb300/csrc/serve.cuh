@@ -39,7 +39,7 @@ struct ServeTable {
 // Time step k of the iteration for every active solve of one kind (k & 1
 // selects the ping-pong buffer, step0 + k seeds the stochastic rounding);
 // thermal = 0 runs the lid tiles, 1 the heated ones.
-cudaError_t launch_serve_step(int form, int sr, int thermal, const ServeTable* tab, int k,
+cudaError_t launch_serve_step(int form, int sr, int aa, int thermal, const ServeTable* tab, int k,
                               unsigned* counter, int grid, int block, cudaStream_t st);
 // resid[s] = max over cells of |u - uprev| / uref (as float bits); uprev <- u;
 // then every solve's step0 advances by steps (the iteration's step count)

@@ -17,10 +17,10 @@ from . import capi
 
 class SolveServer:
     def __init__(self, hbm_budget_gb=16.0, max_active=64, precision="fp16", steps_per_iteration=200,
-                 tol=1e-6, max_steps=50000, autotune=True, keep_results=False):
+                 tol=1e-6, max_steps=50000, autotune=True, keep_results=False, in_place=False):
         p = capi.ServerParams(int(hbm_budget_gb * (1 << 30)), int(max_active), capi.FORMS[precision],
                               int(steps_per_iteration), float(tol), int(max_steps),
-                              int(bool(autotune)), int(bool(keep_results)))
+                              int(bool(autotune)), int(bool(keep_results)), int(bool(in_place)))
         self._s = ctypes.c_void_p()
         rc = capi.lib().mglc_server_create(ctypes.byref(p), ctypes.byref(self._s))
         if rc != capi.MGLC_OK:

@@ -126,3 +126,28 @@ def test_convergence_retires_early(mg):
         srv.run()
         r = srv.results()[0]
     assert r["converged"] == 1 and r["steps"] < 50000 and r["residual"] < 1e-4
+
+
+@pytest.mark.parametrize("precision", ["fp16", "fp16s"])
+def test_in_place_server_matches_two_buffer_server(mg, precision):
+    """AA-pattern serving (one buffer per solve): the same fields as the
+    two-buffer server, for lid and heated solves in one mix."""
+    out = []
+    for in_place in (False, True):
+        with _server(mg, max_steps=300, precision=precision, in_place=in_place) as srv:
+            ids = [srv.submit("lid", 36, reynolds=400.0), srv.submit("thermal", 28, rayleigh=1e4),
+                   srv.submit("lid", 27, reynolds=150.0)]
+            srv.run()
+            out.append([srv.field(i) for i in ids])
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)
+
+
+def test_in_place_admits_twice_the_solves(mg):
+    # a 64^3 FP16 lid solve needs ~23 MiB with two buffers, ~14 MiB in place
+    with _server(mg, hbm_budget_gb=64 / 1024, max_steps=200, in_place=True) as srv:
+        for q in range(6):
+            srv.submit("lid", 64, reynolds=400.0, arrival_s=0.0)
+        srv.run()
+        st = srv.stats()
+    assert st["peak_active"] >= 4
