@@ -624,7 +624,7 @@ def main():
             except Exception as e:  # report, never hide
                 forms[fm] = {"error": str(e)}
         if wl["kind"] == "lid":  # the in-place (AA-pattern, one buffer) kernels
-            for fm in ("fp64", "fp32", "fp16", "fp16s"):
+            for fm in ("fp64", "fx64", "fp32", "fp16", "fp16s"):
                 try:
                     m2, inf2 = time_device(torch, mglc_gb300, wl, fm, args.steps, args.warmup,
                                            in_place=True)

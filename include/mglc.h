@@ -67,7 +67,7 @@ typedef struct mglc_lid_params {
     int top_layer_u0; /* 1: initial u = u0 on the top layer (initial.f90:55-61); 0: u = 0 */
     int precision;    /* MGLC_FP64 ... MGLC_FX64 */
     int in_place;     /* 1: AA-pattern streaming on one population buffer (half the
-                         memory; FP64, FP32, FP16(S), BF16(S); results identical to 0) */
+                         memory; every precision; results identical to 0) */
 } mglc_lid_params;
 
 /* Buoyancy-driven cavity parameters:

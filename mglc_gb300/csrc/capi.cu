@@ -275,10 +275,6 @@ int mglc_lid_create(const mglc_lid_params* p, mglc_ctx** out) {
         *out = c;  // caller reads the message, then destroys
         return rc;
     }
-    if (p->in_place && p->precision == MGLC_FX64) {
-        *out = c;
-        return fail(c, MGLC_ERR_UNSUPPORTED, "the in-place pattern is built for FP64/FP32/FP16/BF16");
-    }
     c->kind = MGLC_KIND_LID;
     c->in_place = p->in_place != 0;
     c->fx64 = p->precision == MGLC_FX64;
@@ -614,7 +610,8 @@ int mglc_step(mglc_ctx* c, int nsteps) {
             a.sr = c->sr ? 1 : 0;
             a.rho = c->rho; a.u = c->u; a.v = c->v; a.w = c->w;
             if (c->in_place) {
-                e = launch_lid_step_aa(c->form, c->first_pending, c->swapped, c->f[0], a, c->stream);
+                e = launch_lid_step_aa(c->fx64 ? FORM_FX64 : c->form, c->first_pending, c->swapped,
+                                       c->f[0], a, c->stream);
                 if (e != cudaSuccess) return cuda_fail(c, e, "step kernel launch");
                 c->swapped = !c->swapped;
                 c->first_pending = false;

@@ -25,6 +25,17 @@ __global__ void __launch_bounds__(128)
     lid_cell_from<S, FIRST, IDX, SR, !ODD>(i, j, k, raw, f, K, P, mrho, mu, mv, mw, K.seed);
 }
 
+// FX64 lid cavity in place (FP64 storage, Q55 collision)
+template <bool FIRST, typename IDX, bool ODD>
+__global__ void __launch_bounds__(128, 4)
+    k_lid_step_fx_aa(double* f, FxK K, IDX P, const double* __restrict__ mrho,
+                     const double* __restrict__ mu, const double* __restrict__ mv,
+                     const double* __restrict__ mw) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= K.nx) return;
+    lid_cell_fx<FIRST, IDX, ODD ? 2 : 1>(i, blockIdx.y, blockIdx.z, f, f, K, P, mrho, mu, mv, mw);
+}
+
 // Heated cavity in place: flow and temperature populations each on one
 // buffer; the carried force is the cell's own (read, then written).
 template <typename S, bool FIRST, bool ROT, typename IDX, bool SR, bool ODD>
@@ -111,6 +122,28 @@ cudaError_t lid_go_aa(bool first, bool odd, void* f, const LidStepArgs& a, cudaS
     return cudaGetLastError();
 }
 
+cudaError_t lid_go_fx_aa(bool first, bool odd, void* f, const LidStepArgs& a, cudaStream_t s) {
+    FxK K;
+    K.nx = a.g.nx; K.ny = a.g.ny; K.nz = a.g.nz;
+    K.c = make_fx_coef(a.cd, a.u0);
+    const dim3 b = aa_block(a.g.nx), gr((a.g.nx + b.x - 1) / b.x, a.g.ny, a.g.nz);
+    double* fp = (double*)f;
+    const bool small = (long long)Q19 * a.g.plane < (1ll << 31);
+#define FA_LAUNCH(FI, IT, OD) \
+    k_lid_step_fx_aa<FI, IT, OD><<<gr, b, 0, s>>>(fp, K, (IT)a.g.plane, a.rho, a.u, a.v, a.w)
+    if (small) {
+        if (odd) FA_LAUNCH(false, unsigned, true);
+        else if (first) FA_LAUNCH(true, unsigned, false);
+        else FA_LAUNCH(false, unsigned, false);
+    } else {
+        if (odd) FA_LAUNCH(false, long long, true);
+        else if (first) FA_LAUNCH(true, long long, false);
+        else FA_LAUNCH(false, long long, false);
+    }
+#undef FA_LAUNCH
+    return cudaGetLastError();
+}
+
 template <typename S, int Q>
 cudaError_t swap_go(const Geom& g, void* f, cudaStream_t s) {
     const dim3 b = aa_block(g.nx), gr((g.nx + b.x - 1) / b.x, g.ny, g.nz);
@@ -172,6 +205,7 @@ cudaError_t launch_lid_step_aa(int form, bool first, bool odd, void* f, const Li
                                cudaStream_t s) {
     if (first && odd) return cudaErrorInvalidValue;
     switch (form) {
+        case FORM_FX64: return lid_go_fx_aa(first, odd, f, a, s);
         case FORM_FP64: return lid_go_aa<double>(first, odd, f, a, s);
         case FORM_FP32: return lid_go_aa<float>(first, odd, f, a, s);
         case FORM_FP16: return lid_go_aa<__half>(first, odd, f, a, s);

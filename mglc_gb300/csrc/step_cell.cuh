@@ -298,9 +298,11 @@ struct FxK {
 #define FX_CVT_OUT 17
 #endif
 
-template <bool FIRST, typename IDX>
-__device__ __forceinline__ void lid_cell_fx(int i, int j, int k, const double* __restrict__ fin,
-                                            double* __restrict__ fout, const FxK& K, IDX P,
+// AAM: 0 push (fin -> fout), 1 in-place even step, 2 in-place odd step (fin ==
+// fout; plain loads; see lid_cell_from for the pattern)
+template <bool FIRST, typename IDX, int AAM = 0>
+__device__ __forceinline__ void lid_cell_fx(int i, int j, int k, const double* fin,
+                                            double* fout, const FxK& K, IDX P,
                                             const double* __restrict__ mrho,
                                             const double* __restrict__ mu,
                                             const double* __restrict__ mv,
@@ -311,8 +313,12 @@ __device__ __forceinline__ void lid_cell_fx(int i, int j, int k, const double* _
     {
         // all loads issued before any conversion
         double raw[Q19];
+        if (AAM == 0) {
 #pragma unroll
-        for (int q = 0; q < Q19; q++) raw[q] = __ldg(fin + ((IDX)q * P + cell));
+            for (int q = 0; q < Q19; q++) raw[q] = __ldg(fin + ((IDX)q * P + cell));
+        } else {
+            lid_load_aa<double, IDX, AAM == 2>(i, j, k, fin, nx, ny, nz, P, raw);
+        }
 #pragma unroll
         for (int q = 0; q < Q19; q++) f[q] = __double_as_longlong(raw[q]);
     }
@@ -349,6 +355,11 @@ __device__ __forceinline__ void lid_cell_fx(int i, int j, int k, const double* _
     for (int q = 0; q < Q19; q++) o[q] = bad ? nan : (q < FX_CVT_OUT ? q2d_cvt(f[q]) : q2d(f[q]));
     const IDX sy = (IDX)nx, sz = (IDX)nx * (IDX)ny;
     const unsigned bm = face_mask(i, j, k, nx, ny, nz);
+    if (AAM == 1) {  // in-place even step: own cell, slot opp(q) (lid term already in o)
+#pragma unroll
+        for (int q = 0; q < Q19; q++) fout[(IDX)opp19(q) * P + cell] = o[q];
+        return;
+    }
     if (bm == 0) {
 #pragma unroll
         for (int q = 0; q < Q19; q++) {

@@ -87,14 +87,6 @@ def test_shear2d_parameters_are_rejected_without_a_gpu(lib):
         lib.mglc_destroy(ctx)
 
 
-def test_in_place_fx64_is_rejected_without_a_gpu(lib):
-    ctx = ctypes.c_void_p()
-    p = capi.LidParams(8, 8, 8, 400.0, 1.0, 0.1, 1, capi.FORMS["fx64"], 1)
-    assert lib.mglc_lid_create(ctypes.byref(p), ctypes.byref(ctx)) == 6
-    assert b"in-place" in lib.mglc_last_error(ctx)
-    lib.mglc_destroy(ctx)
-
-
 def test_in_place_fx64_heated_is_rejected_without_a_gpu(lib):
     ctx = ctypes.c_void_p()
     t = capi.ThermalParams(8, 8, 8, 1e4, 0.71, 0.1, 0.5, -0.5, 0.0, 0.0, 1, 0, capi.FORMS["fx64"], 1)

@@ -23,7 +23,7 @@ def _pair(mg, n, form, **kw):
     return a, b
 
 
-@pytest.mark.parametrize("form", ["fp64", "fp32", "fp16", "fp16s", "bf16", "bf16s"])
+@pytest.mark.parametrize("form", ["fp64", "fx64", "fp32", "fp16", "fp16s", "bf16", "bf16s"])
 def test_matches_two_buffer_kernel_bitwise(mg, form):
     a, b = _pair(mg, (33, 35, 37), form)
     with a, b:
