@@ -83,8 +83,8 @@ typedef struct mglc_thermal_params {
     int bc_y_const_t; /* 1: LeftRightWallsConstT (hot j=1, cold j=ny); 0: adiabatic */
     int bc_z_const_t; /* 1: TopBottomPlatesConstT (hot k=1, cold k=nz); 0: adiabatic */
     int precision;
-    int in_place;     /* 1: AA-pattern streaming of f and g on one buffer each (FP64, FP32,
-                         FP16(S), BF16(S); results identical to 0) */
+    int in_place;     /* 1: AA-pattern streaming of f and g on one buffer each (every
+                         precision; results identical to 0) */
 } mglc_thermal_params;
 
 /* Moving spheres in a D3Q19 flow: the 3-D generalisation of

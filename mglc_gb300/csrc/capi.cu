@@ -311,8 +311,6 @@ int mglc_thermal_create(const mglc_thermal_params* p, mglc_ctx** out) {
         rc = fail(c, MGLC_ERR_INVALID, "unknown precision %d", p->precision);
     if (!rc && !(p->rayleigh > 0.0 && p->prandtl > 0.0 && p->mach > 0.0))
         rc = fail(c, MGLC_ERR_INVALID, "rayleigh, prandtl and mach must be positive");
-    if (!rc && p->in_place && p->precision == MGLC_FX64)
-        rc = fail(c, MGLC_ERR_UNSUPPORTED, "the in-place pattern is built for FP64/FP32/FP16/BF16");
     if (rc) {
         *out = c;
         return rc;
@@ -634,8 +632,8 @@ int mglc_step(mglc_ctx* c, int nsteps) {
             a.sr = c->sr ? 1 : 0;
             a.rho = c->rho; a.u = c->u; a.v = c->v; a.w = c->w; a.T = c->T;
             if (c->in_place) {
-                e = launch_thermal_step_aa(c->form, c->first_pending, c->swapped, c->f[0], c->g[0],
-                                           c->F, a, c->stream);
+                e = launch_thermal_step_aa(c->fx64 ? FORM_FX64 : c->form, c->first_pending,
+                                           c->swapped, c->f[0], c->g[0], c->F, a, c->stream);
                 if (e != cudaSuccess) return cuda_fail(c, e, "step kernel launch");
                 c->swapped = !c->swapped;
                 c->first_pending = false;

@@ -36,6 +36,19 @@ __global__ void __launch_bounds__(128, 4)
     lid_cell_fx<FIRST, IDX, ODD ? 2 : 1>(i, blockIdx.y, blockIdx.z, f, f, K, P, mrho, mu, mv, mw);
 }
 
+// FX64 heated cavity in place (4 blocks of 128 per SM, as the two-buffer kernel)
+template <bool FIRST, bool ROT, typename IDX, bool ODD>
+__global__ void __launch_bounds__(128, 4)
+    k_thermal_step_fx_aa(double* f, double* g, double* __restrict__ F, FxTK K, IDX P,
+                         const double* __restrict__ mrho, const double* __restrict__ mu,
+                         const double* __restrict__ mv, const double* __restrict__ mw,
+                         const double* __restrict__ mT) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= K.nx) return;
+    thermal_cell_fx<FIRST, ROT, IDX, ODD ? 2 : 1>(i, blockIdx.y, blockIdx.z, f, f, g, g, F, K, P,
+                                                  mrho, mu, mv, mw, mT);
+}
+
 // Heated cavity in place: flow and temperature populations each on one
 // buffer; the carried force is the cell's own (read, then written).
 template <typename S, bool FIRST, bool ROT, typename IDX, bool SR, bool ODD>
@@ -214,10 +227,41 @@ cudaError_t launch_lid_step_aa(int form, bool first, bool odd, void* f, const Li
     return cudaErrorInvalidValue;
 }
 
+namespace {
+cudaError_t th_go_fx_aa(bool first, bool odd, void* f, void* g, void* F, const ThermalStepArgs& a,
+                        cudaStream_t s) {
+    FxTK K;
+    K.nx = a.g.nx; K.ny = a.g.ny; K.nz = a.g.nz;
+    K.bc_y = a.bc_y; K.bc_z = a.bc_z;
+    K.t = make_fx_thermal(a.cd, a.gbeta, a.omega_rot, a.t_ref, a.para_a, a.qd, a.qnu, a.t_hot,
+                          a.t_cold);
+    const dim3 b = aa_block(a.g.nx), gr((a.g.nx + b.x - 1) / b.x, a.g.ny, a.g.nz);
+    const bool rot = a.omega_rot != 0.0;
+    const bool small = (long long)Q19 * a.g.plane < (1ll << 31);
+    double *fp = (double*)f, *gp = (double*)g, *Fp = (double*)F;
+#define TFA_LAUNCH(FI, RO, IT, OD)                                                               \
+    k_thermal_step_fx_aa<FI, RO, IT, OD><<<gr, b, 0, s>>>(fp, gp, Fp, K, (IT)a.g.plane, a.rho, a.u, \
+                                                          a.v, a.w, a.T)
+#define TFA_PICK(RO, IT)                               \
+    if (odd) TFA_LAUNCH(false, RO, IT, true);          \
+    else if (first) TFA_LAUNCH(true, RO, IT, false);   \
+    else TFA_LAUNCH(false, RO, IT, false);
+    if (small) {
+        if (rot) { TFA_PICK(true, unsigned) } else { TFA_PICK(false, unsigned) }
+    } else {
+        if (rot) { TFA_PICK(true, long long) } else { TFA_PICK(false, long long) }
+    }
+#undef TFA_PICK
+#undef TFA_LAUNCH
+    return cudaGetLastError();
+}
+}  // namespace
+
 cudaError_t launch_thermal_step_aa(int form, bool first, bool odd, void* f, void* g, void* F,
                                    const ThermalStepArgs& a, cudaStream_t s) {
     if (first && odd) return cudaErrorInvalidValue;
     switch (form) {
+        case FORM_FX64: return th_go_fx_aa(first, odd, f, g, F, a, s);
         case FORM_FP64: return th_go_aa<double>(first, odd, f, g, F, a, s);
         case FORM_FP32: return th_go_aa<float>(first, odd, f, g, F, a, s);
         case FORM_FP16: return th_go_aa<__half>(first, odd, f, g, F, a, s);

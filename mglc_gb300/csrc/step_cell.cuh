@@ -556,10 +556,11 @@ struct FxTK {
     FxThermalCoef t;
 };
 
-template <bool FIRST, bool ROT, typename IDX>
+// AAM: 0 push, 1 in-place even step, 2 in-place odd step (as lid_cell_fx)
+template <bool FIRST, bool ROT, typename IDX, int AAM = 0>
 __device__ __forceinline__ void thermal_cell_fx(
-    int i, int j, int k, const double* __restrict__ fin, double* __restrict__ fout,
-    const double* __restrict__ gin, double* __restrict__ gout, double* __restrict__ F,
+    int i, int j, int k, const double* fin, double* fout, const double* gin, double* gout,
+    double* __restrict__ F,
     const FxTK& K, IDX P, const double* __restrict__ mrho, const double* __restrict__ mu,
     const double* __restrict__ mv, const double* __restrict__ mw, const double* __restrict__ mT) {
     using ll = long long;
@@ -569,10 +570,24 @@ __device__ __forceinline__ void thermal_cell_fx(
     bool bad = false;
     {
         double rf[Q19], rg[Q7];
+        if (AAM == 0) {
 #pragma unroll
-        for (int q = 0; q < Q19; q++) rf[q] = __ldg(fin + ((IDX)q * P + cell));
+            for (int q = 0; q < Q19; q++) rf[q] = __ldg(fin + ((IDX)q * P + cell));
 #pragma unroll
-        for (int q = 0; q < Q7; q++) rg[q] = __ldg(gin + ((IDX)q * P + cell));
+            for (int q = 0; q < Q7; q++) rg[q] = __ldg(gin + ((IDX)q * P + cell));
+        } else {
+            const IDX sy = (IDX)nx, sz = (IDX)nx * (IDX)ny;
+            const unsigned bm = face_mask(i, j, k, nx, ny, nz);
+            auto src = [&](int q) -> IDX {
+                const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
+                if (AAM != 2 || (bm & leave_bits(-dx, -dy, -dz)) != 0) return (IDX)q * P + cell;
+                return (IDX)opp19(q) * P + cell - (IDX)(dx + dy * (int)sy) - (IDX)dz * sz;
+            };
+#pragma unroll
+            for (int q = 0; q < Q19; q++) rf[q] = fin[src(q)];
+#pragma unroll
+            for (int q = 0; q < Q7; q++) rg[q] = __ldcg(gin + src(q));
+        }
 #pragma unroll
         for (int q = 0; q < Q19; q++) {
             bad |= fx_bad(rf[q]);
@@ -634,7 +649,9 @@ __device__ __forceinline__ void thermal_cell_fx(
     for (int q = 0; q < Q19; q++) {
         const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
         const double o = bad ? nan : (q < FX_CVT_OUT ? q2d_cvt(f[q]) : q2d(f[q]));
-        if ((bm & leave_bits(dx, dy, dz)) == 0)
+        if (AAM == 1)  // in-place even step: own cell, slot opp(q)
+            fout[(IDX)opp19(q) * P + cell] = o;
+        else if ((bm & leave_bits(dx, dy, dz)) == 0)
             fout[(IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz] = o;
         else
             fout[(IDX)opp19(q) * P + cell] = o;
@@ -644,8 +661,11 @@ __device__ __forceinline__ void thermal_cell_fx(
     for (int q = 0; q < Q7; q++) {
         const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
         if ((bm & leave_bits(dx, dy, dz)) == 0) {
-            gout[(IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz] =
-                bad ? nan : (q < FXT_CVT_G ? q2d_cvt(g[q]) : q2d(g[q]));
+            const double o = bad ? nan : (q < FXT_CVT_G ? q2d_cvt(g[q]) : q2d(g[q]));
+            if (AAM == 1)
+                gout[(IDX)opp19(q) * P + cell] = o;
+            else
+                gout[(IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz] = o;
         } else {
             ll val = g[q];
             if (dy != 0 && K.bc_y) val = -val + (dy < 0 ? K.t.chot : K.t.ccold);

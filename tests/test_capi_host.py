@@ -85,10 +85,3 @@ def test_shear2d_parameters_are_rejected_without_a_gpu(lib):
         assert lib.mglc_shear2d_create(ctypes.byref(p), c.ctypes.data, len(c), ctypes.byref(ctx)) == 1
         assert msg in lib.mglc_last_error(ctx)
         lib.mglc_destroy(ctx)
-
-
-def test_in_place_fx64_heated_is_rejected_without_a_gpu(lib):
-    ctx = ctypes.c_void_p()
-    t = capi.ThermalParams(8, 8, 8, 1e4, 0.71, 0.1, 0.5, -0.5, 0.0, 0.0, 1, 0, capi.FORMS["fx64"], 1)
-    assert lib.mglc_thermal_create(ctypes.byref(t), ctypes.byref(ctx)) == 6
-    lib.mglc_destroy(ctx)

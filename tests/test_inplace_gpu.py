@@ -86,7 +86,7 @@ def test_64bit_index_path(mg):
     assert np.array_equal(ra, rb) and np.array_equal(ua, ub)
 
 
-@pytest.mark.parametrize("form", ["fp64", "fp32", "fp16", "fp16s", "bf16"])
+@pytest.mark.parametrize("form", ["fp64", "fx64", "fp32", "fp16", "fp16s", "bf16"])
 @pytest.mark.parametrize("ekman", [0.0, 1e-3])
 def test_heated_cavity_matches_two_buffer_kernel_bitwise(mg, form, ekman):
     """Heated cavity in place (f and g on one buffer each, anti-bounce-back
