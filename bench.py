@@ -535,6 +535,8 @@ def main():
     ap.add_argument("--error-steps", type=int, default=0,
                     help="steps for the error runs (default: the workload's own count)")
     ap.add_argument("--no-lid2d", action="store_true", help="skip the D2Q9 lid cavity line")
+    ap.add_argument("--in-place", action="store_true",
+                    help="time the main line with the in-place (AA-pattern, one-buffer) kernels")
     ap.add_argument("--only-lid2d", type=int, default=0, metavar="N",
                     help="time only the D2Q9 lid cavity at N^2 (--steps/--warmup; profiling runs)")
     ap.add_argument("--serve-requests", type=int, default=24)
@@ -573,7 +575,8 @@ def main():
     cells = cells_of(wl)
     peak, peak_kind = load_peaks()
     with ClockSampler(local) as clk:
-        ms, info = time_device(torch, mglc_gb300, wl, args.form, args.steps, args.warmup, dist)
+        ms, info = time_device(torch, mglc_gb300, wl, args.form, args.steps, args.warmup, dist,
+                               in_place=args.in_place)
     clocks = clk.summary()
     value = world * cells * args.steps / (ms * 1e-3) / 1e6
     ms_step = ms / args.steps
@@ -590,7 +593,8 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": {"fp64": "f64", "fx64": "i64 Q55 fixed point (f64 storage)"}.get(args.form, "f32"),
         "data": wl.get("data", "synthetic (analytic cavity initial state, no dataset)"),
-        "config": {"workload": wl["desc"], "form": args.form, "cells": cells,
+        "config": {"workload": wl["desc"], "form": args.form + ("_in_place" if args.in_place else ""),
+                   "cells": cells,
                    "parallelism": f"replicas{world}" if world > 1 else "single",
                    "l2": l2_note(cells * bpc)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",

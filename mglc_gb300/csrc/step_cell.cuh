@@ -259,6 +259,15 @@ __device__ __forceinline__ void lid_load_aa(int i, int j, int k, const S* f, int
     }
     const IDX sy = (IDX)nx, sz = (IDX)nx * (IDX)ny;
     const unsigned bm = face_mask(i, j, k, nx, ny, nz);
+    if (bm == 0) {  // interior cell: every upstream cell is inside
+#pragma unroll
+        for (int q = 0; q < Q19; q++) {
+            const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
+            raw[q] = St<S>::raw_rw(f + ((IDX)opp19(q) * P + cell - (IDX)(dx + dy * (int)sy) -
+                                        (IDX)dz * sz));
+        }
+        return;
+    }
 #pragma unroll
     for (int q = 0; q < Q19; q++) {
         const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
