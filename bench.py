@@ -315,13 +315,15 @@ def form_errors(mg, wl, forms, steps):
     return res
 
 
-def serve_bench(torch, mg, n_req=24, rate=50.0, seed=1234, max_steps=2000, tol=1e-6, K=100,
-                precision="fp16"):
+def serve_bench(torch, mg, n_req=24, rate=50.0, seed=1234, max_steps=50000, tol=1e-6, K=100,
+                precision="fp16", sample_steps=400):
     """Batched serving stream: Poisson arrivals of lid-driven and heated-cavity
     solves (grids from {32,48,64,96,128}, Re ~ U[100,1000] or Ra log-uniform in
-    [1e3,1e5]), each run to max|du|/U < tol or max_steps, through the solve
-    server; then the same requests run one at a time with the FP64 plain
-    context (and with the FP16 context) for the same step counts."""
+    [1e3,1e5]), each run to max|du|/U < tol (checked every K steps) or
+    max_steps, through the solve server.  The serial baselines run each request
+    one at a time with the FP64 plain context (and with the FP16 context): each
+    request is timed over a bounded sample of min(steps, sample_steps) steps
+    after a warm-up, and its time is scaled to its served step count."""
     rng = np.random.default_rng(seed)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
     arrivals -= arrivals[0]
@@ -349,11 +351,14 @@ def serve_bench(torch, mg, n_req=24, rate=50.0, seed=1234, max_steps=2000, tol=1
                                     precision=form) if lid[q] else
                  mg.BuoyancyCavity(n, rayleigh=float(ra[q]), t_hot=0.5, t_cold=-0.5, precision=form))
             c.initial()
+            c.step(4)
+            steps = int(res[i]["steps"])
+            m = min(steps, sample_steps)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            c.step(int(res[i]["steps"]))
+            c.step(m)
             torch.cuda.synchronize()
-            tot += time.perf_counter() - t0
+            tot += (time.perf_counter() - t0) * steps / m
             c.close()
         return tot
 
@@ -362,6 +367,8 @@ def serve_bench(torch, mg, n_req=24, rate=50.0, seed=1234, max_steps=2000, tol=1
     agg = cells_done / span / 1e6
     return {"requests": n_req, "rate_per_s": rate, "seed": seed, "max_steps": max_steps,
             "tol": tol, "steps_per_iteration": K, "precision": precision,
+            "serial_sample_steps": sample_steps,
+            "steps_mean": round(float(np.mean([res[i]["steps"] for i in ids])), 1),
             "converged": int(sum(r["converged"] for r in res.values())),
             "p50_ms": round(float(np.percentile(lat, 50)), 2),
             "p99_ms": round(float(np.percentile(lat, 99)), 2),
@@ -540,7 +547,7 @@ def main():
     ap.add_argument("--only-lid2d", type=int, default=0, metavar="N",
                     help="time only the D2Q9 lid cavity at N^2 (--steps/--warmup; profiling runs)")
     ap.add_argument("--serve-requests", type=int, default=24)
-    ap.add_argument("--serve-max-steps", type=int, default=2000)
+    ap.add_argument("--serve-max-steps", type=int, default=50000)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     wl = dict(WORKLOADS[args.workload])

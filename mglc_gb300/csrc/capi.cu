@@ -6,6 +6,7 @@
 // carried body force (thermal), and a small reduction scratch.  All work runs
 // on the context's stream.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cmath>
 #include <cstdarg>
@@ -21,6 +22,17 @@
 #include "lid2d.cuh"
 
 using namespace mglc;
+
+namespace {
+// NVTX range around an entry point (visible in Nsight timelines; a no-op
+// unless a tool is attached)
+struct Range {
+    explicit Range(const char* name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+    Range(const Range&) = delete;
+    Range& operator=(const Range&) = delete;
+};
+}  // namespace
 
 struct mglc_ctx {
     int kind = 0, form = FORM_FP64;
@@ -430,6 +442,7 @@ int mglc_get_info(const mglc_ctx* c, mglc_info* o) {
 int particle_initial(mglc_ctx* c);
 
 int mglc_initial(mglc_ctx* c) {
+    Range nvtx_range("mglc_initial");
     if (!c || !c->kind) return MGLC_ERR_INVALID;
     if (c->kind == MGLC_KIND_PARTICLE) return particle_initial(c);
     if (c->p2d) {
@@ -493,6 +506,7 @@ int mglc_initial(mglc_ctx* c) {
 
 int mglc_load_state(mglc_ctx* c, const double* f, const double* g, const double* rho,
                     const double* u, const double* v, const double* w, const double* T) {
+    Range nvtx_range("mglc_load_state");
     if (!c || !c->kind || !f) return c ? fail(c, MGLC_ERR_INVALID, "f is required") : MGLC_ERR_INVALID;
     if (c->p2d) return fail(c, MGLC_ERR_UNSUPPORTED, "2-D particle contexts start from mglc_initial");
     if (c->l2d) {
@@ -546,6 +560,7 @@ int mglc_load_state(mglc_ctx* c, const double* f, const double* g, const double*
 }
 
 int mglc_get_f(mglc_ctx* c, double* f, double* g) {
+    Range nvtx_range("mglc_get_f");
     if (!c || !c->kind) return MGLC_ERR_INVALID;
     if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial or mglc_load_state first");
     if (c->p2d) return f ? p2d_get_f(c->p2d, f, c->err) : MGLC_OK;
@@ -559,6 +574,7 @@ int mglc_get_f(mglc_ctx* c, double* f, double* g) {
 }
 
 int mglc_step(mglc_ctx* c, int nsteps) {
+    Range nvtx_range("mglc_step");
     if (!c || !c->kind) return MGLC_ERR_INVALID;
     if (nsteps < 0) return fail(c, MGLC_ERR_INVALID, "nsteps must be >= 0");
     if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial or mglc_load_state first");
@@ -671,6 +687,7 @@ int mglc_get_macros_device(mglc_ctx* c, double* rho, double* u, double* v, doubl
 }
 
 int mglc_get_macros(mglc_ctx* c, double* rho, double* u, double* v, double* w, double* T) {
+    Range nvtx_range("mglc_get_macros");
     if (!c || !c->kind) return MGLC_ERR_INVALID;
     if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial or mglc_load_state first");
     if (c->p2d) return p2d_get_macros(c->p2d, rho, u, v, w, c->err);
@@ -688,6 +705,7 @@ int mglc_get_macros(mglc_ctx* c, double* rho, double* u, double* v, double* w, d
 }
 
 int mglc_check(mglc_ctx* c, double* error_u, double* error_t) {
+    Range nvtx_range("mglc_check");
     if (!c || !c->kind) return MGLC_ERR_INVALID;
     if (c->p2d) return fail(c, MGLC_ERR_UNSUPPORTED, "not available for 2-D particle contexts");
     if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial or mglc_load_state first");
@@ -719,6 +737,7 @@ int mglc_check(mglc_ctx* c, double* error_u, double* error_t) {
 }
 
 int mglc_totals(mglc_ctx* c, double* mass, double* energy, double* heat) {
+    Range nvtx_range("mglc_totals");
     if (!c || !c->kind) return MGLC_ERR_INVALID;
     if (!c->initialised) return fail(c, MGLC_ERR_STATE, "call mglc_initial or mglc_load_state first");
     if (c->p2d) return fail(c, MGLC_ERR_UNSUPPORTED, "not available for 2-D particle contexts");

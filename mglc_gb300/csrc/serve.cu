@@ -13,6 +13,7 @@
 // (threads per CTA, x-rows per tile, CTAs per SM) is chosen once by timing
 // candidates on a synthetic mix.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <chrono>
@@ -299,6 +300,12 @@ int build_graph(mglc_server* s) {
 // synthetic mix (one solve of each size, lid and heated alternating), issued
 // as an iteration issues them (heated beside lid): per candidate two warm-up
 // steps and eight timed ones, the best of two passes over all candidates.
+// NVTX range of one serving iteration (a no-op unless a tool is attached)
+struct IterRange {
+    IterRange() { nvtxRangePushA("serve iteration"); }
+    ~IterRange() { nvtxRangePop(); }
+};
+
 int autotune(mglc_server* s) {
     static const int sizes[] = {32, 48, 64, 96, 128};
     std::vector<Req> mix;
@@ -531,9 +538,12 @@ int mglc_server_run(mglc_server* s, double time_limit_s) {
         }
         if (now_s() - start > time_limit_s) return sfail(s, MGLC_ERR_STATE, "time limit reached");
         const double it0 = now_s();
-        SCK(cudaGraphLaunch(s->graph, s->stream), "graph launch");
-        SCK(cudaEventRecord(s->done, s->stream), "event record");
-        SCK(cudaEventSynchronize(s->done), "iteration");
+        {
+            IterRange nvtx_range;  // graph launch .. completion (NVTX)
+            SCK(cudaGraphLaunch(s->graph, s->stream), "graph launch");
+            SCK(cudaEventRecord(s->done, s->stream), "event record");
+            SCK(cudaEventSynchronize(s->done), "iteration");
+        }
         s->stats.busy_s += now_s() - it0;
         s->stats.iterations++;
         // retire converged solves and solves at the step cap

@@ -535,9 +535,10 @@ __device__ __forceinline__ void thermal_load_aa(int i, int j, int k, const S* f,
     const IDX cell = (IDX)i + (IDX)nx * ((IDX)j + (IDX)ny * (IDX)k);
     const IDX sy = (IDX)nx, sz = (IDX)nx * (IDX)ny;
     const unsigned bm = face_mask(i, j, k, nx, ny, nz);
+    // an interior cell (bm == 0) reads every population from upstream
     auto src = [&](int q) -> IDX {
         const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
-        if (!ODD || (bm & leave_bits(-dx, -dy, -dz)) != 0) return (IDX)q * P + cell;
+        if (!ODD || (bm != 0 && (bm & leave_bits(-dx, -dy, -dz)) != 0)) return (IDX)q * P + cell;
         return (IDX)opp19(q) * P + cell - (IDX)(dx + dy * (int)sy) - (IDX)dz * sz;
     };
     S raw[Q19];
