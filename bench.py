@@ -660,9 +660,15 @@ def main():
         mx = forms.get("fp16s", {})
         base = value if args.form == "fp64" else forms.get("fp64", {}).get("value")
         if "value" in mx and base:
+            # the in-place kernels compute the same bits; report the faster streaming
+            ip = forms.get("fp16s_in_place", {})
+            best, streaming = mx, "two buffers"
+            if ip.get("value", 0.0) > mx["value"]:
+                best, streaming = ip, "in place (AA pattern, one buffer)"
             line["mixed"] = {"form": "fp16 storage of f - w rho0 (stochastic rounding), fp32 arithmetic",
-                             "value": mx["value"], "unit": "MLUPS", "frac": mx["frac"],
-                             "speedup_vs_fp64_plain": round(mx["value"] / base, 2),
+                             "streaming": streaming,
+                             "value": best["value"], "unit": "MLUPS", "frac": best["frac"],
+                             "speedup_vs_fp64_plain": round(best["value"] / base, 2),
                              "u_rel_l2_vs_fp64": mx.get("u_rel_l2_vs_fp64"),
                              "error_steps": mx.get("error_steps"),
                              "within_1e-3": (mx["u_rel_l2_vs_fp64"] <= 1e-3)
