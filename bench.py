@@ -422,6 +422,47 @@ def lid2d_bench(torch, mg, n=1024, steps=400, warmup=20, cpu_s=3.0, cpu=True):
     return out
 
 
+def kernel_tour(torch, mg, steps=3):
+    """One small run of every step-kernel family (profiling runs: a launch list
+    of this covers all of them): lid and heated cavities in every form with two
+    buffers and in place, spheres, the 2-D cases and the server.  Sizes keep
+    each state above or near the 129 MB L2 while the whole tour holds a few GB."""
+    jobs = []
+    for form in ("fp64", "fx64", "fp32", "fp16", "fp16s", "bf16"):
+        for ip in (False, True):
+            jobs.append(("lid", form, ip, lambda f=form, i=ip: mg.LidDrivenCavity(
+                160, reynolds=1000.0, u0=0.1, top_layer_u0=False, precision=f, in_place=i)))
+    for form in ("fp64", "fx64", "fp32", "fp16", "fp16s"):
+        for ip in (False, True):
+            jobs.append(("heated", form, ip, lambda f=form, i=ip: mg.BuoyancyCavity(
+                128, rayleigh=1e5, t_hot=0.5, t_cold=-0.5, precision=f, in_place=i)))
+    cen = place_spheres(256, 128, 128, 200, 5.0, 2026)
+    for form in ("fp64", "fp32"):
+        jobs.append(("spheres", form, False, lambda f=form: mg.ParticleFlow(
+            256, 128, 128, cen, 5.0, tauf=0.65, rho_solid=1.2, periodic_x=True,
+            body_force=(1e-6, 0.0, 0.0), precision=f)))
+    jobs.append(("circles2d", "fp64", False, lambda: mg.ParticleFlow2D(
+        400, 800, [[100.3, 600.7], [200.9, 650.2], [300.1, 610.4]], 10.0, tauf=0.7, gravity=0.01)))
+    jobs.append(("shear2d", "fp64", False, lambda: mg.ShearFlow2D(
+        800, 400, [[200.4, 201.3]], 12.6)))
+    jobs.append(("lid2d", "fp64", False, lambda: mg.LidDrivenCavity2D(1024, reynolds=1000.0)))
+    done = []
+    for kind, form, ip, make in jobs:
+        with make() as c:
+            c.initial()
+            c.step(steps)
+            c.macro()
+        torch.cuda.synchronize()
+        done.append(f"{kind}:{form}{':in_place' if ip else ''}")
+    with mg.SolveServer(hbm_budget_gb=2.0, max_active=8, precision="fp16", steps_per_iteration=4,
+                        tol=1e-12, max_steps=8, autotune=False) as srv:
+        srv.submit("lid", 64, reynolds=400.0)
+        srv.submit("thermal", 48, rayleigh=1e4)
+        srv.run()
+    done.append("serve:fp16")
+    return done
+
+
 def cpu_sample(wl, target_s=10.0):
     """The oracle (restatement of the reference's CPU code) with OpenMP on all
     host cores, on a bounded sample of the workload."""
@@ -542,6 +583,8 @@ def main():
     ap.add_argument("--error-steps", type=int, default=0,
                     help="steps for the error runs (default: the workload's own count)")
     ap.add_argument("--no-lid2d", action="store_true", help="skip the D2Q9 lid cavity line")
+    ap.add_argument("--kernel-tour", action="store_true",
+                    help="run every step-kernel family once on a small case (profiling runs)")
     ap.add_argument("--in-place", action="store_true",
                     help="time the main line with the in-place (AA-pattern, one-buffer) kernels")
     ap.add_argument("--only-lid2d", type=int, default=0, metavar="N",
@@ -574,6 +617,9 @@ def main():
     B.build()
     mglc_gb300.lib()
 
+    if args.kernel_tour:
+        print(json.dumps({"kernel_tour": kernel_tour(torch, mglc_gb300)}))
+        return 0
     if args.only_lid2d:
         print(json.dumps({"lid2d": lid2d_bench(torch, mglc_gb300, n=args.only_lid2d,
                                                steps=args.steps, warmup=args.warmup,

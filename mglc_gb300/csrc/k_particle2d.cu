@@ -45,6 +45,10 @@ struct D2 {
     double *xc, *uc, *om, *xco, *uco, *omo, *force, *torque;  // np x 3
     double* ravg;                                             // [0] current average
     int* status;                                              // [0] code, [1] particle
+    // boundary links of the current mask, per (node, direction 1..8): the
+    // circle that owns the solid end (-1: none) and calQ's q, x0, y0
+    int* lc;
+    double* lq;  // 3 doubles per link
 };
 
 __device__ __forceinline__ int IX(const D2& d, int i, int j) { return (i + 2) + d.X * (j + 2); }
@@ -175,18 +179,242 @@ __global__ void k2_walls(D2 d) {
     }
 }
 
+// Sequential FP64 sums computed in parallel, bit for bit.  While the running
+// sum s stays inside one binade [2^E, 2^(E+1)) and the addends are finite and
+// non-negative, s is an integer S times u = 2^(E-52) with S in [2^52, 2^53),
+// and RN(s + x) = (S + k) u where k is x/u rounded to an integer: down below
+// one half, up above it, and on an exact half to the k that makes S + k even
+// (ties to even).  Only the tie case reads the running sum, and only its
+// parity, so an addend is a map from the incoming parity to (increment,
+// outgoing parity); maps compose associatively, and an ordered tree reduction
+// of a chunk's maps gives the chunk's sum.  A chunk that may leave the binade
+// (or holds a negative or non-finite addend) is added one element at a time.
+struct GridSeg {
+    long long i0, i1;  // increment in units of u for incoming parity 0 / 1
+    int o0, o1;        // outgoing parity for incoming parity 0 / 1
+};
+
+__device__ __forceinline__ GridSeg seg_identity() { return GridSeg{0, 0, 0, 1}; }
+
+// a followed by b
+__device__ __forceinline__ GridSeg seg_cat(const GridSeg& a, const GridSeg& b) {
+    GridSeg r;
+    r.i0 = a.i0 + (a.o0 ? b.i1 : b.i0);
+    r.o0 = a.o0 ? b.o1 : b.o0;
+    r.i1 = a.i1 + (a.o1 ? b.i1 : b.i0);
+    r.o1 = a.o1 ? b.o1 : b.o0;
+    return r;
+}
+
+__device__ __forceinline__ GridSeg seg_shfl_down(const GridSeg& g, int off) {
+    GridSeg r;
+    r.i0 = __shfl_down_sync(0xffffffffu, g.i0, off);
+    r.i1 = __shfl_down_sync(0xffffffffu, g.i1, off);
+    r.o0 = __shfl_down_sync(0xffffffffu, g.o0, off);
+    r.o1 = __shfl_down_sync(0xffffffffu, g.o1, off);
+    return r;
+}
+
+// ordered reduction over a warp: lane 0 ends with lane 0's map, then lane 1's, ...
+__device__ __forceinline__ GridSeg seg_warp_reduce(GridSeg g) {
+    for (int off = 1; off < 32; off <<= 1) {
+        const GridSeg o = seg_shfl_down(g, off);
+        if ((threadIdx.x & 31) + off < 32 && ((threadIdx.x & 31) & (2 * off - 1)) == 0)
+            g = seg_cat(g, o);
+    }
+    return g;
+}
+
+constexpr long long MANT52 = (1LL << 52) - 1;
+constexpr int NO_BINADE = 100000;
+
+// the map of addend x (bits xb) on the grid of binade e (u = 2^(e-52)), from
+// the bit pattern with integer operations only; false when x must be added the
+// plain way (sign bit set, infinite or NaN, or x >= 2^(e+1)).  ub is an upper
+// bound of the increment.
+__device__ __forceinline__ bool seg_of(long long xb, int e, GridSeg& g, long long& ub) {
+    if (xb < 0) return false;
+    const int ex = (int)(xb >> 52);
+    if (ex == 2047) return false;
+    const long long M = (xb & MANT52) | (ex ? (1LL << 52) : 0);  // x = M 2^(max(ex,1)-1075)
+    const int sh = max(ex, 1) - 1023 - e;                         // x / u = M 2^sh
+    if (sh > 0) return false;
+    long long m;
+    int cls = 0;  // fraction of x / u: 0 below one half, 1 above, 2 exactly one half
+    if (sh == 0) {
+        m = M;
+    } else if (sh >= -62) {
+        const int k = -sh;
+        m = M >> k;
+        const long long rem = M & ((1LL << k) - 1), half = 1LL << (k - 1);
+        cls = rem > half ? 1 : (rem == half ? 2 : 0);
+    } else {
+        m = 0;  // x < u / 2
+    }
+    if (cls == 2) {
+        g.i0 = m + (m & 1);
+        g.i1 = m + ((m + 1) & 1);
+        g.o0 = g.o1 = 0;
+        ub = m + 1;
+    } else {
+        const long long v = m + cls;
+        g.i0 = g.i1 = v;
+        g.o0 = (int)(v & 1);
+        g.o1 = (int)((v + 1) & 1);
+        ub = v;
+    }
+    return true;
+}
+
+// binade of a positive normal running sum, NO_BINADE when the grid path is off
+__device__ __forceinline__ int binade_of(double acc) {
+    const long long b = __double_as_longlong(acc);
+    const int e = (int)((b >> 52) & 0x7ff) - 1023;
+    return (acc > 0.0 && e >= -900 && e <= 1000) ? e : NO_BINADE;
+}
+
+// acc + (the chunk whose composed map is h and increment bound hb) on binade e;
+// false when the sum may leave the binade
+__device__ __forceinline__ bool grid_apply(double& acc, int e, const GridSeg& h, long long hb) {
+    const long long S = (__double_as_longlong(acc) & MANT52) | (1LL << 52);
+    if (!(hb < (1LL << 53) - S)) return false;
+    const long long S1 = S + ((S & 1) ? h.i1 : h.i0);
+    acc = __longlong_as_double(((long long)(e + 1023) << 52) | (S1 & MANT52));
+    return true;
+}
+
 // average density over the fluid nodes of mask, in the reference's loop order
-__global__ void k2_rho_avg(D2 d, const int* mask) {
+// and with its sequential rounding (the grid sums above; one block, EPT
+// consecutive addends per thread).  A chunk the block cannot take whole is
+// taken by warp 0 in pieces of 32, and a piece that crosses a binade by lane 0
+// one addend at a time.
+constexpr int SB = 1024;  // threads of the ordered sweeps (one block)
+constexpr int EPT = 4;    // nodes per thread and chunk
+constexpr int CH = SB * EPT;
+__global__ void __launch_bounds__(SB) k2_rho_avg(D2 d, const int* mask) {
     if (d.status[0]) return;
-    double acc = 0.0;
-    long long n = 0;
-    for (int j = 1; j <= d.p.ny; j++)
-        for (int i = 1; i <= d.p.nx; i++)
-            if (mask[IX(d, i, j)] == 0) {
-                acc = acc + d.rho[IX(d, i, j)];
-                n = n + 1;
+    __shared__ double sr[CH];
+    __shared__ unsigned char sm[CH];  // 1 = fluid
+    __shared__ GridSeg wseg[SB / 32];
+    __shared__ long long wub[SB / 32];
+    __shared__ int wbad[SB / 32], wcnt[SB / 32];
+    __shared__ double s_acc;
+    __shared__ int s_e;
+    const int nx = d.p.nx;
+    const long long total = (long long)nx * d.p.ny;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        s_acc = 0.0;
+        s_e = NO_BINADE;
+    }
+    long long n = 0;  // fluid nodes (thread 0)
+    auto fetch = [&](long long t, bool& fl, double& x) {
+        fl = false;
+        x = 0.0;
+        if (t < total) {
+            const int j = 1 + (int)(t / nx), i = 1 + (int)(t % nx);
+            fl = mask[IX(d, i, j)] == 0;
+            x = d.rho[IX(d, i, j)];
+        }
+    };
+    bool fc[EPT];
+    double xc[EPT];
+#pragma unroll
+    for (int u = 0; u < EPT; u++) fetch((long long)threadIdx.x * EPT + u, fc[u], xc[u]);
+    __syncthreads();
+    for (long long base = 0; base < total; base += CH) {
+        bool fn[EPT];
+        double xn[EPT];
+#pragma unroll
+        for (int u = 0; u < EPT; u++)  // next chunk, ahead of use
+            fetch(base + CH + (long long)threadIdx.x * EPT + u, fn[u], xn[u]);
+        const int e = s_e;
+        GridSeg g = seg_identity();
+        long long ub = 0;
+        bool bad = e == NO_BINADE;
+        int cnt = 0;
+#pragma unroll
+        for (int u = 0; u < EPT; u++) {
+            sm[threadIdx.x * EPT + u] = fc[u];
+            sr[threadIdx.x * EPT + u] = xc[u];
+            cnt += fc[u];
+            if (!bad && fc[u]) {
+                GridSeg gu;
+                long long bu;
+                if (seg_of(__double_as_longlong(xc[u]), e, gu, bu)) {
+                    g = seg_cat(g, gu);
+                    ub += bu;
+                } else {
+                    bad = true;
+                }
             }
-    d.ravg[0] = acc / (double)n;
+        }
+        g = seg_warp_reduce(g);
+        for (int off = 16; off > 0; off >>= 1) {
+            ub += __shfl_down_sync(0xffffffffu, ub, off);
+            cnt += __shfl_down_sync(0xffffffffu, cnt, off);
+        }
+        const int wb = __any_sync(0xffffffffu, bad);
+        if (lane == 0) {
+            wseg[w] = g;
+            wub[w] = ub;
+            wbad[w] = wb;
+            wcnt[w] = cnt;
+        }
+        __syncthreads();
+        if (w == 0) {
+            GridSeg h = wseg[lane];
+            long long hb = wub[lane];
+            int hc = wcnt[lane];
+            const int hbad = __any_sync(0xffffffffu, wbad[lane]);
+            h = seg_warp_reduce(h);
+            for (int off = 16; off > 0; off >>= 1) {
+                hb += __shfl_down_sync(0xffffffffu, hb, off);
+                hc += __shfl_down_sync(0xffffffffu, hc, off);
+            }
+            double acc = s_acc;
+            int done = 0;
+            if (lane == 0) {
+                n += hc;
+                done = !hbad && grid_apply(acc, e, h, hb);
+            }
+            if (!__shfl_sync(0xffffffffu, done, 0)) {
+                int ep = e;
+                const int m = (int)min((long long)CH, total - base);
+                for (int p = 0; p < m; p += 32) {
+                    const int q = p + lane;
+                    const bool fl = q < m && sm[q];
+                    GridSeg gp = seg_identity();
+                    long long up = 0;
+                    bool bp = ep == NO_BINADE;
+                    if (!bp && fl) bp = !seg_of(__double_as_longlong(sr[q]), ep, gp, up);
+                    gp = seg_warp_reduce(gp);
+                    for (int off = 16; off > 0; off >>= 1) up += __shfl_down_sync(0xffffffffu, up, off);
+                    const int anyb = __any_sync(0xffffffffu, bp);
+                    if (lane == 0) {
+                        if (anyb || !grid_apply(acc, ep, gp, up)) {
+                            const int mp = min(32, m - p);
+                            for (int r = 0; r < mp; r++)
+                                if (sm[p + r]) acc = acc + sr[p + r];
+                        }
+                        ep = binade_of(acc);
+                    }
+                    ep = __shfl_sync(0xffffffffu, ep, 0);
+                }
+            }
+            if (lane == 0) {
+                s_acc = acc;
+                s_e = binade_of(acc);
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < EPT; u++) {
+            fc[u] = fn[u];
+            xc[u] = xn[u];
+        }
+    }
+    if (threadIdx.x == 0) d.ravg[0] = s_acc / (double)n;
 }
 
 // calQ / calQ2 from node (x, y) along direction a towards circle c
@@ -299,40 +527,91 @@ __global__ void k2_macro(D2 d) {
 
 // calForce (particle_force.F90:35-190): one thread per circle; its links are
 // visited in the reference's global loop order restricted to its box
+// calQ of every boundary link of the current mask, one thread per fluid node,
+// for the force sums below (which visit a circle's links one at a time in the
+// reference's loop order); the values are calq's, so the sums are unchanged
+__global__ void k2_links(D2 d) {
+    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x, j = 1 + blockIdx.y;
+    if (i > d.p.nx || d.status[0] || d.ob[IX(d, i, j)] != 0) return;
+    for (int a = 1; a < 9; a++) {
+        const int ip = i + c_ex[a], jp = j + c_ey[a];
+        if (d.ob[IX(d, ip, jp)] != 1) continue;
+        const size_t li = (size_t)IX(d, i, j) * 8 + (a - 1);
+        int owner = -1;
+        for (int c = 0; c < d.p.np && owner < 0; c++)
+            if (inside(d, d.xc, c, (double)ip, (double)jp)) owner = c;
+        d.lc[li] = owner;
+        if (owner < 0) continue;
+        double x0, y0, q;
+        if (!calq(d, owner, (double)i, (double)j, a, x0, y0, q)) {
+            fail(d, S_Q, owner);
+            return;
+        }
+        d.lq[3 * li] = x0;
+        d.lq[3 * li + 1] = y0;
+        d.lq[3 * li + 2] = q;
+    }
+}
+
+// one warp per circle: the lanes evaluate 32 consecutive candidate links (j
+// outer, i, direction inner: the reference's loop order) at a time, and every
+// lane then adds the valid ones in that order, so the sums are the sequential ones
 __global__ void k2_force(D2 d) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.x, lane = threadIdx.x;
     if (c >= d.p.np || d.status[0]) return;
     const P2Params& p = d.p;
     const double PI = p.pi, R0 = p.radius, ravg = d.ravg[0];
     const double xcc = d.xc[3 * c], ycc = d.xc[3 * c + 1];
     const int i0 = max(1, (int)floor(xcc - R0) - 2), i1 = min(p.nx, (int)ceil(xcc + R0) + 2);
     const int j0 = max(1, (int)floor(ycc - R0) - 2), j1 = min(p.ny, (int)ceil(ycc + R0) + 2);
+    const int ni = max(0, i1 - i0 + 1), nj = max(0, j1 - j0 + 1);
+    const long long ncand = (long long)ni * nj * 8;
+    const double Om = d.om[3 * c + 2], U0 = d.uc[3 * c], U1 = d.uc[3 * c + 1];
     double fs0 = 0.0, fs1 = 0.0, ts = 0.0;
-    for (int j = j0; j <= j1; j++)
-        for (int i = i0; i <= i1; i++) {
-            if (d.ob[IX(d, i, j)] != 0) continue;
-            for (int a = 1; a < 9; a++) {
-                const int ip = i + c_ex[a], jp = j + c_ey[a];
-                if (d.ob[IX(d, ip, jp)] != 1) continue;
-                if (!inside(d, d.xc, c, (double)ip, (double)jp)) continue;
+    for (long long base = 0; base < ncand; base += 32) {
+        const long long k = base + lane;
+        bool ok = false, bad = false;
+        double Fx = 0.0, Fy = 0.0, T = 0.0;
+        if (k < ncand) {
+            const int a = 1 + (int)(k % 8);
+            const int i = i0 + (int)((k / 8) % ni), j = j0 + (int)(k / 8 / ni);
+            const int ip = i + c_ex[a], jp = j + c_ey[a];
+            if (d.ob[IX(d, i, j)] == 0 && d.ob[IX(d, ip, jp)] == 1 &&
+                inside(d, d.xc, c, (double)ip, (double)jp)) {
                 double x0, y0, q;
-                if (!calq(d, c, (double)i, (double)j, a, x0, y0, q)) {
-                    fail(d, S_Q, c);
-                    return;
+                const size_t li = (size_t)IX(d, i, j) * 8 + (a - 1);
+                if (d.lc[li] == c) {  // from k2_links
+                    x0 = d.lq[3 * li];
+                    y0 = d.lq[3 * li + 1];
+                    q = d.lq[3 * li + 2];
+                    ok = true;
+                } else {
+                    ok = calq(d, c, (double)i, (double)j, a, x0, y0, q);
+                    bad = !ok;
                 }
-                const double Om = d.om[3 * c + 2];
-                const double rot0 = -(y0 - ycc) * Om, rot1 = (x0 - xcc) * Om;
-                const int ra = c_r[a];
-                const double U0 = d.uc[3 * c], U1 = d.uc[3 * c + 1];
-                const double Fx = (c_ex[a] - U0 - rot0) * FP(d, a, i, j) - (c_ex[ra] - U0 - rot0) * F(d, ra, i, j);
-                const double Fy = (c_ey[a] - U1 - rot1) * FP(d, a, i, j) - (c_ey[ra] - U1 - rot1) * F(d, ra, i, j);
-                const double rx = x0 - xcc, ry = y0 - ycc;
-                const double T = rx * Fy - ry * Fx;
-                fs0 = fs0 + Fx;
-                fs1 = fs1 + Fy;
-                ts = ts + T;
+                (void)q;
+                if (ok) {
+                    const double rot0 = -(y0 - ycc) * Om, rot1 = (x0 - xcc) * Om;
+                    const int ra = c_r[a];
+                    Fx = (c_ex[a] - U0 - rot0) * FP(d, a, i, j) - (c_ex[ra] - U0 - rot0) * F(d, ra, i, j);
+                    Fy = (c_ey[a] - U1 - rot1) * FP(d, a, i, j) - (c_ey[ra] - U1 - rot1) * F(d, ra, i, j);
+                    const double rx = x0 - xcc, ry = y0 - ycc;
+                    T = rx * Fy - ry * Fx;
+                }
             }
         }
+        if (__any_sync(0xffffffffu, bad)) {
+            if (lane == 0) fail(d, S_Q, c);
+            return;
+        }
+        for (unsigned v = __ballot_sync(0xffffffffu, ok); v; v &= v - 1) {
+            const int l = __ffs(v) - 1;
+            fs0 = fs0 + __shfl_sync(0xffffffffu, Fx, l);
+            fs1 = fs1 + __shfl_sync(0xffffffffu, Fy, l);
+            ts = ts + __shfl_sync(0xffffffffu, T, l);
+        }
+    }
+    if (lane != 0) return;
     if (p.variant == P2_SHEAR) {  // case1 particle_force.F90:86-92: momentum exchange only
         d.force[3 * c] = fs0;
         d.force[3 * c + 1] = fs1;
@@ -435,83 +714,144 @@ __global__ void k2_mask(D2 d, int* mask, bool set_macro) {
     }
 }
 
-// refill of nodes that left a circle (particle_update.F90:122-193), in the
-// reference's sequential sweep order (each refill may read an earlier one)
-__global__ void k2_refill(D2 d) {
-    if (d.status[0]) return;
+// refill of nodes that left a circle (particle_update.F90:122-193) for one
+// node; false when it failed (status set)
+__device__ bool refill_node(const D2& d, int i, int j, double ra) {
     const P2Params& p = d.p;
-    const double ra = d.ravg[0];
-    for (int j = 1; j <= p.ny; j++)
-        for (int i = 1; i <= p.nx; i++) {
-            if (!(d.ob[IX(d, i, j)] == 1 && d.on[IX(d, i, j)] == 0)) continue;
-            bool found = false;
-            for (int c = 0; c < p.np; c++) {
-                if (!inside(d, d.xco, c, (double)i, (double)j)) continue;
-                found = true;
-                const double xc = d.xc[3 * c], yc = d.xc[3 * c + 1];
-                double out = 0.0;
-                int ec = 0;
-                for (int a = 1; a < 9; a++) {
-                    const double t = ((i - xc) * c_ex[a] + (j - yc) * c_ey[a]) /
-                                     sqrt((i - xc) * (i - xc) + (j - yc) * (j - yc));
-                    if (t > out) {
-                        out = t;
-                        ec = a;
-                    }
-                }
-                if (ec == 0) {
-                    fail(d, S_NO_DIR, c);
-                    return;
-                }
-                const int e0 = c_ex[ec], e1 = c_ey[ec];
-                const int i1 = wxi(d, i + e0), i2 = wxi(d, i + 2 * e0), i3 = wxi(d, i + 3 * e0);
-                for (int a = 0; a < 9; a++) {
-                    if (p.linear)  // case1 particle_update.F90:115-119
-                        F(d, a, i, j) = 2.0 * F(d, a, i1, j + e1) - F(d, a, i2, j + 2 * e1);
-                    else
-                        F(d, a, i, j) = 3.0 * F(d, a, i1, j + e1) - 3.0 * F(d, a, i2, j + 2 * e1) +
-                                        F(d, a, i3, j + 3 * e1);
-                }
-                double G[9], m[9];
-                for (int a = 0; a < 9; a++) G[a] = F(d, a, i, j);
-                m[0] = G[0] + G[1] + G[2] + G[3] + G[4] + G[5] + G[6] + G[7] + G[8];
-                m[1] = -4.0 * G[0] - G[1] - G[2] - G[3] - G[4] + 2.0 * G[5] + 2.0 * G[6] + 2.0 * G[7] + 2.0 * G[8];
-                m[2] = 4.0 * G[0] - 2.0 * G[1] - 2.0 * G[2] - 2.0 * G[3] - 2.0 * G[4] + G[5] + G[6] + G[7] + G[8];
-                if (p.variant == P2_SHEAR) {  // case1 :130,132: the first circle's (Uc, Vc)
-                    m[3] = ra * d.uc[0];
-                    m[5] = ra * d.uc[1];
-                } else {
-                    m[3] = ra * (d.uc[3 * c] - (j - yc) * d.om[3 * c + 2]);
-                    m[5] = ra * (d.uc[3 * c + 1] + (i - xc) * d.om[3 * c + 2]);
-                }
-                m[4] = -2.0 * G[1] + 2.0 * G[3] + G[5] - G[6] - G[7] + G[8];
-                m[6] = -2.0 * G[2] + 2.0 * G[4] + G[5] + G[6] - G[7] - G[8];
-                m[7] = G[1] - G[2] + G[3] - G[4];
-                m[8] = G[5] - G[6] + G[7] - G[8];
-                G[0] = (m[0] - m[1] + m[2]) / 9.0;
-                G[1] = m[0] / 9.0 - m[1] / 36.0 - m[2] / 18.0 + m[3] / 6.0 - m[4] / 6.0 + m[7] * 0.25;
-                G[2] = m[0] / 9.0 - m[1] / 36.0 - m[2] / 18.0 + m[5] / 6.0 - m[6] / 6.0 - m[7] * 0.25;
-                G[3] = m[0] / 9.0 - m[1] / 36.0 - m[2] / 18.0 - m[3] / 6.0 + m[4] / 6.0 + m[7] * 0.25;
-                G[4] = m[0] / 9.0 - m[1] / 36.0 - m[2] / 18.0 - m[5] / 6.0 + m[6] / 6.0 - m[7] * 0.25;
-                G[5] = m[0] / 9.0 + m[1] / 18.0 + m[2] / 36.0 + m[3] / 6.0 + m[4] / 12.0 + m[5] / 6.0 +
-                       m[6] / 12.0 + m[8] * 0.25;
-                G[6] = m[0] / 9.0 + m[1] / 18.0 + m[2] / 36.0 - m[3] / 6.0 - m[4] / 12.0 + m[5] / 6.0 +
-                       m[6] / 12.0 - m[8] * 0.25;
-                G[7] = m[0] / 9.0 + m[1] / 18.0 + m[2] / 36.0 - m[3] / 6.0 - m[4] / 12.0 - m[5] / 6.0 -
-                       m[6] / 12.0 + m[8] * 0.25;
-                G[8] = m[0] / 9.0 + m[1] / 18.0 + m[2] / 36.0 + m[3] / 6.0 + m[4] / 12.0 - m[5] / 6.0 -
-                       m[6] / 12.0 - m[8] * 0.25;
-                for (int a = 0; a < 9; a++) F(d, a, i, j) = G[a];
-                const double r = G[0] + G[1] + G[2] + G[3] + G[4] + G[5] + G[6] + G[7] + G[8];
-                d.rho[IX(d, i, j)] = r;
-                d.u[IX(d, i, j)] = (G[1] - G[3] + G[5] - G[6] - G[7] + G[8]) / r;
-                d.v[IX(d, i, j)] = (G[2] - G[4] + G[5] + G[6] - G[7] - G[8]) / r;
-            }
-            if (!found) {
-                fail(d, S_NO_OWNER, -1);
-                return;
+    bool found = false;
+    for (int c = 0; c < p.np; c++) {
+        if (!inside(d, d.xco, c, (double)i, (double)j)) continue;
+        found = true;
+        const double xc = d.xc[3 * c], yc = d.xc[3 * c + 1];
+        double out = 0.0;
+        int ec = 0;
+        for (int a = 1; a < 9; a++) {
+            const double t = ((i - xc) * c_ex[a] + (j - yc) * c_ey[a]) /
+                             sqrt((i - xc) * (i - xc) + (j - yc) * (j - yc));
+            if (t > out) {
+                out = t;
+                ec = a;
             }
         }
+        if (ec == 0) {
+            fail(d, S_NO_DIR, c);
+            return false;
+        }
+        const int e0 = c_ex[ec], e1 = c_ey[ec];
+        const int i1 = wxi(d, i + e0), i2 = wxi(d, i + 2 * e0), i3 = wxi(d, i + 3 * e0);
+        for (int a = 0; a < 9; a++) {
+            if (p.linear)  // case1 particle_update.F90:115-119
+                F(d, a, i, j) = 2.0 * F(d, a, i1, j + e1) - F(d, a, i2, j + 2 * e1);
+            else
+                F(d, a, i, j) = 3.0 * F(d, a, i1, j + e1) - 3.0 * F(d, a, i2, j + 2 * e1) +
+                                F(d, a, i3, j + 3 * e1);
+        }
+        double G[9], m[9];
+        for (int a = 0; a < 9; a++) G[a] = F(d, a, i, j);
+        m[0] = G[0] + G[1] + G[2] + G[3] + G[4] + G[5] + G[6] + G[7] + G[8];
+        m[1] = -4.0 * G[0] - G[1] - G[2] - G[3] - G[4] + 2.0 * G[5] + 2.0 * G[6] + 2.0 * G[7] + 2.0 * G[8];
+        m[2] = 4.0 * G[0] - 2.0 * G[1] - 2.0 * G[2] - 2.0 * G[3] - 2.0 * G[4] + G[5] + G[6] + G[7] + G[8];
+        if (p.variant == P2_SHEAR) {  // case1 :130,132: the first circle's (Uc, Vc)
+            m[3] = ra * d.uc[0];
+            m[5] = ra * d.uc[1];
+        } else {
+            m[3] = ra * (d.uc[3 * c] - (j - yc) * d.om[3 * c + 2]);
+            m[5] = ra * (d.uc[3 * c + 1] + (i - xc) * d.om[3 * c + 2]);
+        }
+        m[4] = -2.0 * G[1] + 2.0 * G[3] + G[5] - G[6] - G[7] + G[8];
+        m[6] = -2.0 * G[2] + 2.0 * G[4] + G[5] + G[6] - G[7] - G[8];
+        m[7] = G[1] - G[2] + G[3] - G[4];
+        m[8] = G[5] - G[6] + G[7] - G[8];
+        G[0] = (m[0] - m[1] + m[2]) / 9.0;
+        G[1] = m[0] / 9.0 - m[1] / 36.0 - m[2] / 18.0 + m[3] / 6.0 - m[4] / 6.0 + m[7] * 0.25;
+        G[2] = m[0] / 9.0 - m[1] / 36.0 - m[2] / 18.0 + m[5] / 6.0 - m[6] / 6.0 - m[7] * 0.25;
+        G[3] = m[0] / 9.0 - m[1] / 36.0 - m[2] / 18.0 - m[3] / 6.0 + m[4] / 6.0 + m[7] * 0.25;
+        G[4] = m[0] / 9.0 - m[1] / 36.0 - m[2] / 18.0 - m[5] / 6.0 + m[6] / 6.0 - m[7] * 0.25;
+        G[5] = m[0] / 9.0 + m[1] / 18.0 + m[2] / 36.0 + m[3] / 6.0 + m[4] / 12.0 + m[5] / 6.0 +
+               m[6] / 12.0 + m[8] * 0.25;
+        G[6] = m[0] / 9.0 + m[1] / 18.0 + m[2] / 36.0 - m[3] / 6.0 - m[4] / 12.0 + m[5] / 6.0 +
+               m[6] / 12.0 - m[8] * 0.25;
+        G[7] = m[0] / 9.0 + m[1] / 18.0 + m[2] / 36.0 - m[3] / 6.0 - m[4] / 12.0 - m[5] / 6.0 -
+               m[6] / 12.0 + m[8] * 0.25;
+        G[8] = m[0] / 9.0 + m[1] / 18.0 + m[2] / 36.0 + m[3] / 6.0 + m[4] / 12.0 - m[5] / 6.0 -
+               m[6] / 12.0 - m[8] * 0.25;
+        for (int a = 0; a < 9; a++) F(d, a, i, j) = G[a];
+        const double r = G[0] + G[1] + G[2] + G[3] + G[4] + G[5] + G[6] + G[7] + G[8];
+        d.rho[IX(d, i, j)] = r;
+        d.u[IX(d, i, j)] = (G[1] - G[3] + G[5] - G[6] - G[7] + G[8]) / r;
+        d.v[IX(d, i, j)] = (G[2] - G[4] + G[5] + G[6] - G[7] - G[8]) / r;
+    }
+    if (!found) {
+        fail(d, S_NO_OWNER, -1);
+        return false;
+    }
+    return true;
+}
+
+// The refill sweep in the reference's order: each refill may read an earlier
+// one, so one thread refills; the block finds the nodes to refill (left a
+// circle: solid before, fluid now) chunk by chunk with an ordered compaction.
+__global__ void __launch_bounds__(SB) k2_refill(D2 d) {
+    if (d.status[0]) return;
+    __shared__ int list[SB];
+    __shared__ int wcount[SB / 32];
+    __shared__ int nlist, stop;
+    const int nx = d.p.nx;
+    const long long total = (long long)nx * d.p.ny;
+    const double ra = d.ravg[0];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x == 0) stop = 0;
+    auto left = [&](long long t) {  // solid before, fluid now
+        if (t >= total) return false;
+        const int j = 1 + (int)(t / nx), i = 1 + (int)(t % nx);
+        return d.ob[IX(d, i, j)] == 1 && d.on[IX(d, i, j)] == 0;
+    };
+    // chunks of EPT sub-chunks of SB nodes; flags of the next chunk are read ahead
+    bool fnext[EPT];
+#pragma unroll
+    for (int u = 0; u < EPT; u++) fnext[u] = left((long long)u * SB + threadIdx.x);
+    for (long long cbase = 0; cbase < total; cbase += CH) {
+        bool fcur[EPT];
+        bool any = false;
+#pragma unroll
+        for (int u = 0; u < EPT; u++) {
+            fcur[u] = fnext[u];
+            any = any || fcur[u];
+            fnext[u] = left(cbase + CH + (long long)u * SB + threadIdx.x);
+        }
+        if (!__syncthreads_or(any)) continue;  // most chunks have none
+        for (int u = 0; u < EPT; u++) {
+            const long long t = cbase + (long long)u * SB + threadIdx.x;
+            const bool flag = fcur[u];
+            if (!__syncthreads_or(flag)) continue;
+            const unsigned bal = __ballot_sync(0xffffffffu, flag);
+            if (lane == 0) wcount[w] = __popc(bal);
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                int acc = 0;
+                for (int q = 0; q < SB / 32; q++) {
+                    const int c = wcount[q];
+                    wcount[q] = acc;
+                    acc += c;
+                }
+                nlist = acc;
+            }
+            __syncthreads();
+            if (flag) list[wcount[w] + __popc(bal & ((1u << lane) - 1u))] = (int)t;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                for (int q = 0; q < nlist; q++) {
+                    const int node = list[q];
+                    if (!refill_node(d, 1 + node % nx, 1 + node / nx, ra)) {
+                        stop = 1;
+                        break;
+                    }
+                }
+            }
+            __syncthreads();
+            if (stop) return;
+        }
+    }
 }
 
 // initial.F90:103-188 with the centres given by the caller: mask, rho = rho_s
@@ -616,6 +956,7 @@ int p2d_create(const P2Params& p, const double* centers_xy, P2Ctx** out, std::st
     double** pa[] = {&d.xc, &d.uc, &d.om, &d.xco, &d.uco, &d.omo, &d.force, &d.torque};
     for (double** a : pa)
         if ((rc = dal(c, a, np3, err))) return rc;
+    if ((rc = dal(c, &d.lc, 8 * cells, err)) || (rc = dal(c, &d.lq, 24 * cells, err))) return rc;
     if ((rc = dal(c, &d.ravg, 2, err)) || (rc = dal(c, &d.status, 2, err)) ||
         (rc = dal(c, &c->owner_tmp, (size_t)p.nx * p.ny, err)))
         return rc;
@@ -631,7 +972,7 @@ void p2d_destroy(P2Ctx* c) {
     if (!c) return;
     D2& d = c->d;
     void* ps[] = {d.f, d.fp, d.rho, d.u, d.v, d.ob, d.on, d.xc, d.uc, d.om, d.xco, d.uco, d.omo,
-                  d.force, d.torque, d.ravg, d.status, c->owner_tmp};
+                  d.force, d.torque, d.ravg, d.status, d.lc, d.lq, c->owner_tmp};
     if (c->s) cudaStreamSynchronize(c->s);
     for (void* p : ps)
         if (p) cudaFree(p);
@@ -690,16 +1031,17 @@ int p2d_step(P2Ctx* c, int nsteps, std::string& err) {
         k2_collide<<<g, 128, 0, c->s>>>(d);
         k2_stream<<<g, 128, 0, c->s>>>(d);
         k2_walls<<<(nw + 127) / 128, 128, 0, c->s>>>(d);
-        k2_rho_avg<<<1, 1, 0, c->s>>>(d, d.ob);
+        k2_rho_avg<<<1, SB, 0, c->s>>>(d, d.ob);
         k2_ibb<<<g, 128, 0, c->s>>>(d);
         k2_macro<<<g, 128, 0, c->s>>>(d);
         if (d.p.np > 0) {
-            k2_force<<<pg, 64, 0, c->s>>>(d);
+            k2_links<<<g, 128, 0, c->s>>>(d);
+            k2_force<<<d.p.np, 32, 0, c->s>>>(d);
             k2_move<<<pg, 64, 0, c->s>>>(d);
         }
         k2_mask<<<dim3((d.p.nx + 2 + 127) / 128, d.p.ny + 2), 128, 0, c->s>>>(d, d.on, true);
-        k2_rho_avg<<<1, 1, 0, c->s>>>(d, d.on);
-        k2_refill<<<1, 1, 0, c->s>>>(d);
+        k2_rho_avg<<<1, SB, 0, c->s>>>(d, d.on);
+        k2_refill<<<1, SB, 0, c->s>>>(d);
         cudaMemcpyAsync(d.ob, d.on, cells * sizeof(int), cudaMemcpyDeviceToDevice, c->s);
         c->itc++;
     }
