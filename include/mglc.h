@@ -368,6 +368,17 @@ int mglc_residual_noalloc(long long n, const double* u, const double* v, const d
                           int with_w, void* cuda_stream, double* error_u, double* error_t,
                           char* errbuf, int errbuf_len);
 
+/* ---- sequential sums ------------------------------------------------------ */
+/* No counterpart in the reference's interface: the primitive behind the 2-D
+ * particle step's density averages (the rhoAvg loops of case4
+ * seq_piece/particle_bounceback.F90:14-26 and particle_update.F90:80-92, run
+ * single-threaded), exposed so it can be tested on its own.
+ * *sum = x[t0] + x[t1] + ... over the t with keep[t] != 0, in increasing t,
+ * rounded after every addition exactly as that loop rounds it, computed in
+ * parallel on the GPU; *count = the number of kept addends.  x and keep are
+ * HOST arrays of n entries.  Synchronises the device. */
+int mglc_sequential_sum(const double* x, const int* keep, int n, double* sum, long long* count);
+
 #ifdef __cplusplus
 }
 #endif

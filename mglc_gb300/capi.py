@@ -142,6 +142,7 @@ SIGNATURES = {
     "mglc_nure_destroy": ([_VP], None),
     "mglc_nure_push": ([_VP, _D, _D, ctypes.POINTER(NuReStatus)], _I),
     "mglc_nure_sample": ([_VP, _VP, ctypes.POINTER(NuReStatus)], _I),
+    "mglc_sequential_sum": ([_VP, _VP, _I, _DP, ctypes.POINTER(_LL)], _I),
 }
 
 _lib = None

@@ -273,8 +273,8 @@ __device__ __forceinline__ int binade_of(double acc) {
     return (acc > 0.0 && e >= -900 && e <= 1000) ? e : NO_BINADE;
 }
 
-// acc + (the chunk whose composed map is h and increment bound hb) on binade e;
-// false when the sum may leave the binade
+// acc + (the addends whose composed map is h and increment bound hb) on binade
+// e; false when the sum may leave the binade
 __device__ __forceinline__ bool grid_apply(double& acc, int e, const GridSeg& h, long long hb) {
     const long long S = (__double_as_longlong(acc) & MANT52) | (1LL << 52);
     if (!(hb < (1LL << 53) - S)) return false;
@@ -283,138 +283,199 @@ __device__ __forceinline__ bool grid_apply(double& acc, int e, const GridSeg& h,
     return true;
 }
 
-// average density over the fluid nodes of mask, in the reference's loop order
-// and with its sequential rounding (the grid sums above; one block, EPT
-// consecutive addends per thread).  A chunk the block cannot take whole is
-// taken by warp 0 in pieces of 32, and a piece that crosses a binade by lane 0
-// one addend at a time.
+__device__ __forceinline__ long long warp_incl_scan(long long x) {
+    const int lane = threadIdx.x & 31;
+    for (int off = 1; off < 32; off <<= 1) {
+        const long long y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= off) x += y;
+    }
+    return x;
+}
+
+__device__ __forceinline__ GridSeg seg_select(bool keep, const GridSeg& g) {
+    return keep ? g : seg_identity();
+}
+
+// Warp 0 adds the addends [lo, hi) of sr (where sm is set) to acc (held by
+// lane 0) in order, 32 at a time: the lanes up to the first addend that cannot
+// take the grid path of the current binade (it is not finite and non-negative,
+// or the sum may leave the binade) are added as one map, that addend the plain
+// way, and the rest start over on the new binade.
+__device__ void warp_sum_pieces(const double* sr, const unsigned char* sm, int lo, int hi,
+                                double& acc) {
+    const int lane = threadIdx.x & 31;
+    for (int p = lo; p < hi; p += 32) {
+        int lstart = 0;
+        while (lstart < 32) {
+            const double a0 = __shfl_sync(0xffffffffu, acc, 0);
+            const int ep = binade_of(a0);
+            const long long S = ep == NO_BINADE ? 0 : (__double_as_longlong(a0) & MANT52) | (1LL << 52);
+            const int q = p + lane;
+            const bool valid = lane >= lstart && q < hi && sm[q];
+            GridSeg g = seg_identity();
+            long long ub = 0;
+            bool bad = false;
+            if (valid) bad = ep == NO_BINADE || !seg_of(__double_as_longlong(sr[q]), ep, g, ub);
+            const long long incl = warp_incl_scan(ub);
+            const bool ok = !bad && (ep == NO_BINADE || incl < (1LL << 53) - S);
+            const unsigned nb = __ballot_sync(0xffffffffu, !ok);
+            const int lstar = nb ? __ffs(nb) - 1 : 32;
+            const GridSeg h = seg_warp_reduce(seg_select(lane < lstar, g));
+            const long long hb = __shfl_sync(0xffffffffu, incl, lstar > 0 ? lstar - 1 : 0);
+            if (lane == 0) {
+                if (ep != NO_BINADE && lstar > 0) grid_apply(acc, ep, h, hb);
+                if (lstar < 32) acc = acc + sr[p + lstar];
+            }
+            lstart = lstar + 1;
+        }
+    }
+}
+
+// The sequential sum x_0 + x_1 + ... over the addends t = 0..total-1 that
+// fetch(t, keep, x) keeps, with the rounding of that order (the grid sums
+// above; one block of SB threads, EPT consecutive addends per thread).  The
+// warps of a chunk up to the first one holding an addend that cannot take the
+// grid path are added as one map, that warp's addends by warp 0
+// (warp_sum_pieces), and the rest start over.  Thread 0 returns the sum and
+// the number of kept addends.
 constexpr int SB = 1024;  // threads of the ordered sweeps (one block)
-constexpr int EPT = 4;    // nodes per thread and chunk
+constexpr int EPT = 4;    // addends per thread and chunk
 constexpr int CH = SB * EPT;
-__global__ void __launch_bounds__(SB) k2_rho_avg(D2 d, const int* mask) {
-    if (d.status[0]) return;
+template <class Fetch>
+__device__ void ordered_sum_block(int total, Fetch fetch, double& sum, long long& count) {
     __shared__ double sr[CH];
     __shared__ unsigned char sm[CH];  // 1 = fluid
     __shared__ GridSeg wseg[SB / 32];
     __shared__ long long wub[SB / 32];
     __shared__ int wbad[SB / 32], wcnt[SB / 32];
     __shared__ double s_acc;
-    __shared__ int s_e;
-    const int nx = d.p.nx;
-    const long long total = (long long)nx * d.p.ny;
+    __shared__ int s_next;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (threadIdx.x == 0) {
-        s_acc = 0.0;
-        s_e = NO_BINADE;
-    }
+    if (threadIdx.x == 0) s_acc = 0.0;
     long long n = 0;  // fluid nodes (thread 0)
-    auto fetch = [&](long long t, bool& fl, double& x) {
-        fl = false;
-        x = 0.0;
-        if (t < total) {
-            const int j = 1 + (int)(t / nx), i = 1 + (int)(t % nx);
-            fl = mask[IX(d, i, j)] == 0;
-            x = d.rho[IX(d, i, j)];
-        }
-    };
     bool fc[EPT];
     double xc[EPT];
 #pragma unroll
-    for (int u = 0; u < EPT; u++) fetch((long long)threadIdx.x * EPT + u, fc[u], xc[u]);
+    for (int u = 0; u < EPT; u++) fetch(threadIdx.x * EPT + u, fc[u], xc[u]);
     __syncthreads();
-    for (long long base = 0; base < total; base += CH) {
+    for (int base = 0; base < total; base += CH) {
         bool fn[EPT];
         double xn[EPT];
 #pragma unroll
         for (int u = 0; u < EPT; u++)  // next chunk, ahead of use
-            fetch(base + CH + (long long)threadIdx.x * EPT + u, fn[u], xn[u]);
-        const int e = s_e;
-        GridSeg g = seg_identity();
-        long long ub = 0;
-        bool bad = e == NO_BINADE;
+            fetch(base + CH + threadIdx.x * EPT + u, fn[u], xn[u]);
         int cnt = 0;
 #pragma unroll
         for (int u = 0; u < EPT; u++) {
             sm[threadIdx.x * EPT + u] = fc[u];
             sr[threadIdx.x * EPT + u] = xc[u];
             cnt += fc[u];
-            if (!bad && fc[u]) {
-                GridSeg gu;
-                long long bu;
-                if (seg_of(__double_as_longlong(xc[u]), e, gu, bu)) {
-                    g = seg_cat(g, gu);
-                    ub += bu;
-                } else {
-                    bad = true;
-                }
-            }
         }
-        g = seg_warp_reduce(g);
-        for (int off = 16; off > 0; off >>= 1) {
-            ub += __shfl_down_sync(0xffffffffu, ub, off);
-            cnt += __shfl_down_sync(0xffffffffu, cnt, off);
-        }
-        const int wb = __any_sync(0xffffffffu, bad);
-        if (lane == 0) {
-            wseg[w] = g;
-            wub[w] = ub;
-            wbad[w] = wb;
-            wcnt[w] = cnt;
-        }
-        __syncthreads();
-        if (w == 0) {
-            GridSeg h = wseg[lane];
-            long long hb = wub[lane];
-            int hc = wcnt[lane];
-            const int hbad = __any_sync(0xffffffffu, wbad[lane]);
-            h = seg_warp_reduce(h);
-            for (int off = 16; off > 0; off >>= 1) {
-                hb += __shfl_down_sync(0xffffffffu, hb, off);
-                hc += __shfl_down_sync(0xffffffffu, hc, off);
-            }
-            double acc = s_acc;
-            int done = 0;
-            if (lane == 0) {
-                n += hc;
-                done = !hbad && grid_apply(acc, e, h, hb);
-            }
-            if (!__shfl_sync(0xffffffffu, done, 0)) {
-                int ep = e;
-                const int m = (int)min((long long)CH, total - base);
-                for (int p = 0; p < m; p += 32) {
-                    const int q = p + lane;
-                    const bool fl = q < m && sm[q];
-                    GridSeg gp = seg_identity();
-                    long long up = 0;
-                    bool bp = ep == NO_BINADE;
-                    if (!bp && fl) bp = !seg_of(__double_as_longlong(sr[q]), ep, gp, up);
-                    gp = seg_warp_reduce(gp);
-                    for (int off = 16; off > 0; off >>= 1) up += __shfl_down_sync(0xffffffffu, up, off);
-                    const int anyb = __any_sync(0xffffffffu, bp);
-                    if (lane == 0) {
-                        if (anyb || !grid_apply(acc, ep, gp, up)) {
-                            const int mp = min(32, m - p);
-                            for (int r = 0; r < mp; r++)
-                                if (sm[p + r]) acc = acc + sr[p + r];
-                        }
-                        ep = binade_of(acc);
+        for (int off = 16; off > 0; off >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, off);
+        if (lane == 0) wcnt[w] = cnt;
+        int startw = 0;
+        for (;;) {
+            const int e = binade_of(s_acc);
+            GridSeg g = seg_identity();
+            long long ub = 0;
+            bool bad = false;
+            if (w >= startw) {
+#pragma unroll
+                for (int u = 0; u < EPT; u++) {
+                    if (!fc[u] || bad) continue;
+                    GridSeg gu;
+                    long long bu;
+                    if (e != NO_BINADE && seg_of(__double_as_longlong(xc[u]), e, gu, bu)) {
+                        g = seg_cat(g, gu);
+                        ub += bu;
+                    } else {
+                        bad = true;
                     }
-                    ep = __shfl_sync(0xffffffffu, ep, 0);
                 }
             }
+            g = seg_warp_reduce(g);
+            for (int off = 16; off > 0; off >>= 1) ub += __shfl_down_sync(0xffffffffu, ub, off);
+            const int wb = __any_sync(0xffffffffu, bad);
             if (lane == 0) {
-                s_acc = acc;
-                s_e = binade_of(acc);
+                wseg[w] = g;
+                wub[w] = ub;
+                wbad[w] = wb;
             }
+            __syncthreads();
+            if (w == 0) {
+                double acc = s_acc;
+                const long long S = e == NO_BINADE ? 0 : (__double_as_longlong(acc) & MANT52) | (1LL << 52);
+                const long long incl = warp_incl_scan(wub[lane]);
+                const bool ok = lane < startw ||
+                                (!wbad[lane] && e != NO_BINADE && incl < (1LL << 53) - S);
+                const unsigned nb = __ballot_sync(0xffffffffu, !ok);
+                const int wstar = nb ? __ffs(nb) - 1 : 32;
+                const GridSeg h = seg_warp_reduce(seg_select(lane < wstar, wseg[lane]));
+                const long long hb = __shfl_sync(0xffffffffu, incl, wstar > 0 ? wstar - 1 : 0);
+                if (lane == 0) {
+                    if (startw == 0) {
+                        int c = 0;
+                        for (int q = 0; q < 32; q++) c += wcnt[q];
+                        n += c;
+                    }
+                    if (e != NO_BINADE && wstar > startw) grid_apply(acc, e, h, hb);
+                }
+                if (wstar < 32) {
+                    const int lo = wstar * 32 * EPT;
+                    warp_sum_pieces(sr, sm, lo, min(lo + 32 * EPT, total - base), acc);
+                }
+                if (lane == 0) {
+                    s_acc = acc;
+                    s_next = wstar >= 31 ? 32 : wstar + 1;
+                }
+            }
+            __syncthreads();
+            startw = s_next;
+            if (startw >= 32) break;
         }
-        __syncthreads();
 #pragma unroll
         for (int u = 0; u < EPT; u++) {
             fc[u] = fn[u];
             xc[u] = xn[u];
         }
     }
-    if (threadIdx.x == 0) d.ravg[0] = s_acc / (double)n;
+    sum = s_acc;
+    count = n;
+}
+
+// average density over the fluid nodes of mask, in the reference's loop order
+// and with its sequential rounding
+__global__ void __launch_bounds__(SB) k2_rho_avg(D2 d, const int* mask) {
+    if (d.status[0]) return;
+    const int nx = d.p.nx;
+    const int total = nx * d.p.ny;  // 2-D grids stay far below 2^31 nodes
+    double sum;
+    long long n;
+    ordered_sum_block(total, [&](int t, bool& fl, double& x) {
+        fl = false;
+        x = 0.0;
+        if (t < total) {
+            const int j = 1 + t / nx, i = 1 + t % nx;
+            fl = mask[IX(d, i, j)] == 0;
+            x = d.rho[IX(d, i, j)];
+        }
+    }, sum, n);
+    if (threadIdx.x == 0) d.ravg[0] = sum / (double)n;
+}
+
+// the same sequential sum over x[t] where keep[t] != 0 (out: sum, count)
+__global__ void __launch_bounds__(SB) k_ordered_sum(const double* x, const int* keep, int total,
+                                                    double* out) {
+    double sum;
+    long long n;
+    ordered_sum_block(total, [&](int t, bool& fl, double& v) {
+        fl = t < total && keep[t] != 0;
+        v = t < total ? x[t] : 0.0;
+    }, sum, n);
+    if (threadIdx.x == 0) {
+        out[0] = sum;
+        out[1] = (double)n;
+    }
 }
 
 // calQ / calQ2 from node (x, y) along direction a towards circle c
@@ -1124,3 +1185,30 @@ double p2d_rho_avg(P2Ctx* c) {
 }
 
 }  // namespace mglc
+
+extern "C" int mglc_sequential_sum(const double* x, const int* keep, int n, double* sum,
+                                   long long* count) {
+    if (n < 0 || !x || !keep || !sum || !count) return MGLC_ERR_INVALID;
+    double* dx = nullptr;
+    int* dk = nullptr;
+    double* dout = nullptr;
+    const size_t m = n > 0 ? (size_t)n : 1;
+    cudaError_t e = cudaMalloc(&dx, m * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&dk, m * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&dout, 2 * sizeof(double));
+    if (e == cudaSuccess && n > 0) e = cudaMemcpy(dx, x, (size_t)n * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && n > 0) e = cudaMemcpy(dk, keep, (size_t)n * sizeof(int), cudaMemcpyHostToDevice);
+    double out[2] = {0.0, 0.0};
+    if (e == cudaSuccess) {
+        mglc::k_ordered_sum<<<1, mglc::SB>>>(dx, dk, n, dout);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, dout, sizeof out, cudaMemcpyDeviceToHost);
+    cudaFree(dx);
+    cudaFree(dk);
+    cudaFree(dout);
+    if (e != cudaSuccess) return MGLC_ERR_CUDA;
+    *sum = out[0];
+    *count = (long long)out[1];
+    return MGLC_OK;
+}

@@ -78,3 +78,74 @@ def test_wall_penetration_is_reported(mg):
 def test_circle_outside_the_box_is_rejected(mg):
     with pytest.raises(mg.MglcError):
         mg.ParticleFlow2D(40, 40, [[3.0, 20.0]], 6.0)
+
+
+def _seq_sum(x, keep):
+    s = 0.0
+    for v, k in zip(x.tolist(), keep.tolist()):
+        if k:
+            s = s + v
+    return s
+
+
+def _gpu_seq_sum(x, keep):
+    import ctypes
+
+    from mglc_gb300 import capi
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    keep = np.ascontiguousarray(keep, dtype=np.int32)
+    s, n = ctypes.c_double(), ctypes.c_longlong()
+    capi.check(None, capi.lib().mglc_sequential_sum(x.ctypes.data, keep.ctypes.data, x.size,
+                                                     ctypes.byref(s), ctypes.byref(n)))
+    return s.value, n.value
+
+
+def _addends(kind, n, rng):
+    if kind == "near_one":  # densities: the 2-D particle step's own case
+        return 1.0 + 1e-3 * (rng.random(n) - 0.5)
+    if kind == "ties":  # few mantissa bits: many exact half-ulp ties
+        return np.ldexp(rng.integers(0, 4096, n).astype(np.float64), -12) + 0.5
+    if kind == "scales":  # addends across 40 binades, the sum crossing many
+        return np.ldexp(rng.random(n), rng.integers(-20, 20, n))
+    if kind == "negative":
+        x = 3.0 * rng.random(n)
+        x[rng.random(n) < 0.002] *= -1.0
+        return x
+    if kind == "tiny":  # subnormal and zero addends between normal ones
+        x = 1.0 + 1e-6 * rng.random(n)
+        x[1::2] = 1e-300 * rng.random(x[1::2].size)
+        x[::7] = 0.0
+        x[::11] = np.ldexp(1.0, -1070)
+        return x
+    if kind == "specials":
+        x = np.ones(n)
+        x[::5000] = np.inf
+        x[::3333] = np.nan
+        return x
+    if kind == "signed_zero":
+        x = np.full(n, -0.0)
+        x[n // 2:] = 1.0
+        return x
+    raise ValueError(kind)
+
+
+@pytest.mark.parametrize("kind", ["near_one", "ties", "scales", "negative", "tiny", "specials",
+                                  "signed_zero"])
+@pytest.mark.parametrize("n", [1, 31, 4097, 70001, 320000])
+def test_sequential_sum_is_the_loop_order_sum_bitwise(mg, kind, n):
+    """The parallel grid sum behind the density averages against the plain
+    left-to-right loop, on addends chosen to hit its every path: ties to even,
+    binade crossings, negative, subnormal, signed-zero and non-finite addends."""
+    rng = np.random.default_rng(n * 7 + len(kind))
+    x = _addends(kind, n, rng)
+    keep = (rng.random(n) >= 0.1).astype(np.int32)
+    got, cnt = _gpu_seq_sum(x, keep)
+    want = _seq_sum(x, keep)
+    assert cnt == int(keep.sum())
+    assert np.array([got]).view(np.int64)[0] == np.array([want]).view(np.int64)[0] or (
+        np.isnan(got) and np.isnan(want)), (got, want)
+
+
+def test_sequential_sum_empty(mg):
+    got, cnt = _gpu_seq_sum(np.zeros(0), np.zeros(0, np.int32))
+    assert cnt == 0 and got == 0.0 and not np.signbit(got)
