@@ -422,6 +422,51 @@ def lid2d_bench(torch, mg, n=1024, steps=400, warmup=20, cpu_s=3.0, cpu=True):
     return out
 
 
+def particles2d_bench(torch, mg, steps=200, warmup=10, cpu_steps=20, cpu=True):
+    """The D2Q9 moving-particle steps of the reference's 2-D programs (FP64,
+    bitwise the reference's statements): case4's three settling circles at
+    400x800 and case1's circle in a sheared channel at 800x400.  Device ms per
+    step between CUDA events on the context's stream; the oracle (single
+    thread, like the reference's sequential build) on a bounded sample."""
+    cen = [[100.3, 600.7], [200.9, 650.2], [300.1, 610.4]]
+    cases = (("circles2d", "case4: 3 settling circles, 400x800, R=10, FP64 bitwise",
+              lambda: mg.ParticleFlow2D(400, 800, cen, 10.0, tauf=0.7, gravity=0.01)),
+             ("shear2d", "case1: 1 circle in a sheared channel, 800x400, R=12.6, FP64 bitwise",
+              lambda: mg.ShearFlow2D(800, 400, [[200.4, 201.3]], 12.6)))
+    out = {}
+    for key, desc, make in cases:
+        c = make()
+        stream = torch.cuda.Stream()
+        c.set_stream(stream.cuda_stream)
+        c.initial()
+        c.step(warmup)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        c.step(steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        c.set_stream(None)
+        c.close()
+        out[key] = {"workload": desc, "value": round(320000 * steps / (ms * 1e-3) / 1e6, 1),
+                    "unit": "MLUPS", "steps": steps, "ms_per_step": round(ms / steps, 4)}
+    if cpu:
+        import numpy as np
+        from oracle import oracle as O
+        o = O.ParticleOracle(np.array([[x, y, 0.0] for x, y in cen]), dim=2, nx=400, ny=800, nz=1,
+                             tauf=0.7, rho_solid=1.01, radius=10.0, gravity=(0.0, -0.01, 0.0),
+                             qmode=0)
+        t0 = time.perf_counter()
+        o.step(cpu_steps)
+        dt = time.perf_counter() - t0
+        out["circles2d"]["cpu_baseline"] = {
+            "value": round(320000 * cpu_steps / dt / 1e6, 2), "unit": "MLUPS", "cores": 1,
+            "kind": "port", "ms_per_step": round(dt / cpu_steps * 1e3, 3),
+            "sample": f"{cpu_steps} steps of the same case (oracle, one thread)"}
+    return out
+
+
 def kernel_tour(torch, mg, steps=3):
     """One small run of every step-kernel family (profiling runs: a launch list
     of this covers all of them): lid and heated cavities in every form with two
@@ -583,6 +628,8 @@ def main():
     ap.add_argument("--error-steps", type=int, default=0,
                     help="steps for the error runs (default: the workload's own count)")
     ap.add_argument("--no-lid2d", action="store_true", help="skip the D2Q9 lid cavity line")
+    ap.add_argument("--only-particles2d", action="store_true",
+                    help="time only the D2Q9 particle cases (--steps/--warmup; no CPU sample)")
     ap.add_argument("--kernel-tour", action="store_true",
                     help="run every step-kernel family once on a small case (profiling runs)")
     ap.add_argument("--in-place", action="store_true",
@@ -617,6 +664,10 @@ def main():
     B.build()
     mglc_gb300.lib()
 
+    if args.only_particles2d:
+        print(json.dumps({"particles2d": particles2d_bench(torch, mglc_gb300, steps=args.steps,
+                                                           warmup=args.warmup, cpu=False)}))
+        return 0
     if args.kernel_tour:
         print(json.dumps({"kernel_tour": kernel_tour(torch, mglc_gb300)}))
         return 0
@@ -724,6 +775,7 @@ def main():
                                     max_steps=args.serve_max_steps)
     if rank == 0 and not args.no_lid2d and wl["kind"] == "lid":
         line["lid2d"] = lid2d_bench(torch, mglc_gb300)
+        line["particles2d"] = particles2d_bench(torch, mglc_gb300)
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_sample(wl)
     if rank == 0:
