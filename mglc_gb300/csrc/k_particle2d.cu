@@ -49,6 +49,12 @@ struct D2 {
     // circle that owns the solid end (-1: none) and calQ's q, x0, y0
     int* lc;
     double* lq;  // 3 doubles per link
+    // per-chunk records of the ordered density sums (GsBuf)
+    double *gs_part, *gs_pre;
+    void* gs_map;  // GridSeg[nch]
+    long long* gs_ub;
+    int *gs_e, *gs_flag, *gs_cnt;
+    int *rf_count, *rf_list;  // nodes to refill: count, list of RF_CAP
 };
 
 __device__ __forceinline__ int IX(const D2& d, int i, int j) { return (i + 2) + d.X * (j + 2); }
@@ -331,151 +337,349 @@ __device__ void warp_sum_pieces(const double* sr, const unsigned char* sm, int l
     }
 }
 
-// The sequential sum x_0 + x_1 + ... over the addends t = 0..total-1 that
-// fetch(t, keep, x) keeps, with the rounding of that order (the grid sums
-// above; one block of SB threads, EPT consecutive addends per thread).  The
-// warps of a chunk up to the first one holding an addend that cannot take the
-// grid path are added as one map, that warp's addends by warp 0
-// (warp_sum_pieces), and the rest start over.  Thread 0 returns the sum and
-// the number of kept addends.
+// The sequential sum x_0 + x_1 + ... over the addends t = 0..total-1 that a
+// fetch functor keeps (fetch(t, keep, x)), with the rounding of that order,
+// in chunks of CH addends (EPT consecutive addends per thread of an SB-thread
+// block):
+//   k_gs_part  (one block per chunk) plain partial sums (any order) and counts;
+//   k_gs_scan  (one block) their exclusive prefix: an estimate of the running
+//              sum where each chunk starts, hence of its binade;
+//   k_gs_map   (one block per chunk) the chunk's composed grid map on that
+//              binade, with its increment bound;
+//   k_gs_apply (one block) walks the chunks in order: a chunk whose binade
+//              estimate is the exact running sum's binade, whose addends all
+//              took the grid path and whose bound keeps the sum in the binade
+//              is added as its map; any other chunk is added by chunk_split.
+// chunk_split adds one chunk with the whole block: the warps up to the first
+// one holding an addend that cannot take the grid path of the current binade
+// are added as one map, that warp's addends by warp 0 (warp_sum_pieces), and
+// the rest start over on the new binade.
 constexpr int SB = 1024;  // threads of the ordered sweeps (one block)
 constexpr int EPT = 4;    // addends per thread and chunk
 constexpr int CH = SB * EPT;
-template <class Fetch>
-__device__ void ordered_sum_block(int total, Fetch fetch, double& sum, long long& count) {
-    __shared__ double sr[CH];
-    __shared__ unsigned char sm[CH];  // 1 = fluid
-    __shared__ GridSeg wseg[SB / 32];
-    __shared__ long long wub[SB / 32];
-    __shared__ int wbad[SB / 32], wcnt[SB / 32];
-    __shared__ double s_acc;
-    __shared__ int s_next;
+constexpr long long UB_CAP = 1LL << 61;  // saturation of chunk increment bounds
+
+struct SumShared {
+    double sr[CH];
+    unsigned char sm[CH];  // 1 = kept
+    GridSeg wseg[SB / 32];
+    long long wub[SB / 32];
+    int wbad[SB / 32];
+    double acc;  // the running sum
+    int next;
+};
+
+// per-chunk records of the pipeline (nch entries each)
+struct GsBuf {
+    double *part, *pre;
+    GridSeg* map;
+    long long* ub;
+    int *e, *flag, *cnt;  // flag: 0 map valid, 1 plain path needed, 2 no kept addend
+};
+
+// adds the chunk at base (this thread's addends fc/xc) to sh.acc; all threads
+// call it; it ends with a barrier
+__device__ void chunk_split(int base, int total, const bool (&fc)[EPT], const double (&xc)[EPT],
+                            SumShared& sh) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (threadIdx.x == 0) s_acc = 0.0;
-    long long n = 0;  // fluid nodes (thread 0)
-    bool fc[EPT];
-    double xc[EPT];
 #pragma unroll
-    for (int u = 0; u < EPT; u++) fetch(threadIdx.x * EPT + u, fc[u], xc[u]);
-    __syncthreads();
-    for (int base = 0; base < total; base += CH) {
-        bool fn[EPT];
-        double xn[EPT];
-#pragma unroll
-        for (int u = 0; u < EPT; u++)  // next chunk, ahead of use
-            fetch(base + CH + threadIdx.x * EPT + u, fn[u], xn[u]);
-        int cnt = 0;
-#pragma unroll
-        for (int u = 0; u < EPT; u++) {
-            sm[threadIdx.x * EPT + u] = fc[u];
-            sr[threadIdx.x * EPT + u] = xc[u];
-            cnt += fc[u];
-        }
-        for (int off = 16; off > 0; off >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, off);
-        if (lane == 0) wcnt[w] = cnt;
-        int startw = 0;
-        for (;;) {
-            const int e = binade_of(s_acc);
-            GridSeg g = seg_identity();
-            long long ub = 0;
-            bool bad = false;
-            if (w >= startw) {
-#pragma unroll
-                for (int u = 0; u < EPT; u++) {
-                    if (!fc[u] || bad) continue;
-                    GridSeg gu;
-                    long long bu;
-                    if (e != NO_BINADE && seg_of(__double_as_longlong(xc[u]), e, gu, bu)) {
-                        g = seg_cat(g, gu);
-                        ub += bu;
-                    } else {
-                        bad = true;
-                    }
-                }
-            }
-            g = seg_warp_reduce(g);
-            for (int off = 16; off > 0; off >>= 1) ub += __shfl_down_sync(0xffffffffu, ub, off);
-            const int wb = __any_sync(0xffffffffu, bad);
-            if (lane == 0) {
-                wseg[w] = g;
-                wub[w] = ub;
-                wbad[w] = wb;
-            }
-            __syncthreads();
-            if (w == 0) {
-                double acc = s_acc;
-                const long long S = e == NO_BINADE ? 0 : (__double_as_longlong(acc) & MANT52) | (1LL << 52);
-                const long long incl = warp_incl_scan(wub[lane]);
-                const bool ok = lane < startw ||
-                                (!wbad[lane] && e != NO_BINADE && incl < (1LL << 53) - S);
-                const unsigned nb = __ballot_sync(0xffffffffu, !ok);
-                const int wstar = nb ? __ffs(nb) - 1 : 32;
-                const GridSeg h = seg_warp_reduce(seg_select(lane < wstar, wseg[lane]));
-                const long long hb = __shfl_sync(0xffffffffu, incl, wstar > 0 ? wstar - 1 : 0);
-                if (lane == 0) {
-                    if (startw == 0) {
-                        int c = 0;
-                        for (int q = 0; q < 32; q++) c += wcnt[q];
-                        n += c;
-                    }
-                    if (e != NO_BINADE && wstar > startw) grid_apply(acc, e, h, hb);
-                }
-                if (wstar < 32) {
-                    const int lo = wstar * 32 * EPT;
-                    warp_sum_pieces(sr, sm, lo, min(lo + 32 * EPT, total - base), acc);
-                }
-                if (lane == 0) {
-                    s_acc = acc;
-                    s_next = wstar >= 31 ? 32 : wstar + 1;
-                }
-            }
-            __syncthreads();
-            startw = s_next;
-            if (startw >= 32) break;
-        }
-#pragma unroll
-        for (int u = 0; u < EPT; u++) {
-            fc[u] = fn[u];
-            xc[u] = xn[u];
-        }
+    for (int u = 0; u < EPT; u++) {
+        sh.sm[threadIdx.x * EPT + u] = fc[u];
+        sh.sr[threadIdx.x * EPT + u] = xc[u];
     }
-    sum = s_acc;
-    count = n;
+    int startw = 0;
+    for (;;) {
+        const int e = binade_of(sh.acc);
+        GridSeg g = seg_identity();
+        long long ub = 0;  // at most 128 bounds below 2^53 per warp: no overflow
+        bool bad = false;
+        if (w >= startw) {
+#pragma unroll
+            for (int u = 0; u < EPT; u++) {
+                if (!fc[u] || bad) continue;
+                GridSeg gu;
+                long long bu;
+                if (e != NO_BINADE && seg_of(__double_as_longlong(xc[u]), e, gu, bu)) {
+                    g = seg_cat(g, gu);
+                    ub += bu;
+                } else {
+                    bad = true;
+                }
+            }
+        }
+        g = seg_warp_reduce(g);
+        for (int off = 16; off > 0; off >>= 1) ub += __shfl_down_sync(0xffffffffu, ub, off);
+        const int wb = __any_sync(0xffffffffu, bad);
+        if (lane == 0) {
+            sh.wseg[w] = g;
+            sh.wub[w] = ub;
+            sh.wbad[w] = wb;
+        }
+        __syncthreads();
+        if (w == 0) {
+            double acc = sh.acc;
+            const long long S = e == NO_BINADE ? 0 : (__double_as_longlong(acc) & MANT52) | (1LL << 52);
+            // the prefix grows by at most 2^60 a lane, so it cannot wrap before
+            // the first lane past the bound, and only lanes before that are used
+            const long long incl = warp_incl_scan(sh.wub[lane]);
+            const bool ok = lane < startw ||
+                            (!sh.wbad[lane] && e != NO_BINADE && incl < (1LL << 53) - S);
+            const unsigned nb = __ballot_sync(0xffffffffu, !ok);
+            const int wstar = nb ? __ffs(nb) - 1 : 32;
+            const GridSeg h = seg_warp_reduce(seg_select(lane < wstar, sh.wseg[lane]));
+            const long long hb = __shfl_sync(0xffffffffu, incl, wstar > 0 ? wstar - 1 : 0);
+            if (lane == 0 && e != NO_BINADE && wstar > startw) grid_apply(acc, e, h, hb);
+            if (wstar < 32) {
+                const int lo = wstar * 32 * EPT;
+                warp_sum_pieces(sh.sr, sh.sm, lo, min(lo + 32 * EPT, total - base), acc);
+            }
+            if (lane == 0) {
+                sh.acc = acc;
+                sh.next = wstar >= 31 ? 32 : wstar + 1;
+            }
+        }
+        __syncthreads();
+        startw = sh.next;
+        if (startw >= 32) break;
+    }
 }
 
-// average density over the fluid nodes of mask, in the reference's loop order
-// and with its sequential rounding
-__global__ void __launch_bounds__(SB) k2_rho_avg(D2 d, const int* mask) {
-    if (d.status[0]) return;
-    const int nx = d.p.nx;
-    const int total = nx * d.p.ny;  // 2-D grids stay far below 2^31 nodes
-    double sum;
-    long long n;
-    ordered_sum_block(total, [&](int t, bool& fl, double& x) {
+template <class Fetch>
+__global__ void __launch_bounds__(SB) k_gs_part(Fetch fetch, int total, GsBuf b) {
+    __shared__ double ws[SB / 32];
+    __shared__ int wc[SB / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, c = blockIdx.x;
+    double v = 0.0;
+    int n = 0;
+#pragma unroll
+    for (int u = 0; u < EPT; u++) {
+        bool fl;
+        double x;
+        fetch(c * CH + threadIdx.x * EPT + u, fl, x);
+        if (fl) {
+            v += x;
+            n++;
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        v += __shfl_down_sync(0xffffffffu, v, off);
+        n += __shfl_down_sync(0xffffffffu, n, off);
+    }
+    if (lane == 0) {
+        ws[w] = v;
+        wc[w] = n;
+    }
+    __syncthreads();
+    if (w == 0) {
+        v = ws[lane];
+        n = wc[lane];
+        for (int off = 16; off > 0; off >>= 1) {
+            v += __shfl_down_sync(0xffffffffu, v, off);
+            n += __shfl_down_sync(0xffffffffu, n, off);
+        }
+        if (lane == 0) {
+            b.part[c] = v;
+            b.cnt[c] = n;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(SB) k_gs_scan(GsBuf b, int nch) {
+    __shared__ double ws[SB / 32];
+    __shared__ double carry;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x == 0) carry = 0.0;
+    __syncthreads();
+    for (int base = 0; base < nch; base += SB) {
+        const int c = base + threadIdx.x;
+        const double own = c < nch ? b.part[c] : 0.0;
+        double v = own;
+        for (int off = 1; off < 32; off <<= 1) {
+            const double y = __shfl_up_sync(0xffffffffu, v, off);
+            if (lane >= off) v += y;
+        }
+        if (lane == 31) ws[w] = v;
+        __syncthreads();
+        if (w == 0) {
+            double t = ws[lane];
+            for (int off = 1; off < 32; off <<= 1) {
+                const double y = __shfl_up_sync(0xffffffffu, t, off);
+                if (lane >= off) t += y;
+            }
+            ws[lane] = t;
+        }
+        __syncthreads();
+        const double incl = v + (w > 0 ? ws[w - 1] : 0.0) + carry;
+        if (c < nch) b.pre[c] = incl - own;  // an estimate: any rounding will do
+        __syncthreads();
+        if (threadIdx.x == SB - 1) carry = incl;
+        __syncthreads();
+    }
+}
+
+template <class Fetch>
+__global__ void __launch_bounds__(SB) k_gs_map(Fetch fetch, int total, GsBuf b) {
+    __shared__ GridSeg wseg[SB / 32];
+    __shared__ long long wub[SB / 32];
+    __shared__ int wbad[SB / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, c = blockIdx.x;
+    const int e = binade_of(b.pre[c]);
+    GridSeg g = seg_identity();
+    long long ub = 0;
+    bool bad = e == NO_BINADE;
+#pragma unroll
+    for (int u = 0; u < EPT; u++) {
+        bool fl;
+        double x;
+        fetch(c * CH + threadIdx.x * EPT + u, fl, x);
+        if (!fl || bad) continue;
+        GridSeg gu;
+        long long bu;
+        if (seg_of(__double_as_longlong(x), e, gu, bu)) {
+            g = seg_cat(g, gu);
+            ub += bu;
+        } else {
+            bad = true;
+        }
+    }
+    g = seg_warp_reduce(g);
+    for (int off = 16; off > 0; off >>= 1) ub += __shfl_down_sync(0xffffffffu, ub, off);
+    const int wb = __any_sync(0xffffffffu, bad);
+    if (lane == 0) {
+        wseg[w] = g;
+        wub[w] = ub;
+        wbad[w] = wb;
+    }
+    __syncthreads();
+    if (w == 0) {
+        const GridSeg h = seg_warp_reduce(wseg[lane]);
+        long long hb = min(wub[lane], UB_CAP);
+        for (int off = 16; off > 0; off >>= 1)
+            hb = min(hb + __shfl_down_sync(0xffffffffu, hb, off), UB_CAP);  // both <= 2^61
+        const int hbad = __any_sync(0xffffffffu, wbad[lane]);
+        if (lane == 0) {
+            b.map[c] = h;
+            b.ub[c] = hb;
+            b.e[c] = e;
+            b.flag[c] = b.cnt[c] == 0 ? 2 : (hbad ? 1 : 0);
+        }
+    }
+}
+
+// the ordered walk; out[0] = the sum and out[1] = the count, or out[0] =
+// sum / count when average is set; nothing when status[0] is set
+template <class Fetch>
+__global__ void __launch_bounds__(SB) k_gs_apply(Fetch fetch, int total, int nch, GsBuf b,
+                                                 double* out, bool average, const int* status) {
+    if (status && status[0]) return;
+    __shared__ SumShared sh;
+    __shared__ long long wn[SB / 32];
+    __shared__ int s_fail;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    long long n = 0;
+    for (int c = threadIdx.x; c < nch; c += SB) n += b.cnt[c];
+    for (int off = 16; off > 0; off >>= 1) n += __shfl_down_sync(0xffffffffu, n, off);
+    if (lane == 0) wn[w] = n;
+    if (threadIdx.x == 0) sh.acc = 0.0;
+    __syncthreads();
+    int next = 0;
+    for (;;) {
+        if (w == 0) {
+            double acc = sh.acc;  // every lane walks the same sums
+            int fail = nch;
+            for (int cb = next; cb < nch && fail == nch; cb += 32) {
+                const int c = cb + lane;
+                GridSeg g = seg_identity();
+                long long ub = 0;
+                int e = NO_BINADE, flag = 1;
+                if (c < nch) {
+                    g = b.map[c];
+                    ub = b.ub[c];
+                    e = b.e[c];
+                    flag = b.flag[c];
+                }
+                const int lim = min(32, nch - cb);
+                for (int l = 0; l < lim; l++) {
+                    const GridSeg gl{__shfl_sync(0xffffffffu, g.i0, l), __shfl_sync(0xffffffffu, g.i1, l),
+                                     __shfl_sync(0xffffffffu, g.o0, l), __shfl_sync(0xffffffffu, g.o1, l)};
+                    const long long ubl = __shfl_sync(0xffffffffu, ub, l);
+                    const int el = __shfl_sync(0xffffffffu, e, l);
+                    const int fl = __shfl_sync(0xffffffffu, flag, l);
+                    if (fl == 2) continue;  // nothing kept
+                    const int ea = binade_of(acc);
+                    if (fl != 0 || ea == NO_BINADE || el != ea || !grid_apply(acc, ea, gl, ubl)) {
+                        fail = cb + l;
+                        break;
+                    }
+                }
+            }
+            if (lane == 0) {
+                sh.acc = acc;
+                s_fail = fail;
+            }
+        }
+        __syncthreads();
+        const int fc = s_fail;
+        if (fc >= nch) break;
+        bool f4[EPT];
+        double x4[EPT];
+#pragma unroll
+        for (int u = 0; u < EPT; u++) fetch(fc * CH + threadIdx.x * EPT + u, f4[u], x4[u]);
+        chunk_split(fc * CH, total, f4, x4, sh);
+        next = fc + 1;
+    }
+    if (threadIdx.x == 0) {
+        long long cnt = 0;
+        for (int q = 0; q < SB / 32; q++) cnt += wn[q];
+        if (average) {
+            out[0] = sh.acc / (double)cnt;
+        } else {
+            out[0] = sh.acc;
+            out[1] = (double)cnt;
+        }
+    }
+}
+
+// the fluid densities of a 2-D mask in the reference's loop order (j outer)
+struct RhoFetch {
+    D2 d;
+    const int* mask;
+    int total;
+    __device__ void operator()(int t, bool& fl, double& x) const {
         fl = false;
         x = 0.0;
         if (t < total) {
-            const int j = 1 + t / nx, i = 1 + t % nx;
+            const int nx = d.p.nx, j = 1 + t / nx, i = 1 + t % nx;
             fl = mask[IX(d, i, j)] == 0;
             x = d.rho[IX(d, i, j)];
         }
-    }, sum, n);
-    if (threadIdx.x == 0) d.ravg[0] = sum / (double)n;
-}
+    }
+};
 
-// the same sequential sum over x[t] where keep[t] != 0 (out: sum, count)
-__global__ void __launch_bounds__(SB) k_ordered_sum(const double* x, const int* keep, int total,
-                                                    double* out) {
-    double sum;
-    long long n;
-    ordered_sum_block(total, [&](int t, bool& fl, double& v) {
+struct ArrayFetch {
+    const double* x;
+    const int* keep;
+    int total;
+    __device__ void operator()(int t, bool& fl, double& v) const {
         fl = t < total && keep[t] != 0;
         v = t < total ? x[t] : 0.0;
-    }, sum, n);
-    if (threadIdx.x == 0) {
-        out[0] = sum;
-        out[1] = (double)n;
     }
+};
+
+GsBuf gs_of(const D2& d) {
+    return GsBuf{d.gs_part, d.gs_pre, (GridSeg*)d.gs_map, d.gs_ub, d.gs_e, d.gs_flag, d.gs_cnt};
+}
+
+int gs_chunks(long long total) { return (int)((total + CH - 1) / CH) > 0 ? (int)((total + CH - 1) / CH) : 1; }
+
+template <class Fetch>
+void gs_launch(const Fetch& f, int total, const GsBuf& b, double* out, bool average,
+               const int* status, cudaStream_t s) {
+    const int nch = gs_chunks(total);
+    k_gs_part<<<nch, SB, 0, s>>>(f, total, b);
+    k_gs_scan<<<1, SB, 0, s>>>(b, nch);
+    k_gs_map<<<nch, SB, 0, s>>>(f, total, b);
+    k_gs_apply<<<1, SB, 0, s>>>(f, total, nch, b, out, average, status);
 }
 
 // calQ / calQ2 from node (x, y) along direction a towards circle c
@@ -850,10 +1054,23 @@ __device__ bool refill_node(const D2& d, int i, int j, double ra) {
 }
 
 // The refill sweep in the reference's order: each refill may read an earlier
-// one, so one thread refills; the block finds the nodes to refill (left a
-// circle: solid before, fluid now) chunk by chunk with an ordered compaction.
-__global__ void __launch_bounds__(SB) k2_refill(D2 d) {
-    if (d.status[0]) return;
+// one, so one thread refills.  The nodes to refill (left a circle: solid
+// before, fluid now) are listed by k2_refill_find in any order; k2_refill sorts
+// the list by node index and refills in that order.  A list longer than
+// RF_CAP is replaced by refill_scan, which finds the nodes chunk by chunk with
+// an ordered block compaction.
+constexpr int RF_CAP = 4096;
+
+__global__ void k2_refill_find(D2 d) {
+    const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x, j = 1 + blockIdx.y;
+    if (i > d.p.nx || d.status[0]) return;
+    if (d.ob[IX(d, i, j)] == 1 && d.on[IX(d, i, j)] == 0) {
+        const int pos = atomicAdd(d.rf_count, 1);
+        if (pos < RF_CAP) d.rf_list[pos] = (j - 1) * d.p.nx + (i - 1);
+    }
+}
+
+__device__ void refill_scan(const D2& d) {
     __shared__ int list[SB];
     __shared__ int wcount[SB / 32];
     __shared__ int nlist, stop;
@@ -912,6 +1129,40 @@ __global__ void __launch_bounds__(SB) k2_refill(D2 d) {
             __syncthreads();
             if (stop) return;
         }
+    }
+}
+
+__global__ void __launch_bounds__(SB) k2_refill(D2 d) {
+    if (d.status[0]) return;
+    const int cnt = d.rf_count[0];
+    if (cnt > RF_CAP) {
+        refill_scan(d);
+        return;
+    }
+    __shared__ int keys[RF_CAP];
+    int n2 = 1;
+    while (n2 < cnt) n2 <<= 1;
+    for (int q = threadIdx.x; q < n2; q += SB) keys[q] = q < cnt ? d.rf_list[q] : 0x7fffffff;
+    __syncthreads();
+    for (int k = 2; k <= n2; k <<= 1)  // bitonic sort, ascending
+        for (int jj = k >> 1; jj > 0; jj >>= 1) {
+            for (int q = threadIdx.x; q < n2; q += SB) {
+                const int r = q ^ jj;
+                if (r > q) {
+                    const int a = keys[q], b = keys[r];
+                    if ((a > b) == ((q & k) == 0)) {
+                        keys[q] = b;
+                        keys[r] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    if (threadIdx.x == 0) {
+        const int nx = d.p.nx;
+        const double ra = d.ravg[0];
+        for (int q = 0; q < cnt; q++)
+            if (!refill_node(d, 1 + keys[q] % nx, 1 + keys[q] / nx, ra)) return;
     }
 }
 
@@ -1018,6 +1269,15 @@ int p2d_create(const P2Params& p, const double* centers_xy, P2Ctx** out, std::st
     for (double** a : pa)
         if ((rc = dal(c, a, np3, err))) return rc;
     if ((rc = dal(c, &d.lc, 8 * cells, err)) || (rc = dal(c, &d.lq, 24 * cells, err))) return rc;
+    const size_t nch = (size_t)gs_chunks((long long)p.nx * p.ny);
+    GridSeg* gmap = nullptr;
+    if ((rc = dal(c, &d.gs_part, nch, err)) || (rc = dal(c, &d.gs_pre, nch, err)) ||
+        (rc = dal(c, &gmap, nch, err)) || (rc = dal(c, &d.gs_ub, nch, err)) ||
+        (rc = dal(c, &d.gs_e, nch, err)) || (rc = dal(c, &d.gs_flag, nch, err)) ||
+        (rc = dal(c, &d.gs_cnt, nch, err)))
+        return rc;
+    d.gs_map = gmap;
+    if ((rc = dal(c, &d.rf_count, 1, err)) || (rc = dal(c, &d.rf_list, RF_CAP, err))) return rc;
     if ((rc = dal(c, &d.ravg, 2, err)) || (rc = dal(c, &d.status, 2, err)) ||
         (rc = dal(c, &c->owner_tmp, (size_t)p.nx * p.ny, err)))
         return rc;
@@ -1033,7 +1293,9 @@ void p2d_destroy(P2Ctx* c) {
     if (!c) return;
     D2& d = c->d;
     void* ps[] = {d.f, d.fp, d.rho, d.u, d.v, d.ob, d.on, d.xc, d.uc, d.om, d.xco, d.uco, d.omo,
-                  d.force, d.torque, d.ravg, d.status, d.lc, d.lq, c->owner_tmp};
+                  d.force, d.torque, d.ravg, d.status, d.lc, d.lq, c->owner_tmp,
+                  d.gs_part, d.gs_pre, d.gs_map, d.gs_ub, d.gs_e, d.gs_flag, d.gs_cnt,
+                  d.rf_count, d.rf_list};
     if (c->s) cudaStreamSynchronize(c->s);
     for (void* p : ps)
         if (p) cudaFree(p);
@@ -1092,7 +1354,8 @@ int p2d_step(P2Ctx* c, int nsteps, std::string& err) {
         k2_collide<<<g, 128, 0, c->s>>>(d);
         k2_stream<<<g, 128, 0, c->s>>>(d);
         k2_walls<<<(nw + 127) / 128, 128, 0, c->s>>>(d);
-        k2_rho_avg<<<1, SB, 0, c->s>>>(d, d.ob);
+        gs_launch(RhoFetch{d, d.ob, d.p.nx * d.p.ny}, d.p.nx * d.p.ny, gs_of(d), d.ravg, true,
+                  d.status, c->s);
         k2_ibb<<<g, 128, 0, c->s>>>(d);
         k2_macro<<<g, 128, 0, c->s>>>(d);
         if (d.p.np > 0) {
@@ -1101,7 +1364,10 @@ int p2d_step(P2Ctx* c, int nsteps, std::string& err) {
             k2_move<<<pg, 64, 0, c->s>>>(d);
         }
         k2_mask<<<dim3((d.p.nx + 2 + 127) / 128, d.p.ny + 2), 128, 0, c->s>>>(d, d.on, true);
-        k2_rho_avg<<<1, SB, 0, c->s>>>(d, d.on);
+        gs_launch(RhoFetch{d, d.on, d.p.nx * d.p.ny}, d.p.nx * d.p.ny, gs_of(d), d.ravg, true,
+                  d.status, c->s);
+        cudaMemsetAsync(d.rf_count, 0, sizeof(int), c->s);
+        k2_refill_find<<<g, 128, 0, c->s>>>(d);
         k2_refill<<<1, SB, 0, c->s>>>(d);
         cudaMemcpyAsync(d.ob, d.on, cells * sizeof(int), cudaMemcpyDeviceToDevice, c->s);
         c->itc++;
@@ -1189,24 +1455,33 @@ double p2d_rho_avg(P2Ctx* c) {
 extern "C" int mglc_sequential_sum(const double* x, const int* keep, int n, double* sum,
                                    long long* count) {
     if (n < 0 || !x || !keep || !sum || !count) return MGLC_ERR_INVALID;
-    double* dx = nullptr;
-    int* dk = nullptr;
-    double* dout = nullptr;
-    const size_t m = n > 0 ? (size_t)n : 1;
+    const size_t m = n > 0 ? (size_t)n : 1, nch = (size_t)mglc::gs_chunks(n);
+    double *dx = nullptr, *dout = nullptr, *part = nullptr, *pre = nullptr;
+    int *dk = nullptr, *ge = nullptr, *gf = nullptr, *gc = nullptr;
+    mglc::GridSeg* gmap = nullptr;
+    long long* gub = nullptr;
     cudaError_t e = cudaMalloc(&dx, m * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&dk, m * sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&dout, 2 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&part, nch * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&pre, nch * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&gmap, nch * sizeof(mglc::GridSeg));
+    if (e == cudaSuccess) e = cudaMalloc(&gub, nch * sizeof(long long));
+    if (e == cudaSuccess) e = cudaMalloc(&ge, nch * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&gf, nch * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&gc, nch * sizeof(int));
     if (e == cudaSuccess && n > 0) e = cudaMemcpy(dx, x, (size_t)n * sizeof(double), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && n > 0) e = cudaMemcpy(dk, keep, (size_t)n * sizeof(int), cudaMemcpyHostToDevice);
     double out[2] = {0.0, 0.0};
     if (e == cudaSuccess) {
-        mglc::k_ordered_sum<<<1, mglc::SB>>>(dx, dk, n, dout);
+        const mglc::GsBuf b{part, pre, gmap, gub, ge, gf, gc};
+        mglc::gs_launch(mglc::ArrayFetch{dx, dk, n}, n, b, dout, false, nullptr, 0);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpy(out, dout, sizeof out, cudaMemcpyDeviceToHost);
-    cudaFree(dx);
-    cudaFree(dk);
-    cudaFree(dout);
+    void* ps[] = {dx, dk, dout, part, pre, gmap, gub, ge, gf, gc};
+    for (void* p : ps)
+        if (p) cudaFree(p);
     if (e != cudaSuccess) return MGLC_ERR_CUDA;
     *sum = out[0];
     *count = (long long)out[1];

@@ -1,5 +1,5 @@
-"""The algorithm of the GPU's sequential FP64 sums (k2_rho_avg and
-mglc_sequential_sum in mglc_gb300/csrc/k_particle2d.cu), modelled in Python
+"""The algorithm of the GPU's sequential FP64 sums (the k_gs_* kernels and
+chunk_split in mglc_gb300/csrc/k_particle2d.cu), modelled in Python
 with the kernel's integer operations on IEEE bit patterns, checked on the CPU
 against the plain left-to-right loop.  While the running sum s lies in the
 binade [2^e, 2^(e+1)), s = S u with u = 2^(e-52), and adding a finite
