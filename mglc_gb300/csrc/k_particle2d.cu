@@ -15,9 +15,11 @@
 // reference's arrays (-1..nx+2 filled with omega*rho0; one more zero layer).
 // Everything is FP64 and this file is compiled without FMA contraction, so
 // each expression rounds as the reference's statement does.  Steps whose
-// order matters in the reference -- the density averages, each particle's
-// link sums, the refill sweep -- run sequentially in its loop order (one
-// thread, or one thread per particle); the rest is one thread per node.
+// order matters in the reference keep its loop order: the density averages
+// are exact parallel replays of the sequential sum (the k_gs_* kernels), each
+// circle's link sums are evaluated by a warp and added in loop order, and the
+// refill sweep refills its sorted node list on one thread; the rest is one
+// thread per node.
 #include <cmath>
 #include <cstdio>
 #include <cstring>

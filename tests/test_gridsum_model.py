@@ -216,3 +216,92 @@ def test_tie_rounds_to_even():
     (i0, i1, o0, o1), ub = seg_of(0.5, e)
     assert (i0, i1, o0, o1, ub) == (0, 1, 0, 0, 1)
     assert apply(s, e, (i0, i1, o0, o1), ub) == s + 0.5
+
+
+def pipeline_sum(xs, chunk, lanes, units, predict):
+    """The multi-block form: every chunk's map is built on the binade that
+    predict(prefix estimate) names; a walk adds a chunk as its map only when
+    that binade is the exact running sum's, every kept addend took the grid
+    path and the bound keeps the sum inside the binade, else it re-adds the
+    chunk with the split (split_sum from the running sum)."""
+    chunks = [xs[p:p + chunk] for p in range(0, len(xs), chunk)] or [[]]
+    parts = [sum(x for x in c if x is not None) for c in chunks]
+    pre = [sum(parts[:k]) for k in range(len(chunks))]
+    recs = []
+    for c, est in zip(chunks, pre):
+        e = predict(est)
+        h, ub, ok = IDENT, 0, e is not None
+        kept = [x for x in c if x is not None]
+        for x in kept:
+            r = seg_of(x, e) if ok else None
+            if r is None:
+                ok = False
+                break
+            h, ub = cat(h, r[0]), ub + r[1]
+        recs.append((e, h, min(ub, 1 << 61), ok, bool(kept)))
+    acc, redone = 0.0, 0
+    for c, (e, h, ub, ok, kept) in zip(chunks, recs):
+        if not kept:
+            continue
+        ea = binade(acc)
+        if ok and ea is not None and ea == e and ub < (1 << 53) - mant_s(acc):
+            acc = apply(acc, e, h, ub)
+            continue
+        redone += 1
+        acc = split_from_acc(acc, c, lanes, units)
+    return acc, redone
+
+
+def split_from_acc(acc, xs, lanes, units):
+    """split_sum over one chunk, starting from the running sum acc."""
+    start = 0
+    while start < len(xs):
+        e = binade(acc)
+        s = mant_s(acc) if e is not None else 0
+        h, incl, stop = IDENT, 0, None
+        for u in range(start, len(xs), units):
+            g, ub, bad = IDENT, 0, False
+            for x in xs[u:u + units]:
+                if x is None:
+                    continue
+                r = seg_of(x, e) if e is not None else None
+                if r is None:
+                    bad = True
+                    break
+                g, ub = cat(g, r[0]), ub + r[1]
+            if bad or incl + ub >= (1 << 53) - s:
+                stop = u
+                break
+            h, incl = cat(h, g), incl + ub
+        if e is not None and incl:
+            acc = apply(acc, e, h, incl)
+        if stop is None:
+            break
+        acc, _ = split_from(acc, xs[stop:stop + units])
+        start = stop + units
+    return acc
+
+
+@pytest.mark.parametrize("kind", ["near_one", "ties", "scales", "negative", "tiny", "specials",
+                                  "signed_zero"])
+@pytest.mark.parametrize("predict", ["estimate", "off_by_one", "none"])
+def test_chunk_walk_equals_the_loop_sum_for_any_prediction(kind, predict):
+    """The walk never trusts a prediction it cannot confirm: right, wrong by one
+    binade, or absent, the result is the loop's sum bit for bit."""
+    fn = {"estimate": binade,
+          "off_by_one": lambda est: None if binade(est) is None else binade(est) + 1,
+          "none": lambda est: None}[predict]
+    rng = np.random.default_rng(3 + len(kind) + len(predict))
+    for n in (1, 50, 700):
+        xs = addends(kind, n, rng)
+        got, _ = pipeline_sum(xs, chunk=64, lanes=4, units=4, predict=fn)
+        assert same(got, loop_sum(xs)), (kind, predict, n)
+
+
+def test_chunk_walk_redoes_only_crossings_on_densities():
+    rng = np.random.default_rng(11)
+    xs = addends("near_one", 40000, rng)
+    got, redone = pipeline_sum(xs, chunk=1024, lanes=32, units=32, predict=binade)
+    assert same(got, loop_sum(xs))
+    # the first chunk (empty running sum) and the chunks holding 2^11 .. 2^15
+    assert redone <= 8
