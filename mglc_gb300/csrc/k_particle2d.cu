@@ -688,8 +688,6 @@ void gs_launch(const Fetch& f, int total, const GsBuf& b, double* out, bool aver
 __device__ bool calq(const D2& d, int c, double x, double y, int a, double& x0, double& y0,
                      double& q) {
     const double xc = d.xc[3 * c], yc = d.xc[3 * c + 1], R = d.p.radius;
-    const double z = 1.0, zc = 0.0;
-    (void)zc;
     if (!d.p.q_bisection) {
         const double ea = c_ex[a], eb = c_ey[a], ec = 0.0;
         const double ca = ea * ea + eb * eb + ec * ec;
@@ -704,8 +702,6 @@ __device__ bool calq(const D2& d, int c, double x, double y, int a, double& x0, 
         const double epsR = (double)1e-9f;  // default-real literal 1e-9 (:106)
         double qq = 0.5, qt = 0.5;
         double px = x + qt * (double)c_ex[a], py = y + qt * (double)c_ey[a];
-        double pz = z + 0.0;
-        (void)pz;
         auto dist = [&]() { return sqrt((px - xc) * (px - xc) + (py - yc) * (py - yc) + 0.0); };
         int guard = 0;
         while (fabs(dist() - R) >= epsR) {

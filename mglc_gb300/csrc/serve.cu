@@ -83,8 +83,8 @@ struct Arena {
 };
 
 struct Req {
-    long long id;
-    mglc_request r;
+    long long id = 0;
+    mglc_request r{};
     int state = 0;  // 0 pending arrival, 1 waiting, 2 active, 3 retired
     int slot = -1;
     size_t off = 0, bytes = 0;

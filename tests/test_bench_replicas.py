@@ -3,7 +3,6 @@ time; every rank must see the maximum (the job ends with its slowest replica).""
 import os
 import socket
 
-import pytest
 import torch.multiprocessing as mp
 
 
