@@ -149,3 +149,17 @@ def test_sequential_sum_is_the_loop_order_sum_bitwise(mg, kind, n):
 def test_sequential_sum_empty(mg):
     got, cnt = _gpu_seq_sum(np.zeros(0), np.zeros(0, np.int32))
     assert cnt == 0 and got == 0.0 and not np.signbit(got)
+
+
+@pytest.mark.parametrize("kind", ["near_one", "scales"])
+def test_sequential_sum_past_one_scan_tile(mg, kind):
+    """4.3 million addends: more than 1024 chunks of 4096, so the chunk scan
+    carries its prefix across tiles."""
+    n = 4_300_000
+    rng = np.random.default_rng(99 + len(kind))
+    x = _addends(kind, n, rng)
+    keep = (rng.random(n) >= 0.1).astype(np.int32)
+    got, cnt = _gpu_seq_sum(x, keep)
+    want = _seq_sum(x, keep)
+    assert cnt == int(keep.sum())
+    assert np.array([got]).view(np.int64)[0] == np.array([want]).view(np.int64)[0], (got, want)
