@@ -85,3 +85,16 @@ def test_shear2d_parameters_are_rejected_without_a_gpu(lib):
         assert lib.mglc_shear2d_create(ctypes.byref(p), c.ctypes.data, len(c), ctypes.byref(ctx)) == 1
         assert msg in lib.mglc_last_error(ctx)
         lib.mglc_destroy(ctx)
+
+
+def test_sequential_sum_rejects_bad_arguments_without_a_gpu(lib):
+    import numpy as np
+    x = np.ones(4)
+    keep = np.ones(4, np.int32)
+    s, n = ctypes.c_double(), ctypes.c_longlong()
+    f = lib.mglc_sequential_sum
+    assert f(x.ctypes.data, keep.ctypes.data, -1, ctypes.byref(s), ctypes.byref(n)) == 1
+    assert f(None, keep.ctypes.data, 4, ctypes.byref(s), ctypes.byref(n)) == 1
+    assert f(x.ctypes.data, None, 4, ctypes.byref(s), ctypes.byref(n)) == 1
+    assert f(x.ctypes.data, keep.ctypes.data, 4, None, ctypes.byref(n)) == 1
+    assert f(x.ctypes.data, keep.ctypes.data, 4, ctypes.byref(s), None) == 1
