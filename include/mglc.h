@@ -177,10 +177,18 @@ typedef struct mglc_lid2d_params {
 } mglc_lid2d_params;
 /* Replaces the allocation part of 2d_revised/mpi_blocked/initial.f90:32-38. */
 int mglc_lid2d_create(const mglc_lid2d_params* p, mglc_ctx** out);
+/* Frees the context's device memory and stream: the deallocate block at the end
+ * of the reference's programs (mpi_3d_blocked/main.f90:122-130,
+ * bouyancy3d_mpi.F90:303-318).  NULL is ignored. */
 void mglc_destroy(mglc_ctx* ctx);
+/* No counterpart (the reference writes a message and stops): the message of
+ * the context's last failed call, valid until its next call. */
 const char* mglc_last_error(const mglc_ctx* ctx);
-/* Bind the context to a caller-owned cudaStream_t (NULL = the context's own stream). */
+/* No counterpart: bind the context to a caller-owned cudaStream_t (NULL = the
+ * context's own stream). */
 int mglc_set_stream(mglc_ctx* ctx, void* cuda_stream);
+/* No counterpart: the derived constants the reference prints at start-up
+ * (relaxation times, viscosity, ...) and the context's device memory. */
 int mglc_get_info(const mglc_ctx* ctx, mglc_info* out);
 
 /* ---- state ------------------------------------------------------------- */
@@ -205,15 +213,17 @@ int mglc_get_f(mglc_ctx* ctx, double* f, double* g);
  * end to report MGLC_ERR_PARTICLE (overlap, wall penetration). */
 int mglc_step(mglc_ctx* ctx, int nsteps);
 
-/* macro() / macroT() output: rho,u,v,w (and T) of the current state, host
+/* macro() / macroT() output (lid macro.f90:6-25; thermal bouyancy3d_mpi.F90:
+ * 986-1010 and 1215-1231): rho,u,v,w (and T) of the current state, host
  * arrays (x fastest).  Any pointer may be NULL.  Synchronises. */
 int mglc_get_macros(mglc_ctx* ctx, double* rho, double* u, double* v, double* w, double* T);
 /* check(): lid check.f90:12-30 (errorU over u,v only in the numerator);
  * thermal bouyancy3d_mpi.F90:1234-1281 (errorU over u,v,w; errorT).  Updates
  * the stored previous fields like the reference.  error_t may be NULL. */
 int mglc_check(mglc_ctx* ctx, double* error_u, double* error_t);
-/* Conserved totals in FP64: mass = sum rho, energy = sum rho|u|^2/2,
- * heat = sum T (thermal, else 0).  Any pointer may be NULL. */
+/* No counterpart (a conservation check for tests and monitoring): totals in
+ * FP64, mass = sum rho, energy = sum rho|u|^2/2, heat = sum T (thermal, else
+ * 0).  Any pointer may be NULL. */
 int mglc_totals(mglc_ctx* ctx, double* mass, double* energy, double* heat);
 
 /* Particle centres, velocities, angular velocities, and the total force and
