@@ -447,10 +447,14 @@ def particles2d_bench(torch, mg, steps=200, warmup=10, cpu_steps=20, cpu=True):
         e1.record(stream)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
+        dev = c.info().device_bytes
         c.set_stream(None)
         c.close()
         out[key] = {"workload": desc, "value": round(320000 * steps / (ms * 1e-3) / 1e6, 1),
-                    "unit": "MLUPS", "steps": steps, "ms_per_step": round(ms / steps, 4)}
+                    "unit": "MLUPS", "steps": steps, "ms_per_step": round(ms / steps, 4),
+                    "l2": f"device state {dev / 1e6:.0f} MB, of which populations "
+                          f"{144 * 320000 / 1e6:.0f} MB, against the 129 MB L2: the "
+                          "reference's own grid size, no flush between steps"}
     if cpu:
         import numpy as np
         from oracle import oracle as O
