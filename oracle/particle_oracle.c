@@ -494,12 +494,6 @@ static void wall_rot(const orc_particles* s, int c, double x0, double y0, double
     rot[2] = O[0] * ry - O[1] * rx;
 }
 
-static int find_owner(const orc_particles* s, int ip, int jp, int kp, const double* centers) {
-    for (int c = 0; c < s->p.np; c++)
-        if (inside(s, c, (double)ip, (double)jp, (double)kp, centers)) return c;
-    return -1;
-}
-
 /* rho average over fluid nodes (particle_bounceback.F90:15-35) */
 static double rho_average(orc_particles* s, const int* mask) {
     const orc_pp* p = &s->p;
