@@ -43,6 +43,7 @@ WORKLOADS = {
                        desc="differentially heated cavity D3Q19+D3Q7 128^3 Ra=1e5 Pr=0.71"),
     "particles": dict(kind="particle", n=(256, 128, 128), np=200, radius=5.0, ratio=1.2,
                       body_force=1e-6, tauf=0.65, seed=2026, launches_per_step=11,
+                      error_steps=10000,
                       data="synthetic (seeded sphere placement, fluid at rest, no dataset)",
                       desc="particle-laden channel D3Q19 256x128x128, 200 spheres R=5, "
                            "density ratio 1.2, body force 1e-6 along x, periodic x"),
@@ -153,6 +154,50 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def fp64_peak():
+    """Measured FP64 instruction rate of this GPU (the probe in
+    mglc_gb300/roof/fp64_rate.cu): the best of DFMA, DADD and DMUL chains,
+    instructions per second."""
+    import ctypes
+    from mglc_gb300 import build as B
+    L = ctypes.CDLL(B.build_roof())
+    L.mglc_roof_fp64.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                 ctypes.POINTER(ctypes.c_double)]
+    out = {}
+    for mode, name in ((0, "dfma"), (1, "dadd"), (2, "dmul")):
+        r, ms = ctypes.c_double(), ctypes.c_double()
+        rc = L.mglc_roof_fp64(mode, 4096, ctypes.byref(r), ctypes.byref(ms))
+        if rc != 0:
+            raise RuntimeError(f"FP64 rate probe failed (CUDA error {rc})")
+        out[name] = r.value
+    return out
+
+
+def load_fp64_instr():
+    """FP64 instructions per cell-update of each FP64 step kernel, counted by
+    ncu (profiles/fp64_instr.json)."""
+    p = os.path.join(ROOT, "profiles", "fp64_instr.json")
+    if not os.path.exists(p):
+        return {}
+    with open(p) as fh:
+        return json.load(fh)
+
+
+def fp64_roof(kind, form, mlups, probe):
+    """The compute roof of an FP64 kernel: its FP64 instructions per cell
+    (ncu count) times cells per second, against the measured FP64 rate."""
+    tab = load_fp64_instr().get(f"{kind}_{form}")
+    if not tab or not probe:
+        return None
+    ipc = tab["fp64_instr_per_cell"]
+    peak = max(probe.values()) / 1e9
+    ach = ipc * mlups * 1e6 / 1e9
+    return {"fp64_achieved": round(ach, 1), "fp64_peak": round(peak, 1),
+            "fp64_unit": "G FP64 instr/s", "fp64_frac": round(ach / peak, 4),
+            "fp64_instr_per_cell": ipc, "fp64_peak_kind": "measured (mglc_gb300/roof/fp64_rate.cu, "
+            "best of DFMA/DADD/DMUL chains, same run)", "fp64_instr_source": tab["source"]}
+
+
 def make_solve(mg, wl, form, in_place=False):
     n = wl["n"]
     if wl["kind"] == "particle":
@@ -168,6 +213,47 @@ def make_solve(mg, wl, form, in_place=False):
                                   precision=form, in_place=in_place)
     return mg.BuoyancyCavity(n, rayleigh=wl["rayleigh"], prandtl=wl["prandtl"], mach=wl["mach"],
                              t_hot=0.5, t_cold=-0.5, ekman=0.0, precision=form)
+
+
+def alg_bytes(kind, form):
+    """Algorithmic bytes per cell-update of a one-solve step kernel (what the
+    context's mglc_get_info reports): every stored population read and
+    written once, plus the owner mask (particles) or the temperature
+    populations and the carried force (heated cavity, no rotation)."""
+    pb = {"fp64": 8, "fx64": 8, "fp32": 4}.get(form, 2)
+    if kind == "lid":
+        return 2.0 * 19 * pb
+    if kind == "particle":
+        return 2.0 * 19 * pb + 4.0
+    cb = 8.0 if form in ("fp64", "fx64") else 4.0
+    return 2.0 * 19 * pb + 2.0 * 7 * cb + 2.0 * cb
+
+
+def replica_command(n, argv, port):
+    """torchrun command that runs this script as n replica ranks (one GPU
+    each, rendezvous on 127.0.0.1)."""
+    return [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+            "--master-addr", "127.0.0.1", "--master-port", str(port),
+            os.path.join(ROOT, "bench.py"), *argv]
+
+
+def free_port():
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        return sk.getsockname()[1]
+
+
+def world_check(gpus):
+    """(spawn, error): spawn N replica ranks when --gpus N > 1 is given
+    without a launcher; an error when a launcher's WORLD_SIZE differs from N."""
+    env = os.environ.get("WORLD_SIZE")
+    if env is not None:
+        if int(env) != gpus:
+            return False, (f"bench.py: WORLD_SIZE={env} but --gpus {gpus}; run one rank per GPU "
+                           f"with --gpus equal to the world size")
+        return False, None
+    return gpus > 1, None
 
 
 def l2_note(resident_bytes):
@@ -188,6 +274,64 @@ def max_over_ranks(torch, dist, x, device="cuda"):
     return float(t.item())
 
 
+class CudaClock:
+    """CUDA events recorded on the stream the kernels are launched on."""
+
+    def __init__(self, torch, stream):
+        self.torch, self.stream = torch, stream
+        self.e0 = torch.cuda.Event(enable_timing=True)
+        self.e1 = torch.cuda.Event(enable_timing=True)
+
+    def sync(self):
+        self.torch.cuda.synchronize()
+
+    def start(self):
+        self.e0.record(self.stream)
+
+    def stop(self):
+        self.e1.record(self.stream)
+
+    def ms(self):
+        return self.e0.elapsed_time(self.e1)
+
+
+class HostClock:
+    """Wall clock for a host-side run (the CPU test of the replica path)."""
+
+    def sync(self):
+        pass
+
+    def start(self):
+        self.t0 = time.perf_counter()
+
+    def stop(self):
+        self.t1 = time.perf_counter()
+
+    def ms(self):
+        return (self.t1 - self.t0) * 1e3
+
+
+def timed_replica(torch, dist, run, steps, warmup, clock, device="cuda"):
+    """One replica's timed region: `warmup` untimed steps, a barrier with the
+    device synchronised on both sides, `steps` steps between the clock's
+    marks; returns the slowest rank's milliseconds."""
+    run(warmup)
+    clock.sync()
+    if dist:
+        dist.barrier()
+    clock.sync()
+    clock.start()
+    run(steps)
+    clock.stop()
+    clock.sync()
+    return max_over_ranks(torch, dist, clock.ms(), device)
+
+
+def replica_mlups(world, cells, steps, ms):
+    """Whole-job throughput: every rank advanced its own `cells` cavity."""
+    return world * cells * steps / (ms * 1e-3) / 1e6
+
+
 def time_device(torch, mg, wl, form, steps, warmup, dist=None, in_place=False):
     """Device-resident MLUPS: state in HBM, K fused steps between CUDA events."""
     s = make_solve(mg, wl, form, in_place)
@@ -196,19 +340,8 @@ def time_device(torch, mg, wl, form, steps, warmup, dist=None, in_place=False):
     stream = torch.cuda.Stream()
     s.set_stream(stream.cuda_stream)
     s.initial()
-    s.step(warmup)
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    s.step(steps)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
+    ms = timed_replica(torch, dist, s.step, steps, warmup, CudaClock(torch, stream))
     s.set_stream(None)
-    ms = max_over_ranks(torch, dist, ms)
     info = s.info()
     s.close()
     return ms, info
@@ -309,10 +442,121 @@ def form_errors(mg, wl, forms, steps):
             if wl["kind"] == "thermal":
                 e["T_rel_l2_vs_fp64"] = rel_l2(got["T"], ref["T"])
                 e["nu_hot_rel_vs_fp64"] = abs(got["nu"][2] - ref["nu"][2]) / abs(ref["nu"][2])
+                e["nu_cold_rel_vs_fp64"] = abs(got["nu"][3] - ref["nu"][3]) / abs(ref["nu"][3])
+                e["nu_hot_fp64"] = ref["nu"][2]
+                e["nu_cold_fp64"] = ref["nu"][3]
             res[fm] = e
         except Exception as ex:  # report, never hide
             res[fm] = {"error_run_failed": str(ex)}
     return res
+
+
+def particle_errors(mg, wl, steps):
+    """FP32 particle channel against FP64 after `steps` steps from the same
+    initial state: fluid velocity, particle displacement, force and torque."""
+    def run(form):
+        s = make_solve(mg, wl, form)
+        s.initial()
+        s.step(steps)
+        r = s.macro()
+        st = s.state()
+        m = s.mask()
+        s.close()
+        return np.stack(r[1:4]), st, m
+    u64, st64, m64 = run("fp64")
+    u32, st32, m32 = run("fp32")
+    x0 = place_spheres(*wl["n"], wl["np"], wl["radius"], wl["seed"])
+    fluid = (m64 < 0) & (m32 < 0)
+    return {"error_steps": steps,
+            "u_rel_l2_vs_fp64": rel_l2(u32[:, fluid], u64[:, fluid]),
+            "displacement_rel_l2_vs_fp64": rel_l2(st32["xc"] - x0, st64["xc"] - x0),
+            "force_rel_l2_vs_fp64": rel_l2(st32["force"], st64["force"]),
+            "torque_rel_l2_vs_fp64": rel_l2(st32["torque"], st64["torque"]),
+            "mask_nodes_differing": int((m64 != m32).sum())}
+
+
+# the forms timed for each side workload (the first is the workload's own)
+SIDE_FORMS = {"thermal128": ("fp64", "fx64", "fp32", "fp16", "fp16s"),
+              "particles": ("fp32", "fp64")}
+# SURVEY-style algorithmic bytes per cell for the workload's reduced form
+# (16-bit g and a carried 3-vector for the heated cavity; FP32 + mask byte
+# for the channel), reported beside what the kernels here move
+SIDE_SPEC_BYTES = {"thermal128": {"fp64": 464, "fp16s": 128}, "particles": {"fp32": 153}}
+
+
+def side_workload(torch, mg, key, steps, warmup, peak, probe, cpu=True, errors=True):
+    """A workload of its own beside the headline one: device MLUPS of each
+    form (CUDA events on the context's stream), HBM (and, for FP64, FP64-pipe)
+    roofline, error of the reduced forms against FP64 after the workload's
+    own step count, and the oracle on the host cores on a bounded sample."""
+    wl = dict(WORKLOADS[key])
+    cells = cells_of(wl)
+    kind = wl["kind"]
+    forms = SIDE_FORMS[key]
+    out = {"workload": wl["desc"], "cells": cells, "unit": "MLUPS", "steps": steps,
+           "warmup": warmup, "l2": l2_note(cells * alg_bytes(kind, forms[0])), "forms": {}}
+    traffic_tab = load_traffic()
+    for fm in forms:
+        try:
+            ms, info = time_device(torch, mg, wl, fm, steps, warmup)
+            v = cells * steps / (ms * 1e-3) / 1e6
+            bpc = info.bytes_per_cell_step
+            ach = bpc * cells / (ms / steps * 1e-3) / 1e9
+            ent = {"value": round(v, 3), "ms_per_step": round(ms / steps, 4),
+                   "bytes_per_cell": bpc, "achieved_gbs": round(ach, 1),
+                   "frac": round(ach / peak, 4)}
+            if fm in SIDE_SPEC_BYTES.get(key, {}):
+                ent["survey_bytes_per_cell"] = SIDE_SPEC_BYTES[key][fm]
+            if fm == "fp64":
+                fr = fp64_roof(kind, fm, v, probe)
+                if fr:
+                    ent.update(fr)
+            tk = f"{kind}_{fm}"
+            if tk in traffic_tab:
+                ent["traffic_bytes_per_cell"] = traffic_tab[tk]["dram_bytes_per_cell"]
+                ent["traffic_source"] = traffic_tab[tk]["source"]
+            out["forms"][fm] = ent
+        except Exception as e:  # report, never hide
+            out["forms"][fm] = {"error": str(e)}
+    head = out["forms"].get(forms[0], {})
+    if "value" in head:
+        out.update(form=forms[0], value=head["value"], ms_per_step=head["ms_per_step"],
+                   gpu_launches=steps * wl.get("launches_per_step", 1))
+        rf = {"bound": "fp64" if "fp64_frac" in head else "hbm", "achieved": head["achieved_gbs"],
+              "peak": peak, "unit": "GB/s", "frac": head["frac"],
+              "bytes_per_cell": head["bytes_per_cell"],
+              "kernel": "particle step (k_pbulk + 10 small kernels)" if kind == "particle"
+              else f"k_thermal_step<{forms[0]}>"}
+        for k in ("fp64_achieved", "fp64_peak", "fp64_unit", "fp64_frac", "survey_bytes_per_cell"):
+            if k in head:
+                rf[k] = head[k]
+        out["roofline"] = rf
+    if errors:
+        try:
+            if kind == "thermal":
+                es = wl["error_steps"]
+                errs = form_errors(mg, wl, [f for f in forms if f != "fp64"], es)
+                for fm, e in errs.items():
+                    out["forms"].setdefault(fm, {}).update(e)
+                    out["forms"][fm]["error_steps"] = es
+            else:
+                out["forms"]["fp32"].update(particle_errors(mg, wl, wl["error_steps"]))
+        except Exception as e:  # report, never hide
+            out["error_runs_failed"] = str(e)
+    if kind == "thermal":
+        mx = out["forms"].get("fp16s", {})
+        base = out["forms"].get("fp64", {}).get("value")
+        if "value" in mx and base:
+            out["mixed"] = {"form": "fp16 storage of f - w rho0 (stochastic rounding), fp32 "
+                                    "arithmetic, fp32 g",
+                            "value": mx["value"], "frac": mx["frac"],
+                            "speedup_vs_fp64_plain": round(mx["value"] / base, 2),
+                            **{k: mx.get(k) for k in ("u_rel_l2_vs_fp64", "T_rel_l2_vs_fp64",
+                                                      "nu_hot_rel_vs_fp64", "nu_cold_rel_vs_fp64",
+                                                      "error_steps")}}
+    if cpu:
+        out["cpu_baseline"] = cpu_sample(wl)
+    return out
 
 
 def serve_bench(torch, mg, n_req=24, rate=50.0, seed=1234, max_steps=50000, tol=1e-6, K=100,
@@ -556,8 +800,17 @@ def cpu_sample(wl, target_s=10.0):
                       f"the reference's Fortran loops) with {threads} OpenMP threads"}
 
 
+def mglc_config(wl, form, world, in_place=False):
+    """The config object of the bench line (both arms print the same one)."""
+    cells = cells_of(wl)
+    return {"workload": wl["desc"], "form": form + ("_in_place" if in_place else ""),
+            "cells": cells, "parallelism": f"replicas{world}" if world > 1 else "single",
+            "l2": l2_note(cells * alg_bytes(wl["kind"], form))}
+
+
 def reference_arm(args, wl):
     rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     if rank != 0:
         return 0
     from oracle import oracle as O
@@ -569,7 +822,7 @@ def reference_arm(args, wl):
         line = {"impl": "reference", "metric": METRIC, "value": round(cb["value"], 3), "unit": "MLUPS",
                 "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic", "config": {"workload": wl["desc"], "form": "fp64"},
+                "data": "synthetic", "config": mglc_config(wl, args.form, world),
                 "cpu_baseline": cb,
                 "e2e": {"value": round(cb["value"], 3), "unit": "MLUPS", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
@@ -604,9 +857,10 @@ def reference_arm(args, wl):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": wl["desc"], "form": "fp64", "sample_cells": m ** 3},
+            "config": mglc_config(wl, args.form, world),
             "cpu_baseline": {"value": round(val, 3), "unit": "MLUPS", "cores": threads,
-                             "kind": "port", "sample": sample},
+                             "kind": "port", "sample": sample, "sample_cells": m ** 3,
+                             "workload_cells": n ** 3},
             "e2e": {"value": round(val, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -642,6 +896,8 @@ def main():
                     help="time only the D2Q9 lid cavity at N^2 (--steps/--warmup; profiling runs)")
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-max-steps", type=int, default=50000)
+    ap.add_argument("--no-side", action="store_true",
+                    help="skip the heated-cavity and particle-channel entries")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     wl = dict(WORKLOADS[args.workload])
@@ -651,10 +907,21 @@ def main():
     if wl["kind"] == "particle" and args.form == "fp64" and "--form" not in sys.argv:
         args.form = "fp32"  # the channel workload is specified with FP32 arithmetic
 
+    spawn, err = world_check(args.gpus)
+    if err:
+        sys.stderr.write(err + "\n")
+        return 2
     if args.impl == "reference":
-        return reference_arm(args, wl)
+        return reference_arm(args, wl)  # rank 0 alone times the CPU path
 
     import torch
+    if spawn:
+        have = torch.cuda.device_count()
+        if have < args.gpus:
+            sys.stderr.write(f"bench.py: --gpus {args.gpus} but {have} GPU(s) visible\n")
+            return 2
+        # one replica rank per GPU; rank 0 prints the line
+        return subprocess.run(replica_command(args.gpus, sys.argv[1:], free_port())).returncode
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -686,7 +953,7 @@ def main():
         ms, info = time_device(torch, mglc_gb300, wl, args.form, args.steps, args.warmup, dist,
                                in_place=args.in_place)
     clocks = clk.summary()
-    value = world * cells * args.steps / (ms * 1e-3) / 1e6
+    value = replica_mlups(world, cells, args.steps, ms)
     ms_step = ms / args.steps
     bpc = info.bytes_per_cell_step
     achieved = bpc * cells / (ms_step * 1e-3) / 1e9
@@ -701,17 +968,23 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": {"fp64": "f64", "fx64": "i64 Q55 fixed point (f64 storage)"}.get(args.form, "f32"),
         "data": wl.get("data", "synthetic (analytic cavity initial state, no dataset)"),
-        "config": {"workload": wl["desc"], "form": args.form + ("_in_place" if args.in_place else ""),
-                   "cells": cells,
-                   "parallelism": f"replicas{world}" if world > 1 else "single",
-                   "l2": l2_note(cells * bpc)},
+        "config": mglc_config(wl, args.form, world, args.in_place),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "traffic_source": traffic_tab.get(tkey, {}).get("source"),
                      "peak_kind": f"hbm_gbs of {peak_kind}",
                      "bytes_per_cell": bpc, "kernel": f"k_{wl['kind']}_step<{args.form}>"},
         "clocks": clocks,
         "gpu_launches": args.steps * wl.get("launches_per_step", 1),
     }
+    probe = None
+    if args.form == "fp64":
+        # the FP64 kernels are bound by the FP64 pipe: report that roof beside HBM's
+        probe = fp64_peak()
+        fr = fp64_roof(wl["kind"], args.form, value / world, probe)
+        if fr:
+            line["roofline"].update(fr)
+            line["roofline"]["bound"] = "fp64"
     if not args.no_e2e:  # every rank runs its replica end to end; the slowest one counts
         dt, h2d, d2h, eu = time_e2e(torch, mglc_gb300, wl, args.form, args.steps, dist)
         line["e2e"] = {"value": round(world * cells * args.steps / dt / 1e6, 3), "unit": "MLUPS",
@@ -780,6 +1053,16 @@ def main():
     if rank == 0 and not args.no_lid2d and wl["kind"] == "lid":
         line["lid2d"] = lid2d_bench(torch, mglc_gb300)
         line["particles2d"] = particles2d_bench(torch, mglc_gb300)
+    if rank == 0 and not args.no_side and wl["kind"] == "lid":
+        # the heated cavity (128^3, 20000-step errors) and the particle channel
+        # (256x128x128, 200 spheres, 10000-step errors) as entries of their own
+        pk = probe if probe else fp64_peak()
+        line["thermal128"] = side_workload(torch, mglc_gb300, "thermal128", 200, 5, peak, pk,
+                                           cpu=world == 1 and not args.no_cpu,
+                                           errors=not args.no_error)
+        line["particles"] = side_workload(torch, mglc_gb300, "particles", 200, 5, peak, pk,
+                                          cpu=world == 1 and not args.no_cpu,
+                                          errors=not args.no_error)
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_sample(wl)
     if rank == 0:

@@ -369,10 +369,13 @@ int mglc_server_get_stats(mglc_server* s, mglc_server_stats* out);
  * MGLC_ERR_INVALID.  with_w = 0 is the lid residual (w left out of the
  * numerator), 1 the thermal one.  up, vp, wp (and Tp) receive the current
  * fields like the reference's check().  All calls share the static array:
- * calls that overlap on the GPU race.  The first call on a device looks up the
- * array's address; make it before any stream capture.  Synchronises
- * cuda_stream (NULL = legacy default stream).  On failure a message is written
- * to errbuf (may be NULL). */
+ * calls that overlap on the GPU race.  The first call in each CUDA context on
+ * a device looks up the array's address (cached under the context's unique
+ * id); make that first call before any stream capture.  Synchronises
+ * cuda_stream (NULL = legacy default stream).  The ratios are written as
+ * computed; when either is not finite (a non-finite field, or sum |u|^2 or
+ * sum |T| equal to zero) the call returns MGLC_ERR_NUMERIC.  On failure a
+ * message is written to errbuf (may be NULL). */
 int mglc_residual_noalloc(long long n, const double* u, const double* v, const double* w,
                           const double* T, double* up, double* vp, double* wp, double* Tp,
                           int with_w, void* cuda_stream, double* error_u, double* error_t,

@@ -16,6 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libmglc_gb300.so")
+ROOF_LIB = os.path.join(BUILD, "libmglc_roof.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code: no multiply-add contraction, so host-side constants (relaxation
 # rates, sums) round the same on x86-64 and aarch64 hosts
@@ -80,7 +81,21 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    build_roof()
     return LIB
+
+
+def build_roof() -> str:
+    """The FP64 instruction-rate probe (measurement only, its own library)."""
+    src = os.path.join(HERE, "roof", "fp64_rate.cu")
+    if os.path.exists(ROOF_LIB) and os.path.getmtime(ROOF_LIB) >= os.path.getmtime(src):
+        return ROOF_LIB
+    cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
+           src, "-o", ROOF_LIB, "-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
+    return ROOF_LIB
 
 
 if __name__ == "__main__":

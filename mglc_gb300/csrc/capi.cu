@@ -603,9 +603,11 @@ int mglc_step(mglc_ctx* c, int nsteps) {
                                          "particle-particle interpenetration",
                                          "particle penetrates a wall",
                                          "no refill direction for a node leaving a particle",
-                                         "too many nodes left one particle in one step"};
+                                         "too many nodes left one particle in one step",
+                                         "particle state diverged (not finite, or a centre moved "
+                                         "half the periodic length or more in one step)"};
             return fail(c, MGLC_ERR_PARTICLE, "%s (particle %d, other %d); the state is frozen at that step",
-                        what[st[0] < 7 ? st[0] : 0], st[1], st[2]);
+                        what[st[0] < 8 ? st[0] : 0], st[1], st[2]);
         }
         return MGLC_OK;
     }

@@ -66,12 +66,18 @@ __device__ __forceinline__ void pset(S* f, long long idx, int q, double v, doubl
     PSt<S>::st(f + idx, PSt<S>::SHIFT ? v - w19(q) * rho0 : v);
 }
 
+// Signed x separation with the nearest periodic image.  Centres stay in
+// [0.5, nx + 0.5) and nodes in [1, nx], so one shift by L brings d into
+// [-L/2, L/2]; a larger |d| (a centre that jumped, which k_pmove reports)
+// takes the closed form d - L rint(d/L).  A non-finite d is returned as is:
+// no loop depends on it.
 __device__ __forceinline__ double dxp(double a, double b, const PartParams& p) {
     double d = a - b;
-    if (p.periodic_x) {
-        const double L = (double)p.nx;
-        while (d > 0.5 * L) d -= L;
-        while (d < -0.5 * L) d += L;
+    if (p.periodic_x && isfinite(d)) {
+        const double L = (double)p.nx, h = 0.5 * L;
+        if (d > h) d -= L;
+        else if (d < -h) d += L;
+        if (d > h || d < -h) d -= L * rint(d / L);
     }
     return d;
 }
@@ -664,6 +670,7 @@ __global__ void k_pmove(PartParams p, PartDev d) {
     const double R0 = p.radius;
     const double M = p.rho_solid * 4.0 / 3.0 * p.pi * R0 * R0 * R0;
     const double I = 0.4 * M * R0 * R0;
+    bool ok = true;
     for (int q = 0; q < 3; q++) {
         d.xc_old[3 * c + q] = d.xc[3 * c + q];
         d.uc_old[3 * c + q] = d.uc[3 * c + q];
@@ -672,12 +679,18 @@ __global__ void k_pmove(PartParams p, PartDev d) {
         d.uc[3 * c + q] = d.uc_old[3 * c + q] + a;
         d.om[3 * c + q] = d.om_old[3 * c + q] + d.ttot[3 * c + q] / I;
         d.xc[3 * c + q] = d.xc_old[3 * c + q] + d.uc_old[3 * c + q] + 0.5 * a;
+        ok = ok && isfinite(d.xc[3 * c + q]) && isfinite(d.uc[3 * c + q]) &&
+             isfinite(d.om[3 * c + q]);
     }
     if (p.periodic_x) {
+        // one wrap per step is enough only while the step moves the centre by
+        // less than half the periodic length
         const double L = (double)p.nx;
+        ok = ok && fabs(d.xc[3 * c] - d.xc_old[3 * c]) < 0.5 * L;
         if (d.xc[3 * c] >= L + 0.5) d.xc[3 * c] -= L;
         if (d.xc[3 * c] < 0.5) d.xc[3 * c] += L;
     }
+    if (!ok && atomicCAS(d.status, 0, PS_DIVERGED) == 0) d.status[1] = c;
 }
 
 // -------------------------------------------------------------- new mask --

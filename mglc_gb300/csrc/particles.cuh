@@ -20,6 +20,8 @@ enum PartStatus {
     PS_WALL = 4,
     PS_NO_REFILL_DIR = 5,
     PS_REFILL_FULL = 6,
+    PS_DIVERGED = 7,  // a centre, velocity or spin is not finite, or a centre
+                      // moved half the periodic length or more in one step
 };
 
 struct PartParams {

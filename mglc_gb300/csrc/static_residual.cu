@@ -15,9 +15,13 @@
 // array per device and it keeps the last call's contents; every slot a call
 // reads is written earlier in the same call, so nothing needs clearing, but
 // calls that overlap on the GPU (concurrent streams) race on the array and
-// must be serialised by the caller.  The first call on a device looks up the
-// array's device address (cudaGetSymbolAddress) with that device current;
-// make that first call before any stream capture.
+// must be serialised by the caller.  The array's device address belongs to a
+// CUDA context: the first call in each context on a device looks it up
+// (cudaGetSymbolAddress, with that device current) and keeps it under the
+// context's unique id, so a new context (after cudaDeviceReset, or a host
+// runtime that makes its own) gets its own lookup; make that first call
+// before any stream capture.  Each call waits for its stream to finish
+// (cudaStreamSynchronize) before it returns the sums.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -39,7 +43,20 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) double g_residual_scratch[kMaxBlocks * 4 + 4];
 
 std::mutex g_setup_mu;
-double* g_scratch_ptr[kMaxDevices] = {};
+// one cached address per device, valid for the context whose id it records
+struct ScratchSlot {
+    bool valid;
+    unsigned long long ctx_id;
+    double* ptr;
+};
+ScratchSlot g_scratch[kMaxDevices] = {};
+
+// driver entry points for the current context's unique id (CUDA 12.0+),
+// looked up through the runtime so the library needs no libcuda link
+using CtxGetCurrentFn = int (*)(void**);
+using CtxGetIdFn = int (*)(void*, unsigned long long*);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
 
 // One block per tile of kCellsPerBlock cells; each block writes its own four
 // partial-sum slots (sum (u-up)^2+(v-vp)^2[+(w-wp)^2], sum |u|^2, sum |T-Tp|,
@@ -105,7 +122,23 @@ int set_error(char* buf, int len, int code, const char* msg) {
     return code;
 }
 
-// Device address of the static scratch for the current device, looked up once.
+// Device address of the static scratch in the current context.
+int symbol_address(double** out, char* errbuf, int errlen) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_residual_scratch);
+    if (e != cudaSuccess || !p) {
+        cudaGetLastError();
+        char m[256];
+        std::snprintf(m, sizeof m, "cudaGetSymbolAddress of the static residual scratch failed: %s",
+                      cudaGetErrorString(e));
+        return set_error(errbuf, errlen, MGLC_ERR_CUDA, m);
+    }
+    *out = (double*)p;
+    return MGLC_OK;
+}
+
+// The scratch address for the current device's current context, looked up
+// once per context (a context's id is unique for the life of the process).
 int scratch_for_current_device(double** out, char* errbuf, int errlen) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
@@ -118,19 +151,48 @@ int scratch_for_current_device(double** out, char* errbuf, int errlen) {
     if (dev < 0 || dev >= kMaxDevices)
         return set_error(errbuf, errlen, MGLC_ERR_UNSUPPORTED, "device ordinal above 63");
     std::lock_guard<std::mutex> lock(g_setup_mu);
-    if (!g_scratch_ptr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_residual_scratch);
-        if (e != cudaSuccess || !p) {
+    if (!g_ctx_get_current || !g_ctx_get_id) {
+        void* a = nullptr;
+        void* b = nullptr;
+        cudaDriverEntryPointQueryResult qa = cudaDriverEntryPointSymbolNotFound, qb = qa;
+        e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa);
+        if (e == cudaSuccess)
+            e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb);
+        if (e != cudaSuccess || qa != cudaDriverEntryPointSuccess ||
+            qb != cudaDriverEntryPointSuccess || !a || !b) {
             cudaGetLastError();
-            char m[256];
-            std::snprintf(m, sizeof m, "cudaGetSymbolAddress of the static residual scratch failed: %s",
-                          cudaGetErrorString(e));
-            return set_error(errbuf, errlen, MGLC_ERR_CUDA, m);
+            return set_error(errbuf, errlen, MGLC_ERR_CUDA,
+                             "the CUDA driver lacks cuCtxGetCurrent/cuCtxGetId (CUDA 12.0 or later needed)");
         }
-        g_scratch_ptr[dev] = (double*)p;
+        g_ctx_get_current = (CtxGetCurrentFn)a;
+        g_ctx_get_id = (CtxGetIdFn)b;
     }
-    *out = g_scratch_ptr[dev];
+    void* ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != 0)
+        return set_error(errbuf, errlen, MGLC_ERR_CUDA, "cuCtxGetCurrent failed");
+    double* fresh = nullptr;
+    if (!ctx) {
+        // nothing current on this thread yet: the runtime call makes the
+        // device's primary context current, then the context is known
+        int rc = symbol_address(&fresh, errbuf, errlen);
+        if (rc != MGLC_OK) return rc;
+        if (g_ctx_get_current(&ctx) != 0 || !ctx)
+            return set_error(errbuf, errlen, MGLC_ERR_CUDA, "no current CUDA context on this thread");
+    }
+    unsigned long long id = 0;
+    if (g_ctx_get_id(ctx, &id) != 0)
+        return set_error(errbuf, errlen, MGLC_ERR_CUDA, "cuCtxGetId failed");
+    ScratchSlot& slot = g_scratch[dev];
+    if (!slot.valid || slot.ctx_id != id) {
+        if (!fresh) {
+            int rc = symbol_address(&fresh, errbuf, errlen);
+            if (rc != MGLC_OK) return rc;
+        }
+        slot.ptr = fresh;
+        slot.ctx_id = id;
+        slot.valid = true;
+    }
+    *out = slot.ptr;
     return MGLC_OK;
 }
 
@@ -160,11 +222,16 @@ extern "C" int mglc_residual_noalloc(long long n, const double* u, const double*
     if (rc != MGLC_OK) return rc;
     cudaStream_t s = (cudaStream_t)cuda_stream;
     const int nb = (int)((n + kCellsPerBlock - 1) / kCellsPerBlock);
+    cudaGetLastError();  // an earlier, unrelated launch error must not be taken for ours
     k_residual_tiles<<<nb, kBlock, 0, s>>>(n, u, v, w, T, up, vp, wp, Tp, with_w, scratch);
-    k_residual_finish<<<1, 32, 0, s>>>(nb, scratch);
-    double sums[4];
-    cudaError_t e = cudaMemcpyAsync(sums, scratch + 4 * kMaxBlocks, sizeof sums,
-                                    cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) {
+        k_residual_finish<<<1, 32, 0, s>>>(nb, scratch);
+        e = cudaGetLastError();
+    }
+    double sums[4] = {0.0, 0.0, 0.0, 0.0};
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(sums, scratch + 4 * kMaxBlocks, sizeof sums, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -172,9 +239,15 @@ extern "C" int mglc_residual_noalloc(long long n, const double* u, const double*
         std::snprintf(m, sizeof m, "residual kernels failed: %s", cudaGetErrorString(e));
         return set_error(errbuf, errbuf_len, MGLC_ERR_CUDA, m);
     }
-    if (error_u) *error_u = std::sqrt(sums[0]) / std::sqrt(sums[1]);
-    if (error_t) *error_t = T ? sums[2] / sums[3] : 0.0;
-    if (!std::isfinite(sums[0]) || !std::isfinite(sums[1]))
-        return set_error(errbuf, errbuf_len, MGLC_ERR_NUMERIC, "non-finite velocity field");
+    const double eu = std::sqrt(sums[0]) / std::sqrt(sums[1]);
+    const double et = T ? sums[2] / sums[3] : 0.0;
+    if (error_u) *error_u = eu;
+    if (error_t) *error_t = et;
+    // a zero velocity field (sum |u|^2 = 0) or zero temperature field gives
+    // 0/0 or x/0, like a non-finite field: the ratios are written as computed
+    // and the call reports MGLC_ERR_NUMERIC
+    if (!std::isfinite(eu) || !std::isfinite(et))
+        return set_error(errbuf, errbuf_len, MGLC_ERR_NUMERIC,
+                         "residual not finite (a non-finite field, or sum |u|^2 or sum |T| is zero)");
     return MGLC_OK;
 }

@@ -122,7 +122,8 @@ typedef struct {
 typedef struct orc_particles orc_particles;
 orc_particles* orc_pt_create(const orc_pp* p, const double* centers /* np*3 */);
 /* returns 0, or 1 no owning particle, 2 q out of range, 3 particle overlap,
- * 4 wall penetration, 5 no refill direction */
+ * 4 wall penetration, 5 no refill direction, 7 diverged (a centre, velocity
+ * or spin not finite, or a periodic-x move of half the period or more) */
 int orc_pt_step(orc_particles* s, int nsteps);
 void orc_pt_get(const orc_particles* s, double* f, double* f_post, double* rho, double* u,
                 double* v, double* w, int* obst, double* xc, double* uc, double* om,

@@ -66,12 +66,16 @@ static size_t IX(const orc_particles* s, int i, int j, int k) {
 #define SC_(arr, i, j, k) s->arr[IX(s, i, j, k)]
 
 /* signed separation along x with the periodic image (case1 pattern) */
+/* One shift by L suffices while centres stay in [0.5, nx + 0.5); a larger
+ * |d| (a centre that jumped, which update_center reports) takes the closed
+ * form d - L rint(d/L), and a non-finite d is returned as is. */
 static double dxp(const orc_particles* s, double a, double b) {
     double d = a - b;
-    if (s->p.periodic_x) {
-        double L = (double)s->p.nx;
-        while (d > 0.5 * L) d -= L;
-        while (d < -0.5 * L) d += L;
+    if (s->p.periodic_x && isfinite(d)) {
+        double L = (double)s->p.nx, h = 0.5 * L;
+        if (d > h) d -= L;
+        else if (d < -h) d += L;
+        if (d > h || d < -h) d -= L * rint(d / L);
     }
     return d;
 }
@@ -788,9 +792,13 @@ static int update_center(orc_particles* s) {
                 s->uc[3 * c + d] = s->uc_old[3 * c + d] + a;
                 s->om[3 * c + d] = s->om_old[3 * c + d] + s->torque[3 * c + d] / I;
                 s->xc[3 * c + d] = s->xc_old[3 * c + d] + s->uc_old[3 * c + d] + 0.5 * a;
+                if (!isfinite(s->xc[3 * c + d]) || !isfinite(s->uc[3 * c + d]) || !isfinite(s->om[3 * c + d]))
+                    return 7;
             }
             if (p->periodic_x) {
                 double L = (double)p->nx;
+                /* one wrap per step holds only for moves below half the period */
+                if (!(fabs(s->xc[3 * c] - s->xc_old[3 * c]) < 0.5 * L)) return 7;
                 if (s->xc[3 * c] >= L + 0.5) s->xc[3 * c] -= L;
                 if (s->xc[3 * c] < 0.5) s->xc[3 * c] += L;
             }

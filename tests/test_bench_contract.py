@@ -39,6 +39,6 @@ def test_reference_arm_prints_the_contract_line():
 
 def test_reference_arm_other_ranks_exit_quietly():
     r = run_bench({"RANK": "1", "WORLD_SIZE": "2"}, "--impl", "reference", "--workload", "lid64",
-                  "--steps", "3", "--warmup", "3")
+                  "--steps", "3", "--warmup", "3", "--gpus", "2")
     assert r.returncode == 0, r.stderr[-2000:]
     assert not [x for x in r.stdout.splitlines() if x.startswith("{")]
