@@ -195,7 +195,8 @@ def fp64_roof(kind, form, mlups, probe):
     return {"fp64_achieved": round(ach, 1), "fp64_peak": round(peak, 1),
             "fp64_unit": "G FP64 instr/s", "fp64_frac": round(ach / peak, 4),
             "fp64_instr_per_cell": ipc, "fp64_peak_kind": "measured (mglc_gb300/roof/fp64_rate.cu, "
-            "best of DFMA/DADD/DMUL chains, same run)", "fp64_instr_source": tab["source"]}
+            "best of DFMA/DADD/DMUL chains, same run)", "fp64_instr_source": tab["source"],
+            "fp64_probe_g_per_s": {k: round(v / 1e9, 1) for k, v in probe.items()}}
 
 
 def make_solve(mg, wl, form, in_place=False):

@@ -96,9 +96,11 @@ __device__ __forceinline__ void moments0(const T* f, T& rho_m, T& jx, T& jy, T& 
 //  (ux,uy,uz): velocity used in the equilibrium (and source)
 //  FORCED: add the reference's moment-space source (evolution_f.F90:107-129)
 //  LID_MEQ12: lid operator quirk, meq(12) without the factor rho (collision.f90:85)
+//  msc  : scale of f, rho_m, rho and the forces (the lid quirk's meq(12), which
+//         carries no rho, is multiplied by it); 1 for unscaled arithmetic
 template <typename T, bool FORCED, bool LID_MEQ12>
 __device__ __forceinline__ void mrt_collide(T* f, T rho_m, T rho, T ux, T uy, T uz, T fx, T fy,
-                                            T fz, const MrtCoef<T>& c) {
+                                            T fz, const MrtCoef<T>& c, T msc = T(1)) {
     const T two = T(2), four = T(4), half = T(0.5);
     // opposite pairs: (a,b) = (1,2) (3,4) (5,6) (7,10) (9,8) (11,14) (13,12) (15,18) (17,16)
     T s1 = f[1] + f[2], d1 = f[1] - f[2];
@@ -146,7 +148,7 @@ __device__ __forceinline__ void mrt_collide(T* f, T rho_m, T rho, T ux, T uy, T 
     T n9 = m9 - rho * p9;
     T n10 = m10 + half * (rho * p9);
     T n11 = m11 - rho * p11;
-    T n12 = LID_MEQ12 ? (m12 + half * p11) : (m12 + half * (rho * p11));
+    T n12 = LID_MEQ12 ? (m12 + half * (msc * p11)) : (m12 + half * (rho * p11));
     T n13 = m13 - rux * uy;
     T n14 = m14 - ruy * uz;
     T n15 = m15 - rux * uz;

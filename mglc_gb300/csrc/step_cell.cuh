@@ -13,10 +13,18 @@ namespace mglc {
 // ---------------------------------------------------------------- storage --
 template <typename S>
 struct St;
+// SCALED (16-bit types): the cell bodies compute in units of the storage
+// scale (a power of two, so every product with it is exact and the results
+// are bitwise those of unscaled arithmetic); cvt_s / st_s / st_sr_s convert
+// without the scale multiply.
 template <>
 struct St<double> {
     using C = double;
     static constexpr bool SHIFT = false;
+    static constexpr bool SCALED = false;
+    __device__ static C cvt_s(double v) { return v; }
+    __device__ static void st_s(double* p, C v) { *p = v; }
+    __device__ static void st_sr_s(double* p, C v, unsigned) { *p = v; }
     __device__ static C ld(const double* p, float) { return __ldg(p); }
     __device__ static double raw(const double* p) { return __ldg(p); }
     // raw_rw: plain load, for a buffer that the same kernel also writes
@@ -29,6 +37,10 @@ template <>
 struct St<float> {
     using C = float;
     static constexpr bool SHIFT = true;
+    static constexpr bool SCALED = false;
+    __device__ static C cvt_s(float v) { return v; }
+    __device__ static void st_s(float* p, C v) { *p = v; }
+    __device__ static void st_sr_s(float* p, C v, unsigned) { *p = v; }
     __device__ static C ld(const float* p, float) { return __ldg(p); }
     __device__ static float raw(const float* p) { return __ldg(p); }
     __device__ static float raw_rw(const float* p) { return *p; }
@@ -40,6 +52,21 @@ template <>
 struct St<__half> {
     using C = float;
     static constexpr bool SHIFT = true;
+    static constexpr bool SCALED = true;
+    __device__ static C cvt_s(__half v) { return __half2float(v); }
+    __device__ static void st_s(__half* p, C v) { *p = __float2half_rn(v); }
+    __device__ static void st_sr_s(__half* p, C v, unsigned r) {
+        *p = __float2half_rz(__uint_as_float(__float_as_uint(v) + (r >> 19)));
+    }
+    // two values rounded stochastically by the conversion itself (cvt.rs):
+    // a into the high half, b into the low half, each with its own 16 bits
+    // of r; NaN and infinities convert as themselves
+    __device__ static unsigned pack_sr(float a, float b, unsigned r) {
+        unsigned d;
+        asm("cvt.rs.f16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(a), "f"(b), "r"(r));
+        return d;
+    }
+    __device__ static void st_bits(__half* p, unsigned short v) { *p = __ushort_as_half(v); }
     __device__ static C ld(const __half* p, float inv) { return __half2float(__ldg(p)) * inv; }
     __device__ static __half raw(const __half* p) { return __ldg(p); }
     __device__ static __half raw_rw(const __half* p) { return *p; }
@@ -58,6 +85,20 @@ template <>
 struct St<__nv_bfloat16> {
     using C = float;
     static constexpr bool SHIFT = true;
+    static constexpr bool SCALED = true;
+    __device__ static C cvt_s(__nv_bfloat16 v) { return __bfloat162float(v); }
+    __device__ static void st_s(__nv_bfloat16* p, C v) { *p = __float2bfloat16_rn(v); }
+    __device__ static void st_sr_s(__nv_bfloat16* p, C v, unsigned r) {
+        *p = __float2bfloat16_rz(__uint_as_float(__float_as_uint(v) + (r >> 16)));
+    }
+    __device__ static unsigned pack_sr(float a, float b, unsigned r) {
+        unsigned d;
+        asm("cvt.rs.bf16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(a), "f"(b), "r"(r));
+        return d;
+    }
+    __device__ static void st_bits(__nv_bfloat16* p, unsigned short v) {
+        *p = __ushort_as_bfloat16(v);
+    }
     __device__ static C ld(const __nv_bfloat16* p, float inv) {
         return __bfloat162float(__ldg(p)) * inv;
     }
@@ -138,6 +179,27 @@ __device__ __forceinline__ unsigned sr_cell(unsigned cell, unsigned step) {
 __device__ __forceinline__ unsigned sr_pop(unsigned h, int q) {
     return h * (0x2545F491u + 2u * 0x9E3779B9u * (unsigned)q);
 }
+// Random bits of population pair p (populations 2p and 2p+1, rounded by one
+// cvt.rs): the cell hash times a distinct odd constant per pair, plus its
+// high half so that the low 16 bits depend on every bit of the hash.
+__device__ __forceinline__ unsigned sr_pair(unsigned h, unsigned hh, int p) {
+    return h * (0x2545F491u + 2u * 0x9E3779B9u * (unsigned)p) + hh;
+}
+constexpr int NPAIR19 = (Q19 + 1) / 2;
+
+// Stochastically rounded 16-bit words of f[19], two populations per
+// conversion (population 2p in the high half of w[p], 2p+1 in the low half).
+template <typename S, typename C>
+__device__ __forceinline__ void sr_pack19(const C (&f)[Q19], unsigned cell, unsigned seed,
+                                          unsigned (&w)[NPAIR19]) {
+    const unsigned h0 = sr_cell(cell, seed), hh = h0 >> 16;
+#pragma unroll
+    for (int p = 0; p < NPAIR19; p++)
+        w[p] = St<S>::pack_sr(f[2 * p], 2 * p + 1 < Q19 ? f[2 * p + 1] : C(0), sr_pair(h0, hh, p));
+}
+__device__ __forceinline__ unsigned short sr_half(const unsigned (&w)[NPAIR19], int q) {
+    return (unsigned short)((q & 1) ? (w[q >> 1] & 0xFFFFu) : (w[q >> 1] >> 16));
+}
 
 // ------------------------------------------------------------ lid kernel --
 // IDX: 32-bit element indices when Q*cells < 2^31, 64-bit otherwise.
@@ -170,70 +232,67 @@ __device__ __forceinline__ void lid_cell_from(int i, int j, int k, const S (&raw
     using C = typename St<S>::C;
     const int nx = K.nx, ny = K.ny, nz = K.nz;
     const IDX cell = (IDX)i + (IDX)nx * ((IDX)j + (IDX)ny * (IDX)k);
+    // f, rho_m and the momenta in units of the storage scale sc (1 unless
+    // SCALED); rho and u are unscaled, rhos = sc * rho
+    const C sc = St<S>::SCALED ? (C)K.scale : C(1);
     C f[Q19];
 #pragma unroll
-    for (int q = 0; q < Q19; q++) f[q] = St<S>::cvt(raw[q], K.inv_scale);
+    for (int q = 0; q < Q19; q++) f[q] = St<S>::cvt_s(raw[q]);
     C rho_m, rho, ux, uy, uz;
     if (FIRST) {
         rho = (C)mrho[cell];
         ux = (C)mu[cell];
         uy = (C)mv[cell];
         uz = (C)mw[cell];
-        rho_m = St<S>::SHIFT ? rho - K.rho0 : rho;
+        rho_m = St<S>::SHIFT ? (rho - K.rho0) * sc : rho;
     } else {
         C jx, jy, jz;
         moments0(f, rho_m, jx, jy, jz);
-        rho = St<S>::SHIFT ? K.rho0 + rho_m : rho_m;
-        const C inv = recip(rho);
+        rho = St<S>::SHIFT ? K.rho0 + (St<S>::SCALED ? rho_m * (C)K.inv_scale : rho_m) : rho_m;
+        const C inv = St<S>::SCALED ? recip(rho) * (C)K.inv_scale : recip(rho);
         ux = jx * inv;
         uy = jy * inv;
         uz = jz * inv;
     }
-    mrt_collide<C, false, true>(f, rho_m, rho, ux, uy, uz, C(0), C(0), C(0), K.c);
+    const C rhos = St<S>::SCALED ? rho * sc : rho;
+    mrt_collide<C, false, true>(f, rho_m, rhos, ux, uy, uz, C(0), C(0), C(0), K.c, sc);
+    // moving lid: f(14) = f_post(11) - rho/6*U0, f(13) = f_post(12) + rho/6*U0
+    // (bounce_back.f90:77-78).  On the top layer populations 11 and 12 always
+    // leave through the lid (the lid face is written last, so it wins on
+    // edges); the term is applied to them before the stores.
+    if (k == nz - 1) {
+        const C lid = rhos / C(6) * K.u0;
+        f[11] = f[11] - lid;
+        f[12] = f[12] + lid;
+    }
     const IDX sy = (IDX)nx, sz = (IDX)nx * (IDX)ny;
     const unsigned bm = face_mask(i, j, k, nx, ny, nz);
-    const unsigned h0 = sr_cell((unsigned)cell, seed);
-    // stochastic rounding for finite cells; a NaN or infinite cell rounds to
-    // nearest so that the non-finite values propagate unchanged
-    const bool sr = SR && isfinite(rho + ux + uy + uz);
-    auto put = [&](S* p, C v, int q) {
-        if (sr) St<S>::st_sr(p, v, K.scale, sr_pop(h0, q));
-        else St<S>::st(p, v, K.scale);
+    unsigned w[NPAIR19];
+    if constexpr (SR) sr_pack19<S>(f, (unsigned)cell, seed, w);
+    auto put = [&](S* p, int q) {
+        if constexpr (SR) St<S>::st_bits(p, sr_half(w, q));
+        else St<S>::st_s(p, f[q]);
     };
     if (SWAP_STORE) {  // in-place even step: own cell, slot opp(q)
-        C lid = C(0);
-        if (k == nz - 1) lid = rho / C(6) * K.u0;
 #pragma unroll
-        for (int q = 0; q < Q19; q++) {
-            const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
-            C val = f[q];
-            if ((bm & leave_bits(dx, dy, dz)) != 0 && dz > 0 && dx != 0) val = val - C(dx) * lid;
-            put(fout + ((IDX)opp19(q) * P + cell), val, q);
-        }
+        for (int q = 0; q < Q19; q++) put(fout + ((IDX)opp19(q) * P + cell), q);
         return;
     }
     if (bm == 0) {  // interior cell: every population streams
 #pragma unroll
         for (int q = 0; q < Q19; q++) {
             const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
-            put(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), f[q], q);
+            put(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), q);
         }
         return;
     }
-    // moving lid: f(14) = f_post(11) - rho/6*U0, f(13) = f_post(12) + rho/6*U0
-    // (bounce_back.f90:77-78); the lid face is written last, so it wins on edges
-    C lid = C(0);
-    if (k == nz - 1) lid = rho / C(6) * K.u0;
 #pragma unroll
     for (int q = 0; q < Q19; q++) {
         const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
-        if ((bm & leave_bits(dx, dy, dz)) == 0) {
-            put(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), f[q], q);
-        } else {
-            C val = f[q];
-            if (dz > 0 && dx != 0) val = val - C(dx) * lid;
-            put(fout + ((IDX)opp19(q) * P + cell), val, q);
-        }
+        if ((bm & leave_bits(dx, dy, dz)) == 0)
+            put(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), q);
+        else
+            put(fout + ((IDX)opp19(q) * P + cell), q);
     }
 }
 
@@ -406,6 +465,10 @@ __device__ __forceinline__ void thermal_cell_from(
     using C = typename St<S>::C;
     const int nx = K.nx, ny = K.ny, nz = K.nz;
     const IDX cell = (IDX)i + (IDX)nx * ((IDX)j + (IDX)ny * (IDX)k);
+    // f (as loaded by the caller), rho_m and the momenta in units of the
+    // storage scale sc (1 unless SCALED); rho, u, T and the carried force are
+    // unscaled
+    const C sc = St<S>::SCALED ? (C)K.scale : C(1);
     C rho_m, rho, ux, uy, uz, temp;
     if (FIRST) {
         rho = (C)mrho[cell];
@@ -413,11 +476,16 @@ __device__ __forceinline__ void thermal_cell_from(
         uy = (C)mv[cell];
         uz = (C)mw[cell];
         temp = (C)mT[cell];
-        rho_m = St<S>::SHIFT ? rho - K.rho0 : rho;
+        rho_m = St<S>::SHIFT ? (rho - K.rho0) * sc : rho;
     } else {
         C jx, jy, jz;
         moments0(f, rho_m, jx, jy, jz);
-        rho = St<S>::SHIFT ? K.rho0 + rho_m : rho_m;
+        if (St<S>::SCALED) {
+            jx = jx * (C)K.inv_scale;
+            jy = jy * (C)K.inv_scale;
+            jz = jz * (C)K.inv_scale;
+        }
+        rho = St<S>::SHIFT ? K.rho0 + (St<S>::SCALED ? rho_m * (C)K.inv_scale : rho_m) : rho_m;
         const C inv = recip(rho);
         // u^n = (sum f e + F^n/2)/rho^n with the force carried from the previous step
         C fxp = C(0), fyp = C(0);
@@ -441,20 +509,23 @@ __device__ __forceinline__ void thermal_cell_from(
     }
     const C fz = rho * K.gbeta * (temp - K.t_ref);
     F[fz_off + cell] = fz;
-    mrt_collide<C, true, false>(f, rho_m, rho, ux, uy, uz, fx, fy, fz, K.c);
+    if (St<S>::SCALED)
+        mrt_collide<C, true, false>(f, rho_m, rho * sc, ux, uy, uz, fx * sc, fy * sc, fz * sc, K.c);
+    else
+        mrt_collide<C, true, false>(f, rho_m, rho, ux, uy, uz, fx, fy, fz, K.c);
     mrt_collide_t<C>(g, temp, ux, uy, uz, K.para_a, K.qd, K.qnu);
 
     const IDX sy = (IDX)nx, sz = (IDX)nx * (IDX)ny;
     const unsigned bm = face_mask(i, j, k, nx, ny, nz);
-    const unsigned h0 = sr_cell((unsigned)cell, seed);
-    const bool sr = SR && isfinite(rho + ux + uy + uz + temp);
-    auto put = [&](S* p, C v, int q) {
-        if (sr) St<S>::st_sr(p, v, K.scale, sr_pop(h0, q));
-        else St<S>::st(p, v, K.scale);
+    unsigned w[NPAIR19];
+    if constexpr (SR) sr_pack19<S>(f, (unsigned)cell, seed, w);
+    auto put = [&](S* p, int q) {
+        if constexpr (SR) St<S>::st_bits(p, sr_half(w, q));
+        else St<S>::st_s(p, f[q]);
     };
     if (SWAP_STORE) {  // in-place even step: own cell, slot opp(q)
 #pragma unroll
-        for (int q = 0; q < Q19; q++) put(fout + ((IDX)opp19(q) * P + cell), f[q], q);
+        for (int q = 0; q < Q19; q++) put(fout + ((IDX)opp19(q) * P + cell), q);
 #pragma unroll
         for (int q = 0; q < Q7; q++) {
             const int dy = ey19(q), dz = ez19(q);
@@ -471,7 +542,7 @@ __device__ __forceinline__ void thermal_cell_from(
 #pragma unroll
         for (int q = 0; q < Q19; q++) {
             const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
-            put(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), f[q], q);
+            put(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), q);
         }
 #pragma unroll
         for (int q = 0; q < Q7; q++) {
@@ -484,9 +555,9 @@ __device__ __forceinline__ void thermal_cell_from(
     for (int q = 0; q < Q19; q++) {
         const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
         if ((bm & leave_bits(dx, dy, dz)) == 0)
-            put(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), f[q], q);
+            put(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), q);
         else
-            put(fout + ((IDX)opp19(q) * P + cell), f[q], q);
+            put(fout + ((IDX)opp19(q) * P + cell), q);
     }
     // D3Q7: adiabatic walls reflect, constant-T walls anti-bounce-back
     // g_in = -g_out + (6+paraA)/21 * T_wall (bouyancy3d_mpi.F90:1101-1210)
@@ -516,7 +587,7 @@ __device__ __forceinline__ void thermal_cell(
     const IDX cell = (IDX)i + (IDX)K.nx * ((IDX)j + (IDX)K.ny * (IDX)k);
     C f[Q19], g[Q7];
 #pragma unroll
-    for (int q = 0; q < Q19; q++) f[q] = St<S>::ld(fin + ((IDX)q * P + cell), K.inv_scale);
+    for (int q = 0; q < Q19; q++) f[q] = St<S>::cvt_s(St<S>::raw(fin + ((IDX)q * P + cell)));
 #pragma unroll
     for (int q = 0; q < Q7; q++) g[q] = gin[(IDX)q * P + cell];
     thermal_cell_from<S, FIRST, ROT, IDX, SR>(i, j, k, f, g, fout, gout, F, K, P, mrho, mu, mv,
@@ -549,7 +620,7 @@ __device__ __forceinline__ void thermal_load_aa(int i, int j, int k, const S* f,
 #pragma unroll
     for (int q = 0; q < Q7; q++) gv[q] = __ldcg(g + src(q));
 #pragma unroll
-    for (int q = 0; q < Q19; q++) fv[q] = St<S>::cvt(raw[q], K.inv_scale);
+    for (int q = 0; q < Q19; q++) fv[q] = St<S>::cvt_s(raw[q]);  // in units of the storage scale
 }
 
 // -------------------------------------------------- heated cavity, FX64 --
