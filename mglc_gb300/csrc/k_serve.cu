@@ -58,9 +58,25 @@ __global__ void __launch_bounds__(256, THERMAL ? 2 : 3)
         const S* fin = (const S*)sv.f[parity];
         S* fout = (S*)sv.f[parity ^ 1];
         const unsigned seed = sv.step0 + (unsigned)kstep;
+        // cell coordinates of idx = lane, lane + 32, ... kept incrementally
+        // (one division per tile instead of three per cell)
+        int i = lane % nx, j, k;
+        {
+            const int r = r0 + lane / nx;
+            j = r % ny;
+            k = r / ny;
+        }
         for (int idx = lane; idx < ncell; idx += 32) {
-            const int i = idx % nx, r = r0 + idx / nx;
-            const int j = r % ny, k = r / ny;
+            if (idx != lane) {
+                i += 32;
+                while (i >= nx) {  // at most 32 / nx + 1 passes
+                    i -= nx;
+                    if (++j == ny) {
+                        j = 0;
+                        ++k;
+                    }
+                }
+            }
             if (AA) {
                 S* f = (S*)sv.f[0];
                 if (!THERMAL) {
