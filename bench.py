@@ -166,7 +166,7 @@ def fp64_peak():
     out = {}
     for mode, name in ((0, "dfma"), (1, "dadd"), (2, "dmul")):
         r, ms = ctypes.c_double(), ctypes.c_double()
-        rc = L.mglc_roof_fp64(mode, 4096, ctypes.byref(r), ctypes.byref(ms))
+        rc = L.mglc_roof_fp64(mode, 4096, ctypes.byref(r), ctypes.byref(ms))  # mode 0..2
         if rc != 0:
             raise RuntimeError(f"FP64 rate probe failed (CUDA error {rc})")
         out[name] = r.value
@@ -192,8 +192,16 @@ def fp64_roof(kind, form, mlups, probe):
     ipc = tab["fp64_instr_per_cell"]
     peak = max(probe.values()) / 1e9
     ach = ipc * mlups * 1e6 / 1e9
+    # the rate this kernel's own instruction mix allows: DADD and DMUL issue
+    # at their measured rates, DFMA and the other FP64-pipe work at DFMA's
+    other = ipc - tab["dadd"] - tab["dfma"] - tab["dmul"]
+    ns_per_cell = (tab["dadd"] / probe["dadd"] + tab["dmul"] / probe["dmul"] +
+                   (tab["dfma"] + other) / probe["dfma"]) * 1e9
+    mix_mlups = 1e3 / ns_per_cell
     return {"fp64_achieved": round(ach, 1), "fp64_peak": round(peak, 1),
             "fp64_unit": "G FP64 instr/s", "fp64_frac": round(ach / peak, 4),
+            "fp64_mix_roof_mlups": round(mix_mlups, 1),
+            "fp64_mix_frac": round(mlups / mix_mlups, 4),
             "fp64_instr_per_cell": ipc, "fp64_peak_kind": "measured (mglc_gb300/roof/fp64_rate.cu, "
             "best of DFMA/DADD/DMUL chains, same run)", "fp64_instr_source": tab["source"],
             "fp64_probe_g_per_s": {k: round(v / 1e9, 1) for k, v in probe.items()}}
@@ -213,7 +221,7 @@ def make_solve(mg, wl, form, in_place=False):
         return mg.LidDrivenCavity(n, reynolds=wl["reynolds"], u0=wl["u0"], top_layer_u0=False,
                                   precision=form, in_place=in_place)
     return mg.BuoyancyCavity(n, rayleigh=wl["rayleigh"], prandtl=wl["prandtl"], mach=wl["mach"],
-                             t_hot=0.5, t_cold=-0.5, ekman=0.0, precision=form)
+                             t_hot=0.5, t_cold=-0.5, ekman=0.0, precision=form, in_place=in_place)
 
 
 def alg_bytes(kind, form):
@@ -477,7 +485,8 @@ def particle_errors(mg, wl, steps):
 
 
 # the forms timed for each side workload (the first is the workload's own)
-SIDE_FORMS = {"thermal128": ("fp64", "fx64", "fp32", "fp16", "fp16s"),
+SIDE_FORMS = {"thermal128": ("fp64", "fx64", "fp32", "fp16", "fp16s", "fp16_in_place",
+                             "fp16s_in_place", "fp32_in_place"),
               "particles": ("fp32", "fp64")}
 # SURVEY-style algorithmic bytes per cell for the workload's reduced form
 # (16-bit g and a carried 3-vector for the heated cavity; FP32 + mask byte
@@ -499,7 +508,9 @@ def side_workload(torch, mg, key, steps, warmup, peak, probe, cpu=True, errors=T
     traffic_tab = load_traffic()
     for fm in forms:
         try:
-            ms, info = time_device(torch, mg, wl, fm, steps, warmup)
+            ip = fm.endswith("_in_place")
+            ms, info = time_device(torch, mg, wl, fm[:-len("_in_place")] if ip else fm, steps,
+                                   warmup, in_place=ip)
             v = cells * steps / (ms * 1e-3) / 1e6
             bpc = info.bytes_per_cell_step
             ach = bpc * cells / (ms / steps * 1e-3) / 1e9
@@ -536,7 +547,8 @@ def side_workload(torch, mg, key, steps, warmup, peak, probe, cpu=True, errors=T
         try:
             if kind == "thermal":
                 es = wl["error_steps"]
-                errs = form_errors(mg, wl, [f for f in forms if f != "fp64"], es)
+                errs = form_errors(mg, wl, [f for f in forms if f != "fp64" and
+                                            not f.endswith("_in_place")], es)
                 for fm, e in errs.items():
                     out["forms"].setdefault(fm, {}).update(e)
                     out["forms"][fm]["error_steps"] = es

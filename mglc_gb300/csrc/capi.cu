@@ -9,7 +9,6 @@
 #include <nvtx3/nvToolsExt.h>
 
 #include <cmath>
-#include <cstdlib>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -63,8 +62,6 @@ struct mglc_ctx {
     double *up = nullptr, *vp = nullptr, *wp = nullptr, *Tp = nullptr;
     double* partials = nullptr;  // reduction scratch
     double* red_out = nullptr;   // 4 doubles
-    int* step_status = nullptr;  // device status word of the staged-load lid kernel
-    bool staged_loads = true;    // lid, FP32/16-bit: bulk-copy staged loads (MGLC_LID_TMA=0: off)
     double* stage = nullptr;     // layout staging for host copies
     size_t stage_bytes = 0;
     long long device_bytes = 0;
@@ -118,8 +115,7 @@ int dalloc(mglc_ctx* c, void** p, size_t bytes, const char* what) {
 
 void release(mglc_ctx* c) {
     void* ptrs[] = {c->f[0], c->f[1], c->g[0], c->g[1], c->F, c->rho, c->u, c->v, c->w, c->T,
-                    c->up, c->vp, c->wp, c->Tp, c->partials, c->red_out, c->stage,
-                    c->step_status};
+                    c->up, c->vp, c->wp, c->Tp, c->partials, c->red_out, c->stage};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     PartDev& d = c->pd;
@@ -166,10 +162,6 @@ int alloc_common(mglc_ctx* c, bool thermal) {
                      "reduction scratch")))
         return rc;
     if ((rc = dalloc(c, (void**)&c->red_out, 4 * sizeof(double), "reduction result"))) return rc;
-    if ((rc = dalloc(c, (void**)&c->step_status, sizeof(int), "step status"))) return rc;
-    CK(cudaMemsetAsync(c->step_status, 0, sizeof(int), c->stream), "zero step status");
-    const char* tma = std::getenv("MGLC_LID_TMA");
-    c->staged_loads = !(tma && tma[0] == '0');
     return MGLC_OK;
 }
 
@@ -244,23 +236,7 @@ int download_pops(mglc_ctx* c, int Q, const void* dev, double* host, bool shifte
 bool thermal(const mglc_ctx* c) { return c->kind == MGLC_KIND_THERMAL; }
 
 // in place: restore the post-stream layout after an even step (pairwise swap)
-// a step kernel that gave up waiting for its staged loads leaves a status
-// word; every read of the state reports it
-int step_status(mglc_ctx* c) {
-    if (!c->step_status) return MGLC_OK;
-    int st = 0;
-    CK(cudaMemcpyAsync(&st, c->step_status, sizeof st, cudaMemcpyDeviceToHost, c->stream),
-       "read step status");
-    CK(cudaStreamSynchronize(c->stream), "synchronize");
-    if (st)
-        return fail(c, MGLC_ERR_CUDA,
-                    "a step kernel timed out waiting for its staged population loads (status %d)", st);
-    return MGLC_OK;
-}
-
 int natural_layout(mglc_ctx* c) {
-    int rc = step_status(c);
-    if (rc) return rc;
     if (!c->in_place || !c->swapped) return MGLC_OK;
     CK(launch_aa_swap(c->form, c->geom, c->f[0], thermal(c) ? c->g[0] : nullptr, c->stream),
        "in-place layout swap");
@@ -649,7 +625,6 @@ int mglc_step(mglc_ctx* c, int nsteps) {
             a.seed = (unsigned)c->itc;
             a.sr = c->sr ? 1 : 0;
             a.rho = c->rho; a.u = c->u; a.v = c->v; a.w = c->w;
-            a.status = c->staged_loads ? c->step_status : nullptr;
             if (c->in_place) {
                 e = launch_lid_step_aa(c->fx64 ? FORM_FX64 : c->form, c->first_pending, c->swapped,
                                        c->f[0], a, c->stream);

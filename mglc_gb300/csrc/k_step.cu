@@ -127,11 +127,6 @@ static cudaError_t lid_go_fx(bool first, const void* fin, void* fout, const LidS
 
 cudaError_t launch_lid_step(int form, bool first, const void* fin, void* fout,
                             const LidStepArgs& a, cudaStream_t s) {
-    // after the first step, the FP32 and 16-bit forms stage their loads
-    // through shared memory when the rows allow aligned bulk copies
-    if (!first && a.status && (form == FORM_FP32 || form == FORM_FP16 || form == FORM_BF16) &&
-        lid_tma_ok(a.g, form_bytes(form), fin, fout))
-        return launch_lid_step_tma(form, fin, fout, a, a.status, s);
     switch (form) {
         case FORM_FX64: return lid_go_fx(first, fin, fout, a, s);
         case FORM_FP64: return lid_go<double>(first, fin, fout, a, s);

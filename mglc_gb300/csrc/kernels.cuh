@@ -31,9 +31,6 @@ struct LidStepArgs {
     // macroscopic fields used by the first step after initial()/load (the
     // reference's collision reads the stored rho,u,v,w)
     const double *rho, *u, *v, *w;
-    // device status word of the staged-load kernel (k_step_tma.cu); NULL
-    // selects the one-thread-per-cell kernel with direct loads
-    int* status = nullptr;
 };
 
 struct ThermalStepArgs {
@@ -58,11 +55,6 @@ cudaError_t launch_thermal_step_aa(int form, bool first, bool odd, void* f, void
 cudaError_t launch_aa_swap(int form, const Geom& g, void* f, void* gt, cudaStream_t s);
 cudaError_t launch_lid_step(int form, bool first, const void* fin, void* fout,
                             const LidStepArgs& a, cudaStream_t s);
-// the lid step with bulk-copy staged loads (FP32 and 16-bit forms, rows of a
-// multiple of 16 bytes); lid_tma_ok tells whether it applies
-bool lid_tma_ok(const Geom& g, size_t elem, const void* fin, const void* fout);
-cudaError_t launch_lid_step_tma(int form, const void* fin, void* fout, const LidStepArgs& a,
-                                int* status, cudaStream_t s);
 cudaError_t launch_thermal_step(int form, bool first, const void* fin, void* fout,
                                 const void* gin, void* gout, void* F, const ThermalStepArgs& a,
                                 cudaStream_t s);

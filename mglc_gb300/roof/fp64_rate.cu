@@ -16,7 +16,8 @@ constexpr int kThreads = 256;
 constexpr int kChains = 8;
 
 template <int MODE>
-__global__ void __launch_bounds__(kThreads) k_fp64_rate(double* out, int iters, double a, double b) {
+__global__ void __launch_bounds__(kThreads) k_fp64_rate(double* out, int iters, double a, double b,
+                                                        double one, double mzero) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     double x[kChains];
 #pragma unroll
@@ -26,7 +27,9 @@ __global__ void __launch_bounds__(kThreads) k_fp64_rate(double* out, int iters, 
         for (int k = 0; k < kChains; k++) {
             if (MODE == 0) x[k] = fma(x[k], a, b);
             else if (MODE == 1) x[k] = x[k] + b;
-            else x[k] = x[k] * a;
+            else if (MODE == 2) x[k] = x[k] * a;
+            else if (MODE == 3) x[k] = fma(x[k], one, b);  // an add issued as a fused multiply-add
+            else x[k] = fma(x[k], a, mzero);                // a multiply issued as one
         }
     }
     double s = 0.0;
@@ -37,16 +40,18 @@ __global__ void __launch_bounds__(kThreads) k_fp64_rate(double* out, int iters, 
 
 template <int MODE>
 cudaError_t launch(int blocks, double* out, int iters, double a, double b) {
-    k_fp64_rate<MODE><<<blocks, kThreads>>>(out, iters, a, b);
+    // one and -0 arrive as kernel arguments, so the compiler cannot fold them
+    k_fp64_rate<MODE><<<blocks, kThreads>>>(out, iters, a, b, 1.0, -0.0);
     return cudaGetLastError();
 }
 
 }  // namespace
 
-// mode 0: DFMA, 1: DADD, 2: DMUL.  Writes FP64 instructions per second and
-// the best kernel time.  Returns 0 or a CUDA error code.
+// mode 0: DFMA, 1: DADD, 2: DMUL, 3: add as DFMA (x * 1 + b), 4: multiply as
+// DFMA (x * a + -0).  Writes FP64 instructions per second and the best kernel
+// time.  Returns 0 or a CUDA error code.
 extern "C" int mglc_roof_fp64(int mode, int iters, double* inst_per_s, double* best_ms) {
-    if (mode < 0 || mode > 2 || iters < 1 || !inst_per_s) return (int)cudaErrorInvalidValue;
+    if (mode < 0 || mode > 4 || iters < 1 || !inst_per_s) return (int)cudaErrorInvalidValue;
     int dev = 0, sms = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -64,7 +69,9 @@ extern "C" int mglc_roof_fp64(int mode, int iters, double* inst_per_s, double* b
         cudaEventRecord(e0);
         e = mode == 0 ? launch<0>(blocks, out, iters, a, b)
           : mode == 1 ? launch<1>(blocks, out, iters, a, b)
-                      : launch<2>(blocks, out, iters, a, b);
+          : mode == 2 ? launch<2>(blocks, out, iters, a, b)
+          : mode == 3 ? launch<3>(blocks, out, iters, a, b)
+                      : launch<4>(blocks, out, iters, a, b);
         cudaEventRecord(e1);
         if (e == cudaSuccess) e = cudaEventSynchronize(e1);
         float ms = 0.f;
