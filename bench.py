@@ -386,6 +386,8 @@ def time_e2e(torch, mg, wl, form, steps, dist=None):
         dist.barrier()
     t0 = time.perf_counter()
     capi.check(s.handle, L.mglc_load_state(s.handle, ptr(f_h), ptr(g_h), None, None, None, None, None))
+    torch.cuda.synchronize()  # phase mark only: the copies are asynchronous from pinned memory
+    t_load = time.perf_counter()
     capi.check(s.handle, L.mglc_step(s.handle, steps))
     capi.check(s.handle, L.mglc_get_macros(s.handle, *[ptr(a) for a in fields[:4]],
                                            ptr(fields[4]) if q_g else None))
@@ -397,7 +399,9 @@ def time_e2e(torch, mg, wl, form, steps, dist=None):
     s.close()
     h2d = 8 * (19 + q_g) * cells
     d2h = 8 * len(fields) * cells + 8
-    return dt, h2d / steps, d2h / steps, float(eu.value)
+    phases = {"load_state_s": round(t_load - t0, 4), "steps_and_readback_s": round(t1 - t_load, 4),
+              "h2d_gbs": round(h2d / max(t_load - t0, 1e-9) / 1e9, 1)}
+    return dt, h2d / steps, d2h / steps, float(eu.value), phases
 
 
 def time_e2e_particles(torch, s, wl, steps, dist=None):
@@ -420,7 +424,7 @@ def time_e2e_particles(torch, s, wl, steps, dist=None):
     capi.check(s.handle, L.mglc_particle_state(s.handle, *[ptr(a) for a in st]))
     dt = max_over_ranks(torch, dist, time.perf_counter() - t0)
     s.close()
-    return dt, 0, (8 * 4 * cells + 8 * 15 * wl["np"]) / steps, 0.0
+    return dt, 0, (8 * 4 * cells + 8 * 15 * wl["np"]) / steps, 0.0, {}
 
 
 def rel_l2(a, b):
@@ -476,11 +480,20 @@ def particle_errors(mg, wl, steps):
     u32, st32, m32 = run("fp32")
     x0 = place_spheres(*wl["n"], wl["np"], wl["radius"], wl["seed"])
     fluid = (m64 < 0) & (m32 < 0)
+    R = wl["radius"]
+    f_rms = float(np.sqrt((st64["force"] ** 2).sum(axis=1).mean()))
     return {"error_steps": steps,
             "u_rel_l2_vs_fp64": rel_l2(u32[:, fluid], u64[:, fluid]),
             "displacement_rel_l2_vs_fp64": rel_l2(st32["xc"] - x0, st64["xc"] - x0),
             "force_rel_l2_vs_fp64": rel_l2(st32["force"], st64["force"]),
             "torque_rel_l2_vs_fp64": rel_l2(st32["torque"], st64["torque"]),
+            # the torques nearly cancel (rms far below force x radius), so their
+            # relative error is large; against the natural scale |F| R it is small
+            "force_rms_fp64": f_rms,
+            "torque_rms_fp64": float(np.sqrt((st64["torque"] ** 2).sum(axis=1).mean())),
+            "torque_err_rms_over_force_rms_x_radius":
+                float(np.sqrt(((st32["torque"] - st64["torque"]) ** 2).sum(axis=1).mean())) /
+                (f_rms * R),
             "mask_nodes_differing": int((m64 != m32).sum())}
 
 
@@ -1025,11 +1038,11 @@ def main():
             line["roofline"].update(fr)
             line["roofline"]["bound"] = "fp64"
     if not args.no_e2e:  # every rank runs its replica end to end; the slowest one counts
-        dt, h2d, d2h, eu = time_e2e(torch, mglc_gb300, wl, args.form, args.steps, dist)
+        dt, h2d, d2h, eu, phases = time_e2e(torch, mglc_gb300, wl, args.form, args.steps, dist)
         line["e2e"] = {"value": round(world * cells * args.steps / dt / 1e6, 3), "unit": "MLUPS",
                        "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                        "what": "mglc_load_state(host f) + mglc_step(K) + mglc_get_macros(host) "
-                               "+ mglc_check, wall clock"}
+                               "+ mglc_check, wall clock", "phases": phases}
     if rank == 0 and not args.no_forms:
         forms = {}
         fms = {"particle": ("fp64", "fp32"),
