@@ -197,7 +197,9 @@ int mglc_initial(mglc_ctx* ctx);
 /* Load a state from host arrays in the reference layout (the reload path
  * bouyancy3d_mpi.F90:598-611).  g is used by thermal contexts only.  rho,u,v,w
  * (and T) are the macroscopic fields the next collision uses; pass NULL for
- * all of them to derive them from f (and g) with the reference macro. */
+ * all of them to derive them from f (and g) with the reference macro.  Returns
+ * once the host arrays have been read (they may be reused); the conversion to
+ * the device layout may still be running on the context's stream. */
 int mglc_load_state(mglc_ctx* ctx, const double* f, const double* g, const double* rho,
                     const double* u, const double* v, const double* w, const double* T);
 /* Copy the post-stream populations f (and g) back in the reference layout. */

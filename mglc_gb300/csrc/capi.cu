@@ -62,8 +62,11 @@ struct mglc_ctx {
     double *up = nullptr, *vp = nullptr, *wp = nullptr, *Tp = nullptr;
     double* partials = nullptr;  // reduction scratch
     double* red_out = nullptr;   // 4 doubles
-    double* stage = nullptr;     // layout staging for host copies
-    size_t stage_bytes = 0;
+    double* stage = nullptr;     // layout staging for host copies: two halves, so the
+    size_t stage_bytes = 0;      // copy of one chunk overlaps the conversion of the other
+    cudaStream_t copy_stream = nullptr;               // host copies of the staged chunks
+    cudaEvent_t stage_ready[2] = {nullptr, nullptr};  // a half holds a copied / converted chunk
+    cudaEvent_t stage_free[2] = {nullptr, nullptr};   // a half's chunk has been used
     long long device_bytes = 0;
     // state flags
     bool first_pending = false;  // next step reads the stored macroscopic fields
@@ -124,6 +127,11 @@ void release(mglc_ctx* c) {
                      d.partials, d.n_fluid, d.rho_avg, d.status};
     for (void* p : pptrs)
         if (p) cudaFree(p);
+    for (int h = 0; h < 2; h++) {
+        if (c->stage_ready[h]) cudaEventDestroy(c->stage_ready[h]);
+        if (c->stage_free[h]) cudaEventDestroy(c->stage_free[h]);
+    }
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -173,8 +181,17 @@ int create_stream(mglc_ctx* c) {
 }
 
 int ensure_stage(mglc_ctx* c, size_t want) {
+    if (!c->copy_stream) {
+        CK(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking), "copy stream");
+        for (int h = 0; h < 2; h++) {
+            CK(cudaEventCreateWithFlags(&c->stage_ready[h], cudaEventDisableTiming), "stage event");
+            CK(cudaEventCreateWithFlags(&c->stage_free[h], cudaEventDisableTiming), "stage event");
+        }
+    }
     if (c->stage_bytes >= want) return MGLC_OK;
     if (c->stage) {
+        CK(cudaStreamSynchronize(c->stream), "synchronize");
+        CK(cudaStreamSynchronize(c->copy_stream), "synchronize");
         cudaFree(c->stage);
         c->device_bytes -= (long long)c->stage_bytes;
         c->stage = nullptr;
@@ -185,10 +202,10 @@ int ensure_stage(mglc_ctx* c, size_t want) {
     return rc;
 }
 
-// cells per host transfer chunk (whole z planes, at most ~64 MiB of AoS doubles)
+// cells per staged chunk: whole x-y planes, about 128 MB of FP64 AoS data
 long long chunk_cells(const mglc_ctx* c, int Q) {
     const long long plane = (long long)c->geom.nx * c->geom.ny;
-    long long kc = (64ll << 20) / ((long long)Q * 8 * plane);
+    long long kc = (128ll << 20) / ((long long)Q * 8 * plane);
     if (kc < 1) kc = 1;
     if (kc > c->geom.nz) kc = c->geom.nz;
     return kc * plane;
@@ -200,35 +217,64 @@ int pop_form(const mglc_ctx* c, int Q) {
     return c->form == FORM_FP64 ? FORM_FP64 : FORM_FP32;
 }
 
+// Host AoS populations -> device SoA form, through the two staging halves:
+// the copy of chunk n (copy stream) overlaps the conversion of chunk n - 1
+// (context stream); events order each half's copy after its previous
+// conversion and each conversion after its copy.
 int upload_pops(mglc_ctx* c, int Q, const double* host, void* dev, bool shifted) {
     const long long cc = chunk_cells(c, Q);
-    int rc = ensure_stage(c, (size_t)cc * Q * sizeof(double));
+    int rc = ensure_stage(c, 2 * (size_t)cc * Q * sizeof(double));
     if (rc) return rc;
-    for (long long c0 = 0; c0 < c->n; c0 += cc) {
+    // the copy stream starts after everything already queued on the context's stream
+    CK(cudaEventRecord(c->stage_free[0], c->stream), "event");
+    CK(cudaEventRecord(c->stage_free[1], c->stream), "event");
+    int n = 0;
+    for (long long c0 = 0; c0 < c->n; c0 += cc, n++) {
+        const int h = n & 1;
+        double* half = c->stage + (size_t)h * cc * Q;
         long long nc = std::min(cc, c->n - c0);
-        CK(cudaMemcpyAsync(c->stage, host + (size_t)c0 * Q, (size_t)nc * Q * sizeof(double),
-                           cudaMemcpyHostToDevice, c->stream),
+        CK(cudaStreamWaitEvent(c->copy_stream, c->stage_free[h], 0), "wait");
+        CK(cudaMemcpyAsync(half, host + (size_t)c0 * Q, (size_t)nc * Q * sizeof(double),
+                           cudaMemcpyHostToDevice, c->copy_stream),
            "copy populations to device");
-        CK(launch_aos_to_soa(pop_form(c, Q), Q, c->geom, c0, nc, c->stage, dev, c->rho0,
+        CK(cudaEventRecord(c->stage_ready[h], c->copy_stream), "event");
+        CK(cudaStreamWaitEvent(c->stream, c->stage_ready[h], 0), "wait");
+        CK(launch_aos_to_soa(pop_form(c, Q), Q, c->geom, c0, nc, half, dev, c->rho0,
                              Q == Q19 ? c->scale : 1.0f, shifted, c->stream),
            "aos_to_soa");
+        CK(cudaEventRecord(c->stage_free[h], c->stream), "event");
     }
+    // the host array may be reused once this returns: wait for its copies (the
+    // last conversions stay queued on the context's stream)
+    CK(cudaStreamSynchronize(c->copy_stream), "synchronize");
     return MGLC_OK;
 }
 
+// Device SoA form -> host AoS, the reverse pipeline: the conversion of chunk
+// n (context stream) overlaps the copy of chunk n - 1 (copy stream).
 int download_pops(mglc_ctx* c, int Q, const void* dev, double* host, bool shifted) {
     const long long cc = chunk_cells(c, Q);
-    int rc = ensure_stage(c, (size_t)cc * Q * sizeof(double));
+    int rc = ensure_stage(c, 2 * (size_t)cc * Q * sizeof(double));
     if (rc) return rc;
-    for (long long c0 = 0; c0 < c->n; c0 += cc) {
+    CK(cudaEventRecord(c->stage_free[0], c->copy_stream), "event");
+    CK(cudaEventRecord(c->stage_free[1], c->copy_stream), "event");
+    int n = 0;
+    for (long long c0 = 0; c0 < c->n; c0 += cc, n++) {
+        const int h = n & 1;
+        double* half = c->stage + (size_t)h * cc * Q;
         long long nc = std::min(cc, c->n - c0);
-        CK(launch_soa_to_aos(pop_form(c, Q), Q, c->geom, c0, nc, dev, c->stage, c->rho0,
+        CK(cudaStreamWaitEvent(c->stream, c->stage_free[h], 0), "wait");
+        CK(launch_soa_to_aos(pop_form(c, Q), Q, c->geom, c0, nc, dev, half, c->rho0,
                              Q == Q19 ? c->inv_scale : 1.0f, shifted, c->stream),
            "soa_to_aos");
-        CK(cudaMemcpyAsync(host + (size_t)c0 * Q, c->stage, (size_t)nc * Q * sizeof(double),
-                           cudaMemcpyDeviceToHost, c->stream),
+        CK(cudaEventRecord(c->stage_ready[h], c->stream), "event");
+        CK(cudaStreamWaitEvent(c->copy_stream, c->stage_ready[h], 0), "wait");
+        CK(cudaMemcpyAsync(host + (size_t)c0 * Q, half, (size_t)nc * Q * sizeof(double),
+                           cudaMemcpyDeviceToHost, c->copy_stream),
            "copy populations to host");
+        CK(cudaEventRecord(c->stage_free[h], c->copy_stream), "event");
     }
+    CK(cudaStreamSynchronize(c->copy_stream), "synchronize");
     CK(cudaStreamSynchronize(c->stream), "synchronize");
     return MGLC_OK;
 }

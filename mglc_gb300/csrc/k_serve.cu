@@ -38,8 +38,16 @@ __device__ __forceinline__ int next_tile_warp(unsigned* counter) {
 // write each cell's own slots, odd steps read upstream and write downstream;
 // iterations have an even step count, so a solve is in the post-stream layout
 // whenever the residual or the field readers see it).
+// resident CTAs of 256 threads per SM the register allocation is held to
+#ifndef MGLC_SERVE_LID_MINB
+#define MGLC_SERVE_LID_MINB 3
+#endif
+#ifndef MGLC_SERVE_HEAT_MINB
+#define MGLC_SERVE_HEAT_MINB 2
+#endif
+
 template <typename S, bool THERMAL, bool SR, bool AA>
-__global__ void __launch_bounds__(256, THERMAL ? 2 : 3)
+__global__ void __launch_bounds__(256, THERMAL ? MGLC_SERVE_HEAT_MINB : MGLC_SERVE_LID_MINB)
     k_serve_step(const ServeTable* __restrict__ tab, int kstep, unsigned* counter) {
     const int parity = kstep & 1;
     const int base = THERMAL ? tab->lid_tiles : 0;
