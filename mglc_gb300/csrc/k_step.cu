@@ -19,14 +19,14 @@
 namespace mglc {
 
 template <typename S, bool FIRST, typename IDX, bool SR>
-__global__ void __launch_bounds__(128, sizeof(S) <= 4 ? MGLC_LID_MINB : 4)
+__global__ void __launch_bounds__(128)
     k_lid_step(const S* __restrict__ fin, S* __restrict__ fout, StepK<typename St<S>::C> K,
                IDX P, const double* __restrict__ mrho, const double* __restrict__ mu,
                const double* __restrict__ mv, const double* __restrict__ mw) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= K.nx) return;
-    for (RowWalk w(K.ny, K.nz); w.more(); w.next())
-        lid_cell<S, FIRST, IDX, SR>(i, w.j, w.k, fin, fout, K, P, mrho, mu, mv, mw, K.seed);
+    lid_cell<S, FIRST, IDX, SR>(i, blockIdx.y, blockIdx.z, fin, fout, K, P, mrho, mu, mv, mw,
+                                K.seed);
 }
 
 template <bool FIRST, typename IDX>
@@ -77,18 +77,6 @@ static dim3 step_block(int nx) {
 static dim3 step_grid(const Geom& g, dim3 b) {
     return dim3((g.nx + b.x - 1) / b.x, g.ny, g.nz);
 }
-// SMs of the current device (looked up once per device ordinal)
-static int sm_count() {
-    static int cache[64] = {};
-    int dev = 0;
-    cudaGetDevice(&dev);
-    int& n = cache[dev & 63];
-    if (n == 0) {
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        if (n < 1) n = 1;
-    }
-    return n;
-}
 
 template <typename S>
 static cudaError_t lid_go(bool first, const void* fin, void* fout, const LidStepArgs& a,
@@ -98,8 +86,6 @@ static cudaError_t lid_go(bool first, const void* fin, void* fout, const LidStep
     K.seed = a.seed;
     K.sr = a.sr;
     dim3 b = step_block(a.g.nx), gr = step_grid(a.g, b);
-    gr.y = row_slots((long long)a.g.ny * a.g.nz, gr.x, sm_count());
-    gr.z = 1;
     const bool small = (long long)Q19 * a.g.plane < (1ll << 31);
     // stochastic rounding exists for the 16-bit storage types only
     constexpr bool kHalf = sizeof(S) == 2;

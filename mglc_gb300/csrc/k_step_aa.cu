@@ -13,17 +13,16 @@
 namespace mglc {
 
 template <typename S, bool FIRST, typename IDX, bool SR, bool ODD>
-__global__ void __launch_bounds__(128, sizeof(S) <= 4 ? MGLC_LID_MINB : 4)
+__global__ void __launch_bounds__(128)
     k_lid_step_aa(S* f, StepK<typename St<S>::C> K, IDX P, const double* __restrict__ mrho,
                   const double* __restrict__ mu, const double* __restrict__ mv,
                   const double* __restrict__ mw) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= K.nx) return;
-    for (RowWalk w(K.ny, K.nz); w.more(); w.next()) {
-        S raw[Q19];  // every load is issued before the first store
-        lid_load_aa<S, IDX, ODD>(i, w.j, w.k, f, K.nx, K.ny, K.nz, P, raw);
-        lid_cell_from<S, FIRST, IDX, SR, !ODD>(i, w.j, w.k, raw, f, K, P, mrho, mu, mv, mw, K.seed);
-    }
+    const int j = blockIdx.y, k = blockIdx.z;
+    S raw[Q19];  // every load is issued before the first store
+    lid_load_aa<S, IDX, ODD>(i, j, k, f, K.nx, K.ny, K.nz, P, raw);
+    lid_cell_from<S, FIRST, IDX, SR, !ODD>(i, j, k, raw, f, K, P, mrho, mu, mv, mw, K.seed);
 }
 
 // FX64 lid cavity in place (FP64 storage, Q55 collision)
@@ -108,12 +107,7 @@ cudaError_t lid_go_aa(bool first, bool odd, void* f, const LidStepArgs& a, cudaS
     StepK<C> K = make_k<C>(a.g, a.cd, a.u0, a.rho0, a.scale, a.inv_scale);
     K.seed = a.seed;
     K.sr = a.sr;
-    const dim3 b = aa_block(a.g.nx);
-    const unsigned gx = (a.g.nx + b.x - 1) / b.x;
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const dim3 gr(gx, row_slots((long long)a.g.ny * a.g.nz, gx, sms > 0 ? sms : 1), 1);
+    const dim3 b = aa_block(a.g.nx), gr((a.g.nx + b.x - 1) / b.x, a.g.ny, a.g.nz);
     const bool small = (long long)Q19 * a.g.plane < (1ll << 31);
     constexpr bool kHalf = sizeof(S) == 2;  // stochastic rounding: 16-bit storage only
     const bool sr = kHalf && a.sr;

@@ -201,52 +201,6 @@ __device__ __forceinline__ unsigned short sr_half(const unsigned (&w)[NPAIR19], 
     return (unsigned short)((q & 1) ? (w[q >> 1] & 0xFFFFu) : (w[q >> 1] >> 16));
 }
 
-// ------------------------------------------------------- row striding --
-// The step kernels run a grid of (x segments) x (a bounded number of row
-// slots): block y-slot b visits the rows (j, k) = b, b + G, b + 2G, ... of the
-// ny*nz rows, so the blocks stay resident for the whole step instead of being
-// launched and retired once per row.  RowWalk keeps (j, k) without divisions.
-// resident 128-thread blocks per SM the FP32/16-bit step kernels hold their
-// registers to (FP64: 4)
-#ifndef MGLC_LID_MINB
-#define MGLC_LID_MINB 8
-#endif
-struct RowWalk {
-    int j, k, dj, dk, ny;
-    long long r, rows, G;
-    __device__ RowWalk(int ny_, int nz_) : ny(ny_) {
-        G = gridDim.y;
-        rows = (long long)ny_ * nz_;
-        r = blockIdx.y;
-        j = (int)(r % ny_);
-        k = (int)(r / ny_);
-        dj = (int)(G % ny_);
-        dk = (int)(G / ny_);
-    }
-    __device__ bool more() const { return r < rows; }
-    __device__ void next() {
-        r += G;
-        j += dj;
-        k += dk;
-        if (j >= ny) {
-            j -= ny;
-            ++k;
-        }
-    }
-};
-
-// y extent of a step grid: every row when that is few, else enough row slots
-// for about MGLC_ROW_BLOCKS_PER_SM blocks per SM (0: one row per block)
-#ifndef MGLC_ROW_BLOCKS_PER_SM
-#define MGLC_ROW_BLOCKS_PER_SM 32
-#endif
-inline unsigned row_slots(long long rows, unsigned x_blocks, int sms) {
-    if (MGLC_ROW_BLOCKS_PER_SM == 0) return (unsigned)rows;
-    long long want = ((long long)sms * MGLC_ROW_BLOCKS_PER_SM + x_blocks - 1) / x_blocks;
-    if (want < 1) want = 1;
-    return (unsigned)(rows < want ? rows : want);
-}
-
 // ------------------------------------------------------------ lid kernel --
 // IDX: 32-bit element indices when Q*cells < 2^31, 64-bit otherwise.
 // lid_cell_from: collide and push one cell whose 19 stored populations are
