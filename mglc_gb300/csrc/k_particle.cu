@@ -129,8 +129,12 @@ template <typename C> struct PBulkK {
 // fluid density before collision and of the post-collision mass to its own
 // slot, so no block barrier is needed and the totals are added in a fixed
 // order by k_pfinish.
+// resident 128-thread blocks per SM the FP32 bulk kernel holds its registers to
+#ifndef MGLC_PBULK_MINB
+#define MGLC_PBULK_MINB 8
+#endif
 template <typename S, bool FIRST, typename IDX>
-__global__ void __launch_bounds__(128, (sizeof(S) == 4 ? 6 : 4))
+__global__ void __launch_bounds__(128, (sizeof(S) == 4 ? MGLC_PBULK_MINB : 4))
     k_pbulk(const S* __restrict__ fin, S* __restrict__ fout, const int* __restrict__ owner,
             PartParams p, MrtCoef<typename PC<S>::C> cd, PBulkK<typename PC<S>::C> bk,
             double* partials, const int* status) {
@@ -163,10 +167,18 @@ __global__ void __launch_bounds__(128, (sizeof(S) == 4 ? 6 : 4))
             C jx, jy, jz;
             moments0(f, rho_m, jx, jy, jz);
             rho = DEV ? rho0 + rho_m : rho_m;
-            // u = (sum f e + F/2)/rho with F = rho*a (thermal macro form)
-            ux = (jx + C(0.5) * (rho * ax)) / rho;
-            uy = (jy + C(0.5) * (rho * ay)) / rho;
-            uz = (jz + C(0.5) * (rho * az)) / rho;
+            // u = (sum f e + F/2)/rho with F = rho*a (thermal macro form); FP32
+            // multiplies by the correctly rounded reciprocal, FP64 divides
+            if constexpr (sizeof(C) == 4) {
+                const C inv = __frcp_rn(rho);
+                ux = (jx + C(0.5) * (rho * ax)) * inv;
+                uy = (jy + C(0.5) * (rho * ay)) * inv;
+                uz = (jz + C(0.5) * (rho * az)) * inv;
+            } else {
+                ux = (jx + C(0.5) * (rho * ax)) / rho;
+                uy = (jy + C(0.5) * (rho * ay)) / rho;
+                uz = (jz + C(0.5) * (rho * az)) / rho;
+            }
         }
         // deviation storage sums deviations (rho0 added back per warp)
         cacc[0] = DEV ? rho_m : rho;
