@@ -14,7 +14,10 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
-BUILD = os.path.join(HERE, "_build")
+# MGLC_BOUNDS_CHECK=1: the diagnostic build whose step kernels check every
+# element index (counted, access skipped), in a directory of its own
+CHECKED = os.environ.get("MGLC_BOUNDS_CHECK") == "1"
+BUILD = os.path.join(HERE, "_build_checked" if CHECKED else "_build")
 LIB = os.path.join(BUILD, "libmglc_gb300.so")
 ROOF_LIB = os.path.join(BUILD, "libmglc_roof.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -22,7 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # rates, sums) round the same on x86-64 and aarch64 hosts
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-fno-strict-aliasing", "-Xcompiler", "-ffp-contract=off",
-              "-I" + os.path.join(HERE, "..", "include")]
+              "-I" + os.path.join(HERE, "..", "include")] + (["-DMGLC_BOUNDS_CHECK"] if CHECKED else [])
 
 
 def nvcc() -> str:

@@ -10,7 +10,9 @@ import ctypes
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "libmglc_gb300.so")
+# MGLC_BOUNDS_CHECK=1 selects the bounds-checked diagnostic build (mglc_gb300/build.py)
+LIB_PATH = os.path.join(HERE, "_build_checked" if os.environ.get("MGLC_BOUNDS_CHECK") == "1"
+                        else "_build", "libmglc_gb300.so")
 
 MGLC_OK = 0
 ERRORS = {1: "MGLC_ERR_INVALID", 2: "MGLC_ERR_CUDA", 3: "MGLC_ERR_NOMEM", 4: "MGLC_ERR_STATE",

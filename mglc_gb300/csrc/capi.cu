@@ -1105,3 +1105,15 @@ int mglc_get_mask(mglc_ctx* c, int* owner) {
 }
 
 }  // extern "C"
+
+#ifdef MGLC_BOUNDS_CHECK
+// Bounds-checked builds only (no counterpart in the reference, not declared in
+// mglc.h): out-of-range element indices counted by the step kernels of every
+// translation unit since the library loaded on the current device.
+extern "C" unsigned long long mglc_oob_hits_k_step();
+extern "C" unsigned long long mglc_oob_hits_k_step_aa();
+extern "C" unsigned long long mglc_oob_hits_k_serve();
+extern "C" unsigned long long mglc_debug_bounds_hits() {
+    return mglc_oob_hits_k_step() + mglc_oob_hits_k_step_aa() + mglc_oob_hits_k_serve();
+}
+#endif

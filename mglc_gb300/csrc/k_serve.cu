@@ -273,3 +273,5 @@ cudaError_t launch_serve_fields(int form, const ServeSolve& s, float* out, cudaS
 }
 
 }  // namespace mglc
+
+MGLC_OOB_READER(mglc_oob_hits_k_serve)

@@ -223,3 +223,5 @@ cudaError_t launch_thermal_step(int form, bool first, const void* fin, void* fou
 }
 
 }  // namespace mglc
+
+MGLC_OOB_READER(mglc_oob_hits_k_step)

@@ -85,8 +85,11 @@ __global__ void __launch_bounds__(128) k_aa_swap(S* f, int nx, int ny, int nz, I
         if (opp19(q) < q) continue;
         const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
         if ((bm & leave_bits(-dx, -dy, -dz)) != 0) continue;
-        S* a = f + ((IDX)q * P + cell);
-        S* b = f + ((IDX)opp19(q) * P + cell - (IDX)(dx + dy * (int)sy) - (IDX)dz * sz);
+        const IDX ia = (IDX)q * P + cell;
+        const IDX ib = (IDX)opp19(q) * P + cell - (IDX)(dx + dy * (int)sy) - (IDX)dz * sz;
+        if (oob(ia, (IDX)Q * P) || oob(ib, (IDX)Q * P)) continue;
+        S* a = f + ia;
+        S* b = f + ib;
         const S t = *a;
         *a = *b;
         *b = t;
@@ -284,3 +287,5 @@ cudaError_t launch_aa_swap(int form, const Geom& g, void* f, void* gt, cudaStrea
 }
 
 }  // namespace mglc
+
+MGLC_OOB_READER(mglc_oob_hits_k_step_aa)

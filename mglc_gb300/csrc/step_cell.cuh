@@ -111,6 +111,45 @@ struct St<__nv_bfloat16> {
     __device__ static void st(__nv_bfloat16* p, C v, float sc) { *p = __float2bfloat16_rn(v * sc); }
 };
 
+// ----------------------------------------------------- bounds checking --
+// Built with MGLC_BOUNDS_CHECK (mglc_gb300/build.py, environment variable of
+// the same name), every global access of the cell bodies below checks its
+// element index against its array's extent; an index outside is counted
+// (per translation unit, read by the host through mglc_debug_bounds_hits)
+// and the access is skipped: a diagnostic build that cannot fault on a bad
+// index.  Without the macro the checks compile to nothing.
+#ifdef MGLC_BOUNDS_CHECK
+static __device__ unsigned long long g_oob_hits;
+template <typename IDX>
+__device__ __forceinline__ bool oob(IDX idx, IDX limit) {
+    if ((long long)idx < 0 || idx >= limit) {
+        atomicAdd(&g_oob_hits, 1ull);
+        return true;
+    }
+    return false;
+}
+#define MGLC_OOB_READER(NAME)                                                  \
+    extern "C" unsigned long long NAME() {                                     \
+        unsigned long long h = 0;                                              \
+        if (cudaMemcpyFromSymbol(&h, mglc::g_oob_hits, sizeof h) != cudaSuccess) {\
+            cudaGetLastError();                                                \
+            return ~0ull;                                                      \
+        }                                                                      \
+        return h;                                                              \
+    }
+#else
+template <typename IDX>
+__device__ __forceinline__ bool oob(IDX, IDX) {
+    return false;
+}
+#define MGLC_OOB_READER(NAME)
+#endif
+// checked store p[idx] = v (skipped when idx is outside [0, limit))
+template <typename T, typename V, typename IDX>
+__device__ __forceinline__ void st_chk(T* p, IDX idx, IDX limit, V v) {
+    if (!oob(idx, limit)) p[idx] = v;
+}
+
 // Reciprocal of the density (rho is within a few percent of 1 in every
 // cavity flow).  FP32: the hardware reciprocal.  FP64: Newton-Raphson
 // refinement r <- r + r(1 - x r) of a single-precision seed; two steps take
@@ -269,20 +308,21 @@ __device__ __forceinline__ void lid_cell_from(int i, int j, int k, const S (&raw
     const unsigned bm = face_mask(i, j, k, nx, ny, nz);
     unsigned w[NPAIR19];
     if constexpr (SR) sr_pack19<S>(f, (unsigned)cell, seed, w);
-    auto put = [&](S* p, int q) {
-        if constexpr (SR) St<S>::st_bits(p, sr_half(w, q));
-        else St<S>::st_s(p, f[q]);
+    auto put = [&](IDX idx, int q) {
+        if (oob(idx, (IDX)Q19 * P)) return;
+        if constexpr (SR) St<S>::st_bits(fout + idx, sr_half(w, q));
+        else St<S>::st_s(fout + idx, f[q]);
     };
     if (SWAP_STORE) {  // in-place even step: own cell, slot opp(q)
 #pragma unroll
-        for (int q = 0; q < Q19; q++) put(fout + ((IDX)opp19(q) * P + cell), q);
+        for (int q = 0; q < Q19; q++) put((IDX)opp19(q) * P + cell, q);
         return;
     }
     if (bm == 0) {  // interior cell: every population streams
 #pragma unroll
         for (int q = 0; q < Q19; q++) {
             const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
-            put(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), q);
+            put((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz, q);
         }
         return;
     }
@@ -290,9 +330,9 @@ __device__ __forceinline__ void lid_cell_from(int i, int j, int k, const S (&raw
     for (int q = 0; q < Q19; q++) {
         const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
         if ((bm & leave_bits(dx, dy, dz)) == 0)
-            put(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), q);
+            put((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz, q);
         else
-            put(fout + ((IDX)opp19(q) * P + cell), q);
+            put((IDX)opp19(q) * P + cell, q);
     }
 }
 
@@ -301,7 +341,10 @@ __device__ __forceinline__ void lid_load(int i, int j, int k, const S* __restric
                                          int ny, IDX P, S (&raw)[Q19]) {
     const IDX cell = (IDX)i + (IDX)nx * ((IDX)j + (IDX)ny * (IDX)k);
 #pragma unroll
-    for (int q = 0; q < Q19; q++) raw[q] = St<S>::raw(fin + ((IDX)q * P + cell));
+    for (int q = 0; q < Q19; q++) {
+        const IDX idx = (IDX)q * P + cell;
+        raw[q] = oob(idx, (IDX)Q19 * P) ? S() : St<S>::raw(fin + idx);
+    }
 }
 
 // in-place pattern loads (plain loads: the buffer is written by the same kernel).
@@ -311,9 +354,10 @@ template <typename S, typename IDX, bool ODD>
 __device__ __forceinline__ void lid_load_aa(int i, int j, int k, const S* f, int nx, int ny,
                                             int nz, IDX P, S (&raw)[Q19]) {
     const IDX cell = (IDX)i + (IDX)nx * ((IDX)j + (IDX)ny * (IDX)k);
+    auto ldaa = [&](IDX idx) -> S { return oob(idx, (IDX)Q19 * P) ? S() : St<S>::raw_rw(f + idx); };
     if (!ODD) {
 #pragma unroll
-        for (int q = 0; q < Q19; q++) raw[q] = St<S>::raw_rw(f + ((IDX)q * P + cell));
+        for (int q = 0; q < Q19; q++) raw[q] = ldaa((IDX)q * P + cell);
         return;
     }
     const IDX sy = (IDX)nx, sz = (IDX)nx * (IDX)ny;
@@ -322,8 +366,8 @@ __device__ __forceinline__ void lid_load_aa(int i, int j, int k, const S* f, int
 #pragma unroll
         for (int q = 0; q < Q19; q++) {
             const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
-            raw[q] = St<S>::raw_rw(f + ((IDX)opp19(q) * P + cell - (IDX)(dx + dy * (int)sy) -
-                                        (IDX)dz * sz));
+            raw[q] = ldaa((IDX)opp19(q) * P + cell - (IDX)(dx + dy * (int)sy) -
+                                        (IDX)dz * sz);
         }
         return;
     }
@@ -331,10 +375,10 @@ __device__ __forceinline__ void lid_load_aa(int i, int j, int k, const S* f, int
     for (int q = 0; q < Q19; q++) {
         const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
         if ((bm & leave_bits(-dx, -dy, -dz)) != 0)
-            raw[q] = St<S>::raw_rw(f + ((IDX)q * P + cell));
+            raw[q] = ldaa((IDX)q * P + cell);
         else
-            raw[q] = St<S>::raw_rw(f + ((IDX)opp19(q) * P + cell - (IDX)(dx + dy * (int)sy) -
-                                        (IDX)dz * sz));
+            raw[q] = ldaa((IDX)opp19(q) * P + cell - (IDX)(dx + dy * (int)sy) -
+                                        (IDX)dz * sz);
     }
 }
 
@@ -383,7 +427,7 @@ __device__ __forceinline__ void lid_cell_fx(int i, int j, int k, const double* f
         double raw[Q19];
         if (AAM == 0) {
 #pragma unroll
-            for (int q = 0; q < Q19; q++) raw[q] = __ldg(fin + ((IDX)q * P + cell));
+            for (int q = 0; q < Q19; q++) raw[q] = oob((IDX)q * P + cell, (IDX)Q19 * P) ? 0.0 : __ldg(fin + ((IDX)q * P + cell));
         } else {
             lid_load_aa<double, IDX, AAM == 2>(i, j, k, fin, nx, ny, nz, P, raw);
         }
@@ -425,14 +469,14 @@ __device__ __forceinline__ void lid_cell_fx(int i, int j, int k, const double* f
     const unsigned bm = face_mask(i, j, k, nx, ny, nz);
     if (AAM == 1) {  // in-place even step: own cell, slot opp(q) (lid term already in o)
 #pragma unroll
-        for (int q = 0; q < Q19; q++) fout[(IDX)opp19(q) * P + cell] = o[q];
+        for (int q = 0; q < Q19; q++) st_chk(fout, (IDX)opp19(q) * P + cell, (IDX)Q19 * P, o[q]);
         return;
     }
     if (bm == 0) {
 #pragma unroll
         for (int q = 0; q < Q19; q++) {
             const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
-            fout[(IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz] = o[q];
+            st_chk(fout, (IDX)((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), (IDX)Q19 * P, o[q]);
         }
         return;
     }
@@ -440,9 +484,9 @@ __device__ __forceinline__ void lid_cell_fx(int i, int j, int k, const double* f
     for (int q = 0; q < Q19; q++) {
         const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
         if ((bm & leave_bits(dx, dy, dz)) == 0)
-            fout[(IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz] = o[q];
+            st_chk(fout, (IDX)((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), (IDX)Q19 * P, o[q]);
         else
-            fout[(IDX)opp19(q) * P + cell] = o[q];
+            st_chk(fout, (IDX)((IDX)opp19(q) * P + cell), (IDX)Q19 * P, o[q]);
     }
 }
 
@@ -490,10 +534,10 @@ __device__ __forceinline__ void thermal_cell_from(
         // u^n = (sum f e + F^n/2)/rho^n with the force carried from the previous step
         C fxp = C(0), fyp = C(0);
         if (ROT) {
-            fxp = F[cell];
-            fyp = F[P + cell];
+            fxp = oob(P + cell, (IDX)3 * P) ? C(0) : F[cell];
+            fyp = oob(P + cell, (IDX)3 * P) ? C(0) : F[P + cell];
         }
-        const C fzp = F[fz_off + cell];
+        const C fzp = oob(fz_off + cell, fz_off + P) ? C(0) : F[fz_off + cell];
         ux = (jx + C(0.5) * fxp) * inv;
         uy = (jy + C(0.5) * fyp) * inv;
         uz = (jz + C(0.5) * fzp) * inv;
@@ -504,11 +548,13 @@ __device__ __forceinline__ void thermal_cell_from(
     if (ROT) {
         fx = C(-2) * rho * uy * K.omega_rot;
         fy = C(2) * rho * ux * K.omega_rot;
-        F[cell] = fx;
-        F[P + cell] = fy;
+        if (!oob(P + cell, (IDX)3 * P)) {
+            F[cell] = fx;
+            F[P + cell] = fy;
+        }
     }
     const C fz = rho * K.gbeta * (temp - K.t_ref);
-    F[fz_off + cell] = fz;
+    if (!oob(fz_off + cell, fz_off + P)) F[fz_off + cell] = fz;
     if (St<S>::SCALED)
         mrt_collide<C, true, false>(f, rho_m, rho * sc, ux, uy, uz, fx * sc, fy * sc, fz * sc, K.c);
     else
@@ -519,13 +565,14 @@ __device__ __forceinline__ void thermal_cell_from(
     const unsigned bm = face_mask(i, j, k, nx, ny, nz);
     unsigned w[NPAIR19];
     if constexpr (SR) sr_pack19<S>(f, (unsigned)cell, seed, w);
-    auto put = [&](S* p, int q) {
-        if constexpr (SR) St<S>::st_bits(p, sr_half(w, q));
-        else St<S>::st_s(p, f[q]);
+    auto put = [&](IDX idx, int q) {
+        if (oob(idx, (IDX)Q19 * P)) return;
+        if constexpr (SR) St<S>::st_bits(fout + idx, sr_half(w, q));
+        else St<S>::st_s(fout + idx, f[q]);
     };
     if (SWAP_STORE) {  // in-place even step: own cell, slot opp(q)
 #pragma unroll
-        for (int q = 0; q < Q19; q++) put(fout + ((IDX)opp19(q) * P + cell), q);
+        for (int q = 0; q < Q19; q++) put((IDX)opp19(q) * P + cell, q);
 #pragma unroll
         for (int q = 0; q < Q7; q++) {
             const int dy = ey19(q), dz = ez19(q);
@@ -534,7 +581,7 @@ __device__ __forceinline__ void thermal_cell_from(
                 if (dy != 0 && K.bc_y) val = -val + (dy < 0 ? K.chot : K.ccold);
                 if (dz != 0 && K.bc_z) val = -val + (dz < 0 ? K.chot : K.ccold);
             }
-            gout[(IDX)opp19(q) * P + cell] = val;
+            st_chk(gout, (IDX)((IDX)opp19(q) * P + cell), (IDX)Q7 * P, val);
         }
         return;
     }
@@ -542,12 +589,12 @@ __device__ __forceinline__ void thermal_cell_from(
 #pragma unroll
         for (int q = 0; q < Q19; q++) {
             const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
-            put(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), q);
+            put((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz, q);
         }
 #pragma unroll
         for (int q = 0; q < Q7; q++) {
             const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
-            gout[(IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz] = g[q];
+            st_chk(gout, (IDX)((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), (IDX)Q7 * P, g[q]);
         }
         return;
     }
@@ -555,9 +602,9 @@ __device__ __forceinline__ void thermal_cell_from(
     for (int q = 0; q < Q19; q++) {
         const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
         if ((bm & leave_bits(dx, dy, dz)) == 0)
-            put(fout + ((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), q);
+            put((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz, q);
         else
-            put(fout + ((IDX)opp19(q) * P + cell), q);
+            put((IDX)opp19(q) * P + cell, q);
     }
     // D3Q7: adiabatic walls reflect, constant-T walls anti-bounce-back
     // g_in = -g_out + (6+paraA)/21 * T_wall (bouyancy3d_mpi.F90:1101-1210)
@@ -565,12 +612,12 @@ __device__ __forceinline__ void thermal_cell_from(
     for (int q = 0; q < Q7; q++) {
         const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
         if ((bm & leave_bits(dx, dy, dz)) == 0) {
-            gout[(IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz] = g[q];
+            st_chk(gout, (IDX)((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), (IDX)Q7 * P, g[q]);
         } else {
             C val = g[q];
             if (dy != 0 && K.bc_y) val = -val + (dy < 0 ? K.chot : K.ccold);
             if (dz != 0 && K.bc_z) val = -val + (dz < 0 ? K.chot : K.ccold);
-            gout[(IDX)opp19(q) * P + cell] = val;
+            st_chk(gout, (IDX)((IDX)opp19(q) * P + cell), (IDX)Q7 * P, val);
         }
     }
 }
@@ -587,9 +634,10 @@ __device__ __forceinline__ void thermal_cell(
     const IDX cell = (IDX)i + (IDX)K.nx * ((IDX)j + (IDX)K.ny * (IDX)k);
     C f[Q19], g[Q7];
 #pragma unroll
-    for (int q = 0; q < Q19; q++) f[q] = St<S>::cvt_s(St<S>::raw(fin + ((IDX)q * P + cell)));
+    for (int q = 0; q < Q19; q++)
+        f[q] = St<S>::cvt_s(oob((IDX)q * P + cell, (IDX)Q19 * P) ? S() : St<S>::raw(fin + ((IDX)q * P + cell)));
 #pragma unroll
-    for (int q = 0; q < Q7; q++) g[q] = gin[(IDX)q * P + cell];
+    for (int q = 0; q < Q7; q++) g[q] = oob((IDX)q * P + cell, (IDX)Q7 * P) ? C(0) : gin[(IDX)q * P + cell];
     thermal_cell_from<S, FIRST, ROT, IDX, SR>(i, j, k, f, g, fout, gout, F, K, P, mrho, mu, mv,
                                               mw, mT, fz_off, seed);
 }
@@ -614,11 +662,12 @@ __device__ __forceinline__ void thermal_load_aa(int i, int j, int k, const S* f,
     };
     S raw[Q19];
 #pragma unroll
-    for (int q = 0; q < Q19; q++) raw[q] = St<S>::raw_rw(f + src(q));
+    for (int q = 0; q < Q19; q++) raw[q] = oob(src(q), (IDX)Q19 * P) ? S() : St<S>::raw_rw(f + src(q));
     // g through L2 only (ld.global.cg, coherent): measured 1.3x faster for the
     // stochastically rounded 16-bit form, neutral for the others
 #pragma unroll
-    for (int q = 0; q < Q7; q++) gv[q] = __ldcg(g + src(q));
+    for (int q = 0; q < Q7; q++)
+        gv[q] = oob(src(q), (IDX)Q7 * P) ? typename St<S>::C(0) : __ldcg(g + src(q));
 #pragma unroll
     for (int q = 0; q < Q19; q++) fv[q] = St<S>::cvt_s(raw[q]);  // in units of the storage scale
 }
@@ -653,9 +702,9 @@ __device__ __forceinline__ void thermal_cell_fx(
         double rf[Q19], rg[Q7];
         if (AAM == 0) {
 #pragma unroll
-            for (int q = 0; q < Q19; q++) rf[q] = __ldg(fin + ((IDX)q * P + cell));
+            for (int q = 0; q < Q19; q++) rf[q] = oob((IDX)q * P + cell, (IDX)Q19 * P) ? 0.0 : __ldg(fin + ((IDX)q * P + cell));
 #pragma unroll
-            for (int q = 0; q < Q7; q++) rg[q] = __ldg(gin + ((IDX)q * P + cell));
+            for (int q = 0; q < Q7; q++) rg[q] = oob((IDX)q * P + cell, (IDX)Q7 * P) ? 0.0 : __ldg(gin + ((IDX)q * P + cell));
         } else {
             const IDX sy = (IDX)nx, sz = (IDX)nx * (IDX)ny;
             const unsigned bm = face_mask(i, j, k, nx, ny, nz);
@@ -667,7 +716,7 @@ __device__ __forceinline__ void thermal_cell_fx(
 #pragma unroll
             for (int q = 0; q < Q19; q++) rf[q] = fin[src(q)];
 #pragma unroll
-            for (int q = 0; q < Q7; q++) rg[q] = __ldcg(gin + src(q));
+            for (int q = 0; q < Q7; q++) rg[q] = oob(src(q), (IDX)Q7 * P) ? 0.0 : __ldcg(gin + src(q));
         }
 #pragma unroll
         for (int q = 0; q < Q19; q++) {
@@ -691,10 +740,10 @@ __device__ __forceinline__ void thermal_cell_fx(
         // u = (sum f e + F/2) / rho with the force carried from the previous step
         ll fxp = 0, fyp = 0;
         if (ROT) {
-            fxp = d2q(F[cell]);
-            fyp = d2q(F[P + cell]);
+            fxp = d2q(oob(P + cell, (IDX)3 * P) ? 0.0 : F[cell]);
+            fyp = d2q(oob(P + cell, (IDX)3 * P) ? 0.0 : F[P + cell]);
         }
-        const ll fzp = d2q(F[2 * P + cell]);
+        const ll fzp = d2q(oob((IDX)2 * P + cell, (IDX)3 * P) ? 0.0 : F[2 * P + cell]);
         const ll s1 = f[1] + f[2], s2 = f[3] + f[4], s3 = f[5] + f[6];
         const ll s4 = f[7] + f[10], s5 = f[9] + f[8], s6 = f[11] + f[14], s7 = f[13] + f[12];
         const ll s8 = f[15] + f[18], s9 = f[17] + f[16];
@@ -715,11 +764,13 @@ __device__ __forceinline__ void thermal_cell_fx(
     if (ROT) {
         fx = -qmul(qmul(rho, uy), K.t.omega2);
         fy = qmul(qmul(rho, ux), K.t.omega2);
-        F[cell] = q2d(fx);
-        F[P + cell] = q2d(fy);
+        if (!oob(P + cell, (IDX)3 * P)) {
+            F[cell] = q2d(fx);
+            F[P + cell] = q2d(fy);
+        }
     }
     const ll fz = qmul(rho, qmulc(temp - K.t.t_ref, K.t.gbeta));
-    F[2 * P + cell] = q2d(fz);
+    if (!oob((IDX)2 * P + cell, (IDX)3 * P)) F[2 * P + cell] = q2d(fz);
     bad |= !mrt_collide_fx_forced(f, rho, ux, uy, uz, rux, ruy, ruz, fx, fy, fz, K.t);
     mrt_collide_t_fx(g, temp, ux, uy, uz, K.t);
 
@@ -731,11 +782,11 @@ __device__ __forceinline__ void thermal_cell_fx(
         const int dx = ex19(q), dy = ey19(q), dz = ez19(q);
         const double o = bad ? nan : (q < FX_CVT_OUT ? q2d_cvt(f[q]) : q2d(f[q]));
         if (AAM == 1)  // in-place even step: own cell, slot opp(q)
-            fout[(IDX)opp19(q) * P + cell] = o;
+            st_chk(fout, (IDX)((IDX)opp19(q) * P + cell), (IDX)Q19 * P, o);
         else if ((bm & leave_bits(dx, dy, dz)) == 0)
-            fout[(IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz] = o;
+            st_chk(fout, (IDX)((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), (IDX)Q19 * P, o);
         else
-            fout[(IDX)opp19(q) * P + cell] = o;
+            st_chk(fout, (IDX)((IDX)opp19(q) * P + cell), (IDX)Q19 * P, o);
     }
     // D3Q7: adiabatic walls reflect, constant-T walls anti-bounce-back
 #pragma unroll
@@ -744,14 +795,14 @@ __device__ __forceinline__ void thermal_cell_fx(
         if ((bm & leave_bits(dx, dy, dz)) == 0) {
             const double o = bad ? nan : (q < FXT_CVT_G ? q2d_cvt(g[q]) : q2d(g[q]));
             if (AAM == 1)
-                gout[(IDX)opp19(q) * P + cell] = o;
+                st_chk(gout, (IDX)((IDX)opp19(q) * P + cell), (IDX)Q7 * P, o);
             else
-                gout[(IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz] = o;
+                st_chk(gout, (IDX)((IDX)q * P + cell + (IDX)(dx + dy * (int)sy) + (IDX)dz * sz), (IDX)Q7 * P, o);
         } else {
             ll val = g[q];
             if (dy != 0 && K.bc_y) val = -val + (dy < 0 ? K.t.chot : K.t.ccold);
             if (dz != 0 && K.bc_z) val = -val + (dz < 0 ? K.t.chot : K.t.ccold);
-            gout[(IDX)opp19(q) * P + cell] = bad ? nan : (q < FXT_CVT_G ? q2d_cvt(val) : q2d(val));
+            st_chk(gout, (IDX)((IDX)opp19(q) * P + cell), (IDX)Q7 * P, bad ? nan : (q < FXT_CVT_G ? q2d_cvt(val) : q2d(val)));
         }
     }
 }
