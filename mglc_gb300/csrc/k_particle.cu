@@ -603,6 +603,31 @@ __global__ void __launch_bounds__(PB) k_plinks(S* __restrict__ f, PartParams p, 
     }
 }
 
+// The node t = bi + bw (bj + bw bk) of a particle's box, walked by one thread
+// in strides of PB without divisions: PB's digits in base bw are added with
+// carries (the same nodes, in the same order, as t % bw, (t / bw) % bw, ...).
+struct BoxWalk {
+    int bi, bj, bk, ai, aj, ak, bw;
+    __device__ BoxWalk(long long t0, int bw_) : bw(bw_) {
+        const long long b2 = (long long)bw_ * bw_;
+        bi = (int)(t0 % bw_);
+        bj = (int)((t0 / bw_) % bw_);
+        bk = (int)(t0 / b2);
+        ai = PB % bw_;
+        aj = (int)(((long long)PB / bw_) % bw_);
+        ak = (int)((long long)PB / b2);
+    }
+    __device__ void next() {
+        bi += ai;
+        int carry = 0;
+        if (bi >= bw) { bi -= bw; carry = 1; }
+        bj += aj + carry;
+        carry = 0;
+        if (bj >= bw) { bj -= bw; carry = 1; }
+        bk += ak + carry;
+    }
+};
+
 // ----------------------------------------------------------- update --------
 // particle_force.F90:96-190 in 3-D: one warp per particle; the lanes split the
 // pair loop and a fixed shuffle tree adds their spring forces.
@@ -716,8 +741,9 @@ __global__ void __launch_bounds__(PB) k_pmark(int* owner, const double* xc, Part
     const int ci = (int)floor(X[0]) - 1, cj = (int)floor(X[1]) - 1, ck = (int)floor(X[2]) - 1;
     const int bw = 2 * h + 2;
     const long long nbox = (long long)bw * bw * bw;
-    for (long long t = threadIdx.x; t < nbox; t += PB) {
-        const int bi = (int)(t % bw), bj = (int)((t / bw) % bw), bk = (int)(t / ((long long)bw * bw));
+    BoxWalk bw_it(threadIdx.x, bw);
+    for (long long t = threadIdx.x; t < nbox; t += PB, bw_it.next()) {
+        const int bi = bw_it.bi, bj = bw_it.bj, bk = bw_it.bk;
         int i = ci - h + bi;
         const int j = cj - h + bj, k = ck - h + bk;
         if (j < 0 || j >= p.ny || k < 0 || k >= p.nz) continue;
@@ -749,8 +775,9 @@ __global__ void __launch_bounds__(PB) k_pprep(const S* __restrict__ f, PartParam
         const int ci = (int)floor(X[0]) - 1, cj = (int)floor(X[1]) - 1, ck = (int)floor(X[2]) - 1;
         const int bw = 2 * h + 2;
         const long long nbox = (long long)bw * bw * bw;
-        for (long long t = threadIdx.x; t < nbox; t += PB) {
-            const int bi = (int)(t % bw), bj = (int)((t / bw) % bw), bk = (int)(t / ((long long)bw * bw));
+        BoxWalk bw_it(threadIdx.x, bw);
+        for (long long t = threadIdx.x; t < nbox; t += PB, bw_it.next()) {
+            const int bi = bw_it.bi, bj = bw_it.bj, bk = bw_it.bk;
             int i = ci - h + bi;
             const int j = cj - h + bj, k = ck - h + bk;
             if (j < 0 || j >= p.ny || k < 0 || k >= p.nz) continue;
@@ -865,8 +892,9 @@ __global__ void __launch_bounds__(PB) k_prefill(S* __restrict__ f, PartParams p,
     const int ci = (int)floor(Xo[0]) - 1, cj = (int)floor(Xo[1]) - 1, ck = (int)floor(Xo[2]) - 1;
     const int bw = 2 * h + 2;
     const long long nbox = (long long)bw * bw * bw;
-    for (long long t = threadIdx.x; t < nbox; t += PB) {
-        const int bi = (int)(t % bw), bj = (int)((t / bw) % bw), bk = (int)(t / ((long long)bw * bw));
+    BoxWalk bw_it(threadIdx.x, bw);
+    for (long long t = threadIdx.x; t < nbox; t += PB, bw_it.next()) {
+        const int bi = bw_it.bi, bj = bw_it.bj, bk = bw_it.bk;
         int i = ci - h + bi;
         const int j = cj - h + bj, k = ck - h + bk;
         if (j < 0 || j >= p.ny || k < 0 || k >= p.nz) continue;
