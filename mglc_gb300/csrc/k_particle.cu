@@ -389,7 +389,8 @@ __global__ void __launch_bounds__(PB) k_plinks(S* __restrict__ f, PartParams p, 
     const int bw = 2 * h + 2;
     const int kz0 = slab * bw / NSLAB, kz1 = (slab + 1) * bw / NSLAB;
     const int nbox = bw * bw * (kz1 - kz0);
-    const double reach2 = (R + 1.8) * (R + 1.8);  // |x - X| <= R + sqrt(2) for a link
+    const float reach2f = (float)((R + 1.8) * (R + 1.8));  // |x - X| <= R + sqrt(2) for a link
+    const float Xf0 = (float)X0, Xf1 = (float)X1, Xf2 = (float)X2, Lf = (float)p.nx;
     int nf[3] = {0, 0, 0};  // sum m e
     int nt[3] = {0, 0, 0};  // sum m (n x e)
     L av[7] = {L(0), L(0), L(0), L(0), L(0), L(0), L(0)};  // variable force, torque, mass change
@@ -430,9 +431,15 @@ __global__ void __launch_bounds__(PB) k_plinks(S* __restrict__ f, PartParams p, 
             const int j = cj - h + bj, k = ck - h + bk;
             bool ok = !(j < 0 || j >= ny || k < 0 || k >= nz);
             if (ok) {
-                const double ox = dxp((double)(i + 1), X0, p), oy = (double)(j + 1) - X1,
-                             oz = (double)(k + 1) - X2;
-                ok = ox * ox + oy * oy + oz * oz <= reach2;
+                // a filter only: every link node lies within R + sqrt(2) of the
+                // centre, well inside the R + 1.8 kept here, so FP32 suffices
+                float ox = (float)(i + 1) - Xf0;
+                if (p.periodic_x) {
+                    if (ox > 0.5f * Lf) ox -= Lf;
+                    else if (ox < -0.5f * Lf) ox += Lf;
+                }
+                const float oy = (float)(j + 1) - Xf1, oz = (float)(k + 1) - Xf2;
+                ok = ox * ox + oy * oy + oz * oz <= reach2f;
             }
             if (ok) {
                 if (p.periodic_x) i = wrapx(i, nx);
@@ -741,6 +748,8 @@ __global__ void __launch_bounds__(PB) k_pmark(int* owner, const double* xc, Part
     const int ci = (int)floor(X[0]) - 1, cj = (int)floor(X[1]) - 1, ck = (int)floor(X[2]) - 1;
     const int bw = 2 * h + 2;
     const long long nbox = (long long)bw * bw * bw;
+    const float Xf0 = (float)X[0], Xf1 = (float)X[1], Xf2 = (float)X[2], Lf = (float)p.nx;
+    const float Xmax = fmaxf(fabsf(Xf0), fmaxf(fabsf(Xf1), fabsf(Xf2))) + Lf;  // wrapped nodes too
     BoxWalk bw_it(threadIdx.x, bw);
     for (long long t = threadIdx.x; t < nbox; t += PB, bw_it.next()) {
         const int bi = bw_it.bi, bj = bw_it.bj, bk = bw_it.bk;
@@ -749,13 +758,20 @@ __global__ void __launch_bounds__(PB) k_pmark(int* owner, const double* xc, Part
         if (j < 0 || j >= p.ny || k < 0 || k >= p.nz) continue;
         if (p.periodic_x) i = wrapx(i, p.nx);
         else if (i < 0 || i >= p.nx) continue;
-        // FP32 decides far from the surface; nodes within 1e-3 R^2 of it use
-        // the IEEE-rounded FP64 test
-        const float fx = (float)dxp((double)(i + 1), X[0], p), fy = (float)((double)(j + 1) - X[1]),
-                    fz = (float)((double)(k + 1) - X[2]);
+        // FP32 decides far from the surface; nodes within tol of it use the
+        // IEEE-rounded FP64 test.  tol bounds the FP32 error of d2 (the centre
+        // rounded to FP32, then the differences, squares and sums) at least
+        // twice over, so wherever FP32 decides, its decision is the FP64 test's.
+        float fx = (float)(i + 1) - Xf0;
+        if (p.periodic_x) {
+            if (fx > 0.5f * Lf) fx -= Lf;
+            else if (fx < -0.5f * Lf) fx += Lf;
+        }
+        const float fy = (float)(j + 1) - Xf1, fz = (float)(k + 1) - Xf2;
         const float d2 = fx * fx + fy * fy + fz * fz, r2 = (float)(R * R);
+        const float tol = 1e-3f * r2 + 4e-6f * (float)(h + 1) * (Xmax + (float)(h + 1)) + 1e-6f * d2;
         bool in;
-        if (fabsf(d2 - r2) > 1e-3f * r2) in = d2 < r2;
+        if (fabsf(d2 - r2) > tol) in = d2 < r2;
         else in = inside((double)(i + 1), (double)(j + 1), (double)(k + 1), X, R, p);
         if (in) owner[i + (long long)p.nx * (j + (long long)p.ny * k)] = c;
     }
