@@ -1081,8 +1081,9 @@ static cudaError_t pstep_go(bool first, const void* fin, void* fout, const PartP
         } else {
             k_plinks<S, false><<<dim3(p.np, NSLAB), PB, 0, s>>>((S*)fout, p, d);
         }
-        k_pforce<<<(p.np + 7) / 8, 256, 0, s>>>(p, d);
-        k_pmove<<<(p.np + 127) / 128, 128, 0, s>>>(p, d);
+        // one warp per particle, one warp per block: the particles spread over the SMs
+        k_pforce<<<p.np, 32, 0, s>>>(p, d);
+        k_pmove<<<(p.np + 31) / 32, 32, 0, s>>>(p, d);
     }
     cudaError_t e = cudaMemsetAsync(d.owner_new, 0xFF, sizeof(int) * (size_t)p.nx * p.ny * p.nz, s);
     if (e != cudaSuccess) return e;
