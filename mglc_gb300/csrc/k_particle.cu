@@ -367,7 +367,8 @@ __device__ __forceinline__ bool node_avail(int i, int j, int k, const PartParams
 //   sum r x (2 e w rho0)  = rho0/18 * (sum m n x e - X x sum m e)
 // because r = o + q e gives r x e = o x e, and o = n - X with n the node's
 // (unwrapped) coordinates.  The variable parts use the population arithmetic
-// type; q (calQ2) is computed in FP64 in both forms.
+// type; q (calQ2) is computed in FP64 for the FP64 form and, from the FP64
+// |x - X|^2 - R^2, in FP32 for the FP32 form.
 // TILE: the owner ids of the slab's box plus a one-node halo are staged in
 // dynamic shared memory (walls and, without periodicity, the x faces as -2),
 // so the scan's 19 lookups per node stay on chip.
@@ -507,12 +508,25 @@ __global__ void __launch_bounds__(PB) k_plinks(S* __restrict__ f, PartParams p, 
             const double sx = ea > 0 ? ox : (ea < 0 ? -ox : 0.0);
             const double sy = eb > 0 ? oy : (eb < 0 ? -oy : 0.0);
             const double sz = ec > 0 ? oz : (ec < 0 ? -oz : 0.0);
-            const double cb = 2.0 * (sx + sy + sz);
             const double cc = ox * ox + oy * oy + oz * oz - R * R;
-            const double delta = cb * cb - (a <= 6 ? 4.0 : 8.0) * cc;
-            if (delta < 0) { atomicCAS(d.status, 0, PS_Q_RANGE); d.status[1] = c; continue; }
-            const double qd = (-cb - sqrt(delta)) * (a <= 6 ? 0.5 : 0.25);  // /(2 |e|^2), exact
-            if (qd > 1.0 || qd < 0.0) { atomicCAS(d.status, 0, PS_Q_RANGE); d.status[1] = c; continue; }
+            double qd;
+            if constexpr (sizeof(L) == 4) {
+                // FP32 form: |x - X|^2 - R^2 (the cancelling part) in FP64, the
+                // root in FP32; FP32 rounding may put a root on the node (q = 0)
+                // or the solid node (q = 1) a few ulps outside, which is clamped
+                const float cbf = 2.0f * (float)(sx + sy + sz);
+                const float delta = cbf * cbf - (a <= 6 ? 4.0f : 8.0f) * (float)cc;
+                if (delta < -1e-4f) { atomicCAS(d.status, 0, PS_Q_RANGE); d.status[1] = c; continue; }
+                const float qf = (-cbf - sqrtf(fmaxf(delta, 0.0f))) * (a <= 6 ? 0.5f : 0.25f);
+                if (qf > 1.0f + 1e-5f || qf < -1e-5f) { atomicCAS(d.status, 0, PS_Q_RANGE); d.status[1] = c; continue; }
+                qd = (double)fminf(fmaxf(qf, 0.0f), 1.0f);
+            } else {
+                const double cb = 2.0 * (sx + sy + sz);
+                const double delta = cb * cb - (a <= 6 ? 4.0 : 8.0) * cc;
+                if (delta < 0) { atomicCAS(d.status, 0, PS_Q_RANGE); d.status[1] = c; continue; }
+                qd = (-cb - sqrt(delta)) * (a <= 6 ? 0.5 : 0.25);  // /(2 |e|^2), exact
+                if (qd > 1.0 || qd < 0.0) { atomicCAS(d.status, 0, PS_Q_RANGE); d.status[1] = c; continue; }
+            }
             // constant parts (integers)
             const int n0 = iu + 1, n1 = j + 1, n2 = k + 1;
             nf[0] += m * ea;
