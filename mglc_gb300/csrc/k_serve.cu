@@ -99,16 +99,18 @@ __global__ void __launch_bounds__(256, THERMAL ? MGLC_SERVE_HEAT_MINB : MGLC_SER
                             i, j, k, raw, f, sv.K, sv.plane, nullptr, nullptr, nullptr, nullptr, seed);
                     }
                 } else {
-                    float fv[Q19], gv[Q7];
+                    float fv[Q19], gv[Q7], fp[3];
                     if (parity) {
-                        thermal_load_aa<S, unsigned, true>(i, j, k, f, sv.g[0], sv.K, sv.plane, fv, gv);
+                        thermal_load_aa<S, unsigned, true>(i, j, k, f, sv.g[0], sv.F, 0u, sv.K,
+                                                           sv.plane, fv, gv, fp);
                         thermal_cell_from<S, false, false, unsigned, SR, false>(
-                            i, j, k, fv, gv, f, sv.g[0], sv.F, sv.K, sv.plane, nullptr, nullptr,
+                            i, j, k, fv, gv, fp, f, sv.g[0], sv.F, sv.K, sv.plane, nullptr, nullptr,
                             nullptr, nullptr, nullptr, 0u, seed);
                     } else {
-                        thermal_load_aa<S, unsigned, false>(i, j, k, f, sv.g[0], sv.K, sv.plane, fv, gv);
+                        thermal_load_aa<S, unsigned, false>(i, j, k, f, sv.g[0], sv.F, 0u, sv.K,
+                                                            sv.plane, fv, gv, fp);
                         thermal_cell_from<S, false, false, unsigned, SR, true>(
-                            i, j, k, fv, gv, f, sv.g[0], sv.F, sv.K, sv.plane, nullptr, nullptr,
+                            i, j, k, fv, gv, fp, f, sv.g[0], sv.F, sv.K, sv.plane, nullptr, nullptr,
                             nullptr, nullptr, nullptr, 0u, seed);
                     }
                 }

@@ -61,10 +61,10 @@ __global__ void __launch_bounds__(128)
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= K.nx) return;
     const int j = blockIdx.y, k = blockIdx.z;
-    C fv[Q19], gv[Q7];  // every load is issued before the first store
-    thermal_load_aa<S, IDX, ODD>(i, j, k, f, g, K, P, fv, gv);
-    thermal_cell_from<S, FIRST, ROT, IDX, SR, !ODD>(i, j, k, fv, gv, f, g, F, K, P, mrho, mu, mv,
-                                                    mw, mT, (IDX)2 * P, K.seed);
+    C fv[Q19], gv[Q7], fp[3];  // every load is issued before the first store
+    thermal_load_aa<S, IDX, ODD, ROT>(i, j, k, f, g, F, (IDX)2 * P, K, P, fv, gv, fp);
+    thermal_cell_from<S, FIRST, ROT, IDX, SR, !ODD>(i, j, k, fv, gv, fp, f, g, F, K, P, mrho, mu,
+                                                    mv, mw, mT, (IDX)2 * P, K.seed);
 }
 
 // Pairwise exchange (q, x) <-> (opp(q), x - e_q) for the directions with

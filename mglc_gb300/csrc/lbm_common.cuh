@@ -45,14 +45,19 @@ __host__ __device__ constexpr double w19(int a) {
 
 // Relaxation coefficients folded with 1/|M_k|^2 (host-computed in FP64).
 // c_k = s_k / |M_k|^2, h_k = (1 - s_k/2) / |M_k|^2.
+// snu, le = snu/2, lo = sq/2: the two rates of the pair form;
+// ke2 = (1 - le)/le and ko = (1 - lo)/(2 lo): its force terms.
 template <typename T>
 struct MrtCoef {
     T c1, c2, c4, c9, c10, c11, c12, c13, c16;
     T h1, h2, h3, h4, h9, h10, h11, h12, h13;
+    T snu, le, lo, ke2, ko;
 };
 
 inline MrtCoef<double> make_mrt_coef(double snu, double sq) {
     MrtCoef<double> c;
+    c.snu = snu; c.le = 0.5 * snu; c.lo = 0.5 * sq;
+    c.ke2 = (1.0 - c.le) / c.le; c.ko = (1.0 - c.lo) / (2.0 * c.lo);
     c.c1 = snu / 2394.0; c.c2 = snu / 252.0; c.c4 = sq / 40.0;
     c.c9 = snu / 36.0; c.c10 = snu / 72.0; c.c11 = snu / 12.0; c.c12 = snu / 24.0;
     c.c13 = snu / 4.0; c.c16 = sq / 8.0;
@@ -69,6 +74,7 @@ inline MrtCoef<T> cast_coef(const MrtCoef<double>& d) {
     c.c11 = (T)d.c11; c.c12 = (T)d.c12; c.c13 = (T)d.c13; c.c16 = (T)d.c16;
     c.h1 = (T)d.h1; c.h2 = (T)d.h2; c.h3 = (T)d.h3; c.h4 = (T)d.h4; c.h9 = (T)d.h9;
     c.h10 = (T)d.h10; c.h11 = (T)d.h11; c.h12 = (T)d.h12; c.h13 = (T)d.h13;
+    c.snu = (T)d.snu; c.le = (T)d.le; c.lo = (T)d.lo; c.ke2 = (T)d.ke2; c.ko = (T)d.ko;
     return c;
 }
 
@@ -215,6 +221,166 @@ __device__ __forceinline__ void mrt_collide(T* f, T rho_m, T rho, T ux, T uy, T 
     // P9 (17,16)
     E = bz - r14; O = Y - Z + (r17 + r18);
     f[17] -= E + O; f[16] -= E - O;
+}
+
+// The lid-driven cavity's MRT collision (collision.f90:15-202) in its pair
+// form.  The reference relaxes every even non-conserved moment (e, epsilon,
+// p_ww, pi_ww, p_xx-type, pi-type, p_xy, p_yz, p_xz) at Snu and every odd one
+// (q_x,y,z, m_x,y,z) at Sq (collision.f90:94-112), and its basis is orthogonal,
+// so M^-1 S (m - meq) = Snu [(f - feq)^+ - P_rho] + Sq [(f - feq)^- - P_j]:
+// the parts of f - feq that are even and odd under e -> -e, less their
+// projections on the conserved moments (s = 0 there), with feq = M^-1 meq.
+// That feq is the second-order polynomial equilibrium
+//     feq_i = w_i rho (1 + 3 e.u + 9/2 (e.u)^2 - 3/2 u.u)
+// plus M_12^T (meq12_lid - meq12) / |M_12|^2 for the lid quirk (meq(12)
+// without rho, collision.f90:85).  When rho and u come from the same
+// populations (every step but the first after initial or load) the
+// projections, P_rho = (sum f - rho)/19 and P_j = e.(j - rho u)/10, are at
+// rounding level and are left out; CONS adds them (dr = sum f - rho,
+// dj = j - rho u, in storage units) for the step that takes rho and u from
+// the macro arrays.  Per opposite pair (a, b = opp a), with t = f_a + f_b,
+// d = f_a - f_b, E = feq_a + feq_b (+ 2 P_rho) and O = feq_a - feq_b (+ 2 P_j):
+//     f_a' = f_a - Snu/2 (t - E) - Sq/2 (d - O)
+//     f_b' = f_b - Snu/2 (t - E) + Sq/2 (d - O)
+// About 150 operations per cell against the moment form's 215 (FP64, ncu);
+// results differ from the moment form by rounding (a few ulp).
+// Arguments as mrt_collide's (rho_m: the equilibrium's density less rho0,
+// rhos: its density, both in units of the storage scale; msc: the scale).
+template <typename T, bool CONS = false>
+__device__ __forceinline__ void trt_collide_lid(T* f, T rho_m, T rhos, T ux, T uy, T uz,
+                                                const MrtCoef<T>& c, T msc = T(1),
+                                                T dr = T(0), T djx = T(0), T djy = T(0),
+                                                T djz = T(0)) {
+    const T ux2 = ux * ux, uy2 = uy * uy, uz2 = uz * uz;
+    const T usq = ux2 + uy2 + uz2;
+    // feq_i = w_i (base + rhos (3 e.u + 9/2 (e.u)^2)), base = rho_m - 3/2 rhos u.u
+    const T base = rho_m + T(-1.5) * rhos * usq;
+    T ea = base * T(1.0 / 9.0);    // 2 w base, axis pairs (w = 1/18)
+    T ee = base * T(1.0 / 18.0);   // edge pairs (w = 1/36)
+    T e0 = base * T(1.0 / 3.0);    // feq_0
+    const T ka = rhos * T(0.5), ke = rhos * T(0.25);            // 9 w rhos
+    const T oa = rhos * T(1.0 / 3.0), oe = rhos * T(1.0 / 6.0);  // 6 w rhos
+    T gx = T(0), gy = T(0), gz = T(0);  // 2 P_j per unit of e (CONS)
+    if constexpr (CONS) {
+        const T d19 = dr * T(2.0 / 19.0);
+        ea = ea + d19;
+        ee = ee + d19;
+        e0 = e0 + T(0.5) * d19;
+        gx = djx * T(0.2);
+        gy = djy * T(0.2);
+        gz = djz * T(0.2);
+    }
+    // lid quirk: E gains 2 M_12,a D / 24, D = (rhos - msc)(uy^2 - uz^2) / 2;
+    // M_12 = -2 (y axis), +2 (z axis), +1 (xy edges), -1 (xz edges), 0 (yz)
+    const T q6 = (uy2 - uz2) * ((rhos - msc) * T(1.0 / 12.0));  // D / 6
+    const T q12 = q6 * T(0.5);                                    // D / 12
+    const T exy = ee + q12, exz = ee - q12;
+    const T le = c.le, lo = c.lo;
+    auto pair = [&](int a, int b, T E, T O) {
+        const T ne = (f[a] + f[b]) - E;
+        const T no = (f[a] - f[b]) - O;
+        const T fa = f[a] - lo * no - le * ne;
+        const T fb = f[b] + lo * no - le * ne;
+        f[a] = fa;
+        f[b] = fb;
+    };
+    f[0] = f[0] - c.snu * (f[0] - e0);
+    T v;
+    if constexpr (CONS) {
+        pair(1, 2, ea + ka * ux2, oa * ux + gx);
+        pair(3, 4, (ea + ka * uy2) - q6, oa * uy + gy);
+        pair(5, 6, (ea + ka * uz2) + q6, oa * uz + gz);
+        v = ux + uy; pair(7, 10, exy + ke * v * v, oe * v + (gx + gy));
+        v = ux - uy; pair(9, 8, exy + ke * v * v, oe * v + (gx - gy));
+        v = ux + uz; pair(11, 14, exz + ke * v * v, oe * v + (gx + gz));
+        v = ux - uz; pair(13, 12, exz + ke * v * v, oe * v + (gx - gz));
+        v = uy + uz; pair(15, 18, ee + ke * v * v, oe * v + (gy + gz));
+        v = uy - uz; pair(17, 16, ee + ke * v * v, oe * v + (gy - gz));
+    } else {
+        pair(1, 2, ea + ka * ux2, oa * ux);
+        pair(3, 4, (ea + ka * uy2) - q6, oa * uy);
+        pair(5, 6, (ea + ka * uz2) + q6, oa * uz);
+        v = ux + uy; pair(7, 10, exy + ke * v * v, oe * v);
+        v = ux - uy; pair(9, 8, exy + ke * v * v, oe * v);
+        v = ux + uz; pair(11, 14, exz + ke * v * v, oe * v);
+        v = ux - uz; pair(13, 12, exz + ke * v * v, oe * v);
+        v = uy + uz; pair(15, 18, ee + ke * v * v, oe * v);
+        v = uy - uz; pair(17, 16, ee + ke * v * v, oe * v);
+    }
+}
+
+// The heated cavity's forced MRT collision (bouyancy3d_mpi.F90:641-864) in
+// the same pair form.  Its rates are the lid operator's (even Snu, odd Sq,
+// :723-741), its equilibrium has no quirk, and its moment source is M F with
+// F_i = w_i (3 e.F + 9 (e.u)(e.F) - 3 u.F) (fSource, :747-765), relaxed by
+// 1 - s/2 and added in full to the conserved momentum.  The velocity of the
+// equilibrium is u = (j + Fp/2)/rho with the force Fp carried from the
+// previous step (:998-1002), so j - rho u = -Fp/2 is not zero;
+// working the three moment groups through gives, per pair,
+//     f_a' = f_a - Snu/2 (t - E) - Sq/2 (d - O),  f_b' likewise with +Sq/2,
+//     E = 2w (rho_m - 3/2 u.V) + 9w (e.u)(e.V),   V = rho u + (1 - le)/le F
+//     O = 6w e.W + e.(F - Fp)/10,                 W = rho u + (1 - lo)/(2 lo) F
+// (the equilibrium shifted by the relaxed source; the last term is what the
+// unrelaxed momentum source and the carried force leave in the odd part),
+// and f_0' = f_0 - Snu (f_0 - (rho_m - 3/2 u.V)/3).  About 130 operations
+// against the moment form's 230; the difference is rounding.  In general the
+// odd term is e.(2 (j - rho u) + F)/10, which the caller passes as dF; for
+// the first step after initial or load (rho, u from the macro arrays) CONS
+// also takes the density projection back out (dr = sum f - rho, as in
+// trt_collide_lid).
+// f, rho_m, rhos and the forces (F this step's, dF = F - Fp) in units of the
+// storage scale, u unscaled; ROT: F_x, F_y (rotation) are not zero.
+template <typename T, bool ROT, bool CONS = false>
+__device__ __forceinline__ void trt_collide_forced(T* f, T rho_m, T rhos, T ux, T uy, T uz, T fx,
+                                                   T fy, T fz, T dfx, T dfy, T dfz,
+                                                   const MrtCoef<T>& c, T dr = T(0)) {
+    const T rux = rhos * ux, ruy = rhos * uy, ruz = rhos * uz;
+    T vx = rux, vy = ruy, wx = rux, wy = ruy;
+    if (ROT) {
+        vx = rux + c.ke2 * fx;
+        vy = ruy + c.ke2 * fy;
+        wx = rux + c.ko * fx;
+        wy = ruy + c.ko * fy;
+    }
+    const T vz = ruz + c.ke2 * fz, wz = ruz + c.ko * fz;
+    const T base = rho_m + T(-1.5) * (ux * vx + uy * vy + uz * vz);
+    const T r3 = T(1.0 / 3.0), r6 = T(1.0 / 6.0), r10 = T(0.1);
+    T ea = base * T(1.0 / 9.0), ee = base * T(1.0 / 18.0), e0 = base * r3;
+    if constexpr (CONS) {
+        const T d19 = dr * T(2.0 / 19.0);
+        ea = ea + d19;
+        ee = ee + d19;
+        e0 = e0 + T(0.5) * d19;
+    }
+    // odd parts: O = e.Ga on axis pairs, e.Ge on edge pairs
+    T gax = wx * r3, gay = wy * r3, gex = wx * r6, gey = wy * r6;
+    if (ROT || CONS) {  // dF_x, dF_y: rotation, or j - rho u of the first step
+        gax = gax + dfx * r10;
+        gay = gay + dfy * r10;
+        gex = gex + dfx * r10;
+        gey = gey + dfy * r10;
+    }
+    const T gaz = wz * r3 + dfz * r10, gez = wz * r6 + dfz * r10;
+    const T le = c.le, lo = c.lo;
+    auto pair = [&](int a, int b, T E, T O) {
+        const T ne = (f[a] + f[b]) - E;
+        const T no = (f[a] - f[b]) - O;
+        const T fa = f[a] - lo * no - le * ne;
+        const T fb = f[b] + lo * no - le * ne;
+        f[a] = fa;
+        f[b] = fb;
+    };
+    f[0] = f[0] - c.snu * (f[0] - e0);
+    pair(1, 2, ea + T(0.5) * ux * vx, gax);
+    pair(3, 4, ea + T(0.5) * uy * vy, gay);
+    pair(5, 6, ea + T(0.5) * uz * vz, gaz);
+    const T q = T(0.25);
+    pair(7, 10, ee + q * (ux + uy) * (vx + vy), gex + gey);
+    pair(9, 8, ee + q * (ux - uy) * (vx - vy), gex - gey);
+    pair(11, 14, ee + q * (ux + uz) * (vx + vz), gex + gez);
+    pair(13, 12, ee + q * (ux - uz) * (vx - vz), gex - gez);
+    pair(15, 18, ee + q * (uy + uz) * (vy + vz), gey + gez);
+    pair(17, 16, ee + q * (uy - uz) * (vy - vz), gey - gez);
 }
 
 // D3Q7 MRT for the temperature populations (evolution_g.F90:1-57), in place.

@@ -5,6 +5,8 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <type_traits>
+
 #include "fixed64.cuh"
 #include "kernels.cuh"
 
@@ -294,7 +296,25 @@ __device__ __forceinline__ void lid_cell_from(int i, int j, int k, const S (&raw
         uz = jz * inv;
     }
     const C rhos = St<S>::SCALED ? rho * sc : rho;
-    mrt_collide<C, false, true>(f, rho_m, rhos, ux, uy, uz, C(0), C(0), C(0), K.c, sc);
+    // The pair form rounds the equilibrium itself (error ~ eps |feq|, where
+    // the moment form rounds only m - meq), and that rounding leaks into the
+    // conserved density and momentum step after step.  In FP64 the leak is
+    // ~1e-15 relative and in the 16-bit forms far below the storage error,
+    // but FP32 storage keeps 1e-7 of the FP64 result only with the moment
+    // form (64^3, Re = 400, 2000 steps: velocity 4e-6 with the pair form).
+    // The first step after initial or load takes rho and u from the macro
+    // arrays, so the pair form adds back what its relaxation would take from
+    // the conserved sums of f (zero when the arrays agree with f).
+    if (std::is_same<S, float>::value) {
+        mrt_collide<C, false, true>(f, rho_m, rhos, ux, uy, uz, C(0), C(0), C(0), K.c, sc);
+    } else if (FIRST) {
+        C rf, jx, jy, jz;
+        moments0(f, rf, jx, jy, jz);
+        trt_collide_lid<C, true>(f, rho_m, rhos, ux, uy, uz, K.c, sc, rf - rho_m,
+                                 jx - rhos * ux, jy - rhos * uy, jz - rhos * uz);
+    } else {
+        trt_collide_lid<C>(f, rho_m, rhos, ux, uy, uz, K.c, sc);
+    }
     // moving lid: f(14) = f_post(11) - rho/6*U0, f(13) = f_post(12) + rho/6*U0
     // (bounce_back.f90:77-78).  On the top layer populations 11 and 12 always
     // leave through the lid (the lid face is written last, so it wins on
@@ -494,14 +514,30 @@ __device__ __forceinline__ void lid_cell_fx(int i, int j, int k, const double* f
 // Temperature populations are kept in the arithmetic type (FP64, or FP32 for
 // the reduced forms): g_0 ~ 0.7 T has a 16-bit ulp (~2e-4) far above the
 // per-step diffusive increments, so 16-bit g would stagnate.
-// thermal_cell_from: collide and push one cell whose populations are already
-// loaded (f converted to the arithmetic type, g); SWAP_STORE: the in-place
+// thermal_cell_from: collide and push one cell whose populations and carried
+// force are already loaded (f converted to the arithmetic type, g, fp =
+// F_x, F_y, F_z of the previous step; load_carried); SWAP_STORE: the in-place
 // even step (own cell, slot opp(q), reflected and anti-bounce-back values
 // formed as the push kernel forms them).  thermal_cell: load, then the same.
+// The carried force is loaded with the populations, not where it is used: a
+// load left inside the cell body has been issued only after the population
+// loads were consumed in some builds (a second memory round trip per cell,
+// halving the 16-bit forms' speed).
+template <typename C, bool ROT, typename IDX>
+__device__ __forceinline__ void load_carried(const C* F, IDX P, IDX cell, IDX fz_off,
+                                             C (&fp)[3]) {
+    fp[0] = fp[1] = C(0);
+    if (ROT) {
+        fp[0] = oob(P + cell, (IDX)3 * P) ? C(0) : F[cell];
+        fp[1] = oob(P + cell, (IDX)3 * P) ? C(0) : F[P + cell];
+    }
+    fp[2] = oob(fz_off + cell, fz_off + P) ? C(0) : F[fz_off + cell];
+}
+
 template <typename S, bool FIRST, bool ROT, typename IDX, bool SR = false, bool SWAP_STORE = false>
 __device__ __forceinline__ void thermal_cell_from(
     int i, int j, int k, typename St<S>::C (&f)[Q19], typename St<S>::C (&g)[Q7],
-    S* __restrict__ fout, typename St<S>::C* __restrict__ gout,
+    const typename St<S>::C (&fp)[3], S* __restrict__ fout, typename St<S>::C* __restrict__ gout,
     typename St<S>::C* __restrict__ F, const StepK<typename St<S>::C>& K, IDX P,
     const double* __restrict__ mrho, const double* __restrict__ mu, const double* __restrict__ mv,
     const double* __restrict__ mw, const double* __restrict__ mT, IDX fz_off, unsigned seed) {
@@ -514,6 +550,7 @@ __device__ __forceinline__ void thermal_cell_from(
     // unscaled
     const C sc = St<S>::SCALED ? (C)K.scale : C(1);
     C rho_m, rho, ux, uy, uz, temp;
+    const C fxp = fp[0], fyp = fp[1], fzp = fp[2];  // carried from the previous step
     if (FIRST) {
         rho = (C)mrho[cell];
         ux = (C)mu[cell];
@@ -532,12 +569,6 @@ __device__ __forceinline__ void thermal_cell_from(
         rho = St<S>::SHIFT ? K.rho0 + (St<S>::SCALED ? rho_m * (C)K.inv_scale : rho_m) : rho_m;
         const C inv = recip(rho);
         // u^n = (sum f e + F^n/2)/rho^n with the force carried from the previous step
-        C fxp = C(0), fyp = C(0);
-        if (ROT) {
-            fxp = oob(P + cell, (IDX)3 * P) ? C(0) : F[cell];
-            fyp = oob(P + cell, (IDX)3 * P) ? C(0) : F[P + cell];
-        }
-        const C fzp = oob(fz_off + cell, fz_off + P) ? C(0) : F[fz_off + cell];
         ux = (jx + C(0.5) * fxp) * inv;
         uy = (jy + C(0.5) * fyp) * inv;
         uz = (jz + C(0.5) * fzp) * inv;
@@ -555,10 +586,27 @@ __device__ __forceinline__ void thermal_cell_from(
     }
     const C fz = rho * K.gbeta * (temp - K.t_ref);
     if (!oob(fz_off + cell, fz_off + P)) F[fz_off + cell] = fz;
-    if (St<S>::SCALED)
-        mrt_collide<C, true, false>(f, rho_m, rho * sc, ux, uy, uz, fx * sc, fy * sc, fz * sc, K.c);
-    else
+    // the pair form where its equilibrium rounding stays below the storage
+    // error (FP64 and the 16-bit forms; see lid_cell_from)
+    if (std::is_same<S, float>::value) {
         mrt_collide<C, true, false>(f, rho_m, rho, ux, uy, uz, fx, fy, fz, K.c);
+    } else if (FIRST) {
+        // rho, u from the macro arrays: the odd term is e.(2 (j - rho u) + F)/10
+        // and the density projection goes back in (trt_collide_forced)
+        C rf, jx, jy, jz;
+        moments0(f, rf, jx, jy, jz);
+        const C rhos = rho * sc;
+        trt_collide_forced<C, ROT, true>(
+            f, rho_m, rhos, ux, uy, uz, fx * sc, fy * sc, fz * sc,
+            fx * sc + C(2) * (jx - rhos * ux), fy * sc + C(2) * (jy - rhos * uy),
+            fz * sc + C(2) * (jz - rhos * uz), K.c, rf - rho_m);
+    } else if (St<S>::SCALED) {
+        trt_collide_forced<C, ROT>(f, rho_m, rho * sc, ux, uy, uz, fx * sc, fy * sc, fz * sc,
+                                   (fx - fxp) * sc, (fy - fyp) * sc, (fz - fzp) * sc, K.c);
+    } else {
+        trt_collide_forced<C, ROT>(f, rho_m, rho, ux, uy, uz, fx, fy, fz, fx - fxp, fy - fyp,
+                                   fz - fzp, K.c);
+    }
     mrt_collide_t<C>(g, temp, ux, uy, uz, K.para_a, K.qd, K.qnu);
 
     const IDX sy = (IDX)nx, sz = (IDX)nx * (IDX)ny;
@@ -632,24 +680,34 @@ __device__ __forceinline__ void thermal_cell(
     const double* __restrict__ mw, const double* __restrict__ mT, IDX fz_off, unsigned seed) {
     using C = typename St<S>::C;
     const IDX cell = (IDX)i + (IDX)K.nx * ((IDX)j + (IDX)K.ny * (IDX)k);
-    C f[Q19], g[Q7];
+    // every load is issued before the first conversion (as in lid_cell):
+    // left to itself the scheduler has interleaved them with the arithmetic
+    // in some builds of the 16-bit forms, halving their speed
+    S raw[Q19];
+    C f[Q19], g[Q7], fp[3];
 #pragma unroll
     for (int q = 0; q < Q19; q++)
-        f[q] = St<S>::cvt_s(oob((IDX)q * P + cell, (IDX)Q19 * P) ? S() : St<S>::raw(fin + ((IDX)q * P + cell)));
+        raw[q] = oob((IDX)q * P + cell, (IDX)Q19 * P) ? S() : St<S>::raw(fin + ((IDX)q * P + cell));
 #pragma unroll
-    for (int q = 0; q < Q7; q++) g[q] = oob((IDX)q * P + cell, (IDX)Q7 * P) ? C(0) : gin[(IDX)q * P + cell];
-    thermal_cell_from<S, FIRST, ROT, IDX, SR>(i, j, k, f, g, fout, gout, F, K, P, mrho, mu, mv,
-                                              mw, mT, fz_off, seed);
+    for (int q = 0; q < Q7; q++)
+        g[q] = oob((IDX)q * P + cell, (IDX)Q7 * P) ? C(0) : St<C>::raw(gin + ((IDX)q * P + cell));
+    load_carried<C, ROT, IDX>(F, P, cell, fz_off, fp);
+#pragma unroll
+    for (int q = 0; q < Q19; q++) f[q] = St<S>::cvt_s(raw[q]);
+    thermal_cell_from<S, FIRST, ROT, IDX, SR>(i, j, k, f, g, fp, fout, gout, F, K, P, mrho, mu,
+                                              mv, mw, mT, fz_off, seed);
 }
 
 // in-place pattern loads of a heated-cavity cell (plain loads; ODD: from the
 // upstream cells' opposite slots, or the own slot where upstream is outside)
-template <typename S, typename IDX, bool ODD>
+template <typename S, typename IDX, bool ODD, bool ROT = false>
 __device__ __forceinline__ void thermal_load_aa(int i, int j, int k, const S* f,
                                                 const typename St<S>::C* g,
+                                                const typename St<S>::C* F, IDX fz_off,
                                                 const StepK<typename St<S>::C>& K, IDX P,
                                                 typename St<S>::C (&fv)[Q19],
-                                                typename St<S>::C (&gv)[Q7]) {
+                                                typename St<S>::C (&gv)[Q7],
+                                                typename St<S>::C (&fp)[3]) {
     const int nx = K.nx, ny = K.ny, nz = K.nz;
     const IDX cell = (IDX)i + (IDX)nx * ((IDX)j + (IDX)ny * (IDX)k);
     const IDX sy = (IDX)nx, sz = (IDX)nx * (IDX)ny;
@@ -668,6 +726,7 @@ __device__ __forceinline__ void thermal_load_aa(int i, int j, int k, const S* f,
 #pragma unroll
     for (int q = 0; q < Q7; q++)
         gv[q] = oob(src(q), (IDX)Q7 * P) ? typename St<S>::C(0) : __ldcg(g + src(q));
+    load_carried<typename St<S>::C, ROT, IDX>(F, P, cell, fz_off, fp);
 #pragma unroll
     for (int q = 0; q < Q19; q++) fv[q] = St<S>::cvt_s(raw[q]);  // in units of the storage scale
 }
