@@ -509,18 +509,21 @@ __global__ void __launch_bounds__(PB) k_plinks(S* __restrict__ f, PartParams p, 
             const double sy = eb > 0 ? oy : (eb < 0 ? -oy : 0.0);
             const double sz = ec > 0 ? oz : (ec < 0 ? -oz : 0.0);
             const double cc = ox * ox + oy * oy + oz * oz - R * R;
-            double qd;
+            double qd = -1.0;
+            bool exact = true;
             if constexpr (sizeof(L) == 4) {
                 // FP32 form: |x - X|^2 - R^2 (the cancelling part) in FP64, the
-                // root in FP32; FP32 rounding may put a root on the node (q = 0)
-                // or the solid node (q = 1) a few ulps outside, which is clamped
+                // root in FP32.  Its error grows where the ray is nearly tangent
+                // (small delta) and matters where q is near 0 or 1, the ends
+                // the range check tests: those links take the FP64 root, so the
+                // FP32 and FP64 forms accept and reject the same links.
                 const float cbf = 2.0f * (float)(sx + sy + sz);
                 const float delta = cbf * cbf - (a <= 6 ? 4.0f : 8.0f) * (float)cc;
-                if (delta < -1e-4f) { atomicCAS(d.status, 0, PS_Q_RANGE); d.status[1] = c; continue; }
                 const float qf = (-cbf - sqrtf(fmaxf(delta, 0.0f))) * (a <= 6 ? 0.5f : 0.25f);
-                if (qf > 1.0f + 1e-5f || qf < -1e-5f) { atomicCAS(d.status, 0, PS_Q_RANGE); d.status[1] = c; continue; }
-                qd = (double)fminf(fmaxf(qf, 0.0f), 1.0f);
-            } else {
+                exact = !(delta > 1e-2f * cbf * cbf + 1e-3f && qf > 1e-3f && qf < 1.0f - 1e-3f);
+                if (!exact) qd = (double)qf;
+            }
+            if (exact) {
                 const double cb = 2.0 * (sx + sy + sz);
                 const double delta = cb * cb - (a <= 6 ? 4.0 : 8.0) * cc;
                 if (delta < 0) { atomicCAS(d.status, 0, PS_Q_RANGE); d.status[1] = c; continue; }
