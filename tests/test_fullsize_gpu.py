@@ -1,8 +1,9 @@
-"""Size-independent properties at the benchmark sizes, where the CPU oracle
-would take hours: the closed cavity conserves mass, the lid flow is
+"""Size-independent properties at the benchmark sizes (the oracle comparisons
+at those sizes are in test_config_parity_gpu.py): the closed cavity conserves mass, the lid flow is
 mirror-symmetric about y = ny/2, the 64-bit index path (19 * cells >= 2^31)
 agrees with those properties, the heated cavity is centro-symmetric, and the
-FP32 particle channel tracks the FP64 one at full size."""
+FP32 particle channel tracks the FP64 one at full size and runs its full
+step count."""
 import numpy as np
 import pytest
 
@@ -83,3 +84,20 @@ def test_particle_channel_full_size_fp32_tracks_fp64(mg):
     assert rel_l2(U32, U64) <= 1e-4
     assert rel_l2(st32["uc"], st64["uc"]) <= 1e-3
     assert np.abs(st32["xc"] - st64["xc"]).max() <= 1e-6
+
+
+def test_particle_channel_fp32_runs_its_10000_steps(mg):
+    """The channel's own step count in FP32 with no particle status: where a
+    link's FP32 ray-sphere root is near a range end (q near 0 or 1) or the ray
+    is nearly tangent, the link takes the FP64 root, so FP32 rounding cannot
+    put q outside [0, 1] and stop the run (it did, once, before that rule)."""
+    import bench
+    wl = bench.WORKLOADS["particles"]
+    with bench.make_solve(mg, wl, "fp32") as s:
+        s.initial()
+        for _ in range(wl["error_steps"] // 1000):
+            s.step(1000)  # raises on a particle status
+        u = s.macro()[1]
+        xc = s.state()["xc"]
+    assert np.isfinite(u).all() and np.isfinite(xc).all()
+    assert 1e-3 < np.abs(u).max() < 0.1  # the body force drives a channel flow
