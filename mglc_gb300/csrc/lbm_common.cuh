@@ -5,13 +5,18 @@
 // (MPI/Lid_driven_cavity/fortran/3d/mpi_3d_blocked/commondata.f90:29-40):
 //   0; +-x (1,2); +-y (3,4); +-z (5,6); (+1,+1,0) (-1,+1,0) (+1,-1,0) (-1,-1,0) (7..10);
 //   (+1,0,+1) (-1,0,+1) (+1,0,-1) (-1,0,-1) (11..14); (0,+1,+1) (0,-1,+1) (0,+1,-1) (0,-1,-1) (15..18).
-// The moment basis is the reference's M (collision.f90:20-70).  The collision
-// is evaluated in the algebraically equal form
-//     f_post = f - M^-1 r,   r_k = s_k (m_k - meq_k) - (1 - s_k/2) S_k,
-// with M^-1 = M^T diag(1/|M_k|^2) and opposite-direction pairs sharing their
-// even/odd parts, which needs about half the FP64 operations of the literal
-// m -> m_post -> M^-1 m_post evaluation.  Results differ from the literal form
-// only by rounding (about 1 ulp per step).
+// The moment basis is the reference's M (collision.f90:20-70).  Two
+// algebraically equal evaluations of the collision are kept:
+//  - the moment form (mrt_collide, mrt_collide_t)
+//        f_post = f - M^-1 r,   r_k = s_k (m_k - meq_k) - (1 - s_k/2) S_k,
+//    with M^-1 = M^T diag(1/|M_k|^2) and opposite-direction pairs sharing
+//    their even/odd parts, about half the operations of the literal
+//    m -> m_post -> M^-1 m_post;
+//  - the pair form (trt_collide_lid, trt_collide_forced, trt_collide_t): the
+//    reference relaxes all even non-conserved moments at one rate and all odd
+//    ones at another, so the collision is a two-relaxation-time update of
+//    each opposite pair, about 3/4 of the moment form's operations.
+// Results differ from the literal form only by rounding (a few ulp per step).
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -407,6 +412,39 @@ __device__ __forceinline__ void mrt_collide_t(T* g, T temp, T ux, T uy, T uz, T 
     g[1] -= ex5 + t1; g[2] -= ex5 - t1;
     g[3] -= (ey5 + t6) + t2; g[4] -= (ey5 + t6) - t2;
     g[5] -= (ey5 - t6) + t3; g[6] -= (ey5 - t6) - t3;
+}
+
+// The same D3Q7 collision in pair form.  Its even non-conserved moments
+// (n4..n6) relax at qnu and its odd ones (the fluxes n1..n3) at qd
+// (evolution_g.F90:1-57), so g' = g - qnu (g - geq)^+ - qd (g - geq)^- with
+// geq = N^-1 neq: geq_0 = T (1 - a)/7 and, per axis pair,
+// E = geq_a + geq_b = T (6 + a)/21, O = geq_a - geq_b = T u_a.  The
+// temperature's projection (sum g - T)/7 is at rounding level when T is the
+// sum of g; CONS adds it back (dT = sum g - T) for the first step after
+// initial or load, where T comes from the macro array.  About half the
+// operations of the moment form.
+template <typename T, bool CONS = false>
+__device__ __forceinline__ void trt_collide_t(T* g, T temp, T ux, T uy, T uz, T para_a, T qd,
+                                              T qnu, T dT = T(0)) {
+    T e0 = temp * ((T(1) - para_a) * T(1.0 / 7.0));
+    T E = temp * ((T(6) + para_a) * T(1.0 / 21.0));
+    if constexpr (CONS) {
+        e0 = e0 + dT * T(1.0 / 7.0);
+        E = E + dT * T(2.0 / 7.0);
+    }
+    const T hn = T(0.5) * qnu, hd = T(0.5) * qd;
+    g[0] = g[0] - qnu * (g[0] - e0);
+    auto pair = [&](int a, int b, T O) {
+        const T ne = (g[a] + g[b]) - E;
+        const T no = (g[a] - g[b]) - O;
+        const T ga = g[a] - hd * no - hn * ne;
+        const T gb = g[b] + hd * no - hn * ne;
+        g[a] = ga;
+        g[b] = gb;
+    };
+    pair(1, 2, temp * ux);
+    pair(3, 4, temp * uy);
+    pair(5, 6, temp * uz);
 }
 
 }  // namespace mglc

@@ -607,7 +607,17 @@ __device__ __forceinline__ void thermal_cell_from(
         trt_collide_forced<C, ROT>(f, rho_m, rho, ux, uy, uz, fx, fy, fz, fx - fxp, fy - fyp,
                                    fz - fzp, K.c);
     }
-    mrt_collide_t<C>(g, temp, ux, uy, uz, K.para_a, K.qd, K.qnu);
+    // D3Q7: the pair form in FP64; the FP32 temperature populations of the
+    // reduced forms keep the moment form (its rounding does not leak into
+    // the conserved sum of g; see lid_cell_from for the FP32 measurement)
+    if (!std::is_same<C, double>::value) {
+        mrt_collide_t<C>(g, temp, ux, uy, uz, K.para_a, K.qd, K.qnu);
+    } else if (FIRST) {
+        const C sg = ((g[0] + g[1]) + (g[2] + g[3])) + ((g[4] + g[5]) + g[6]);
+        trt_collide_t<C, true>(g, temp, ux, uy, uz, K.para_a, K.qd, K.qnu, sg - temp);
+    } else {
+        trt_collide_t<C>(g, temp, ux, uy, uz, K.para_a, K.qd, K.qnu);
+    }
 
     const IDX sy = (IDX)nx, sz = (IDX)nx * (IDX)ny;
     const unsigned bm = face_mask(i, j, k, nx, ny, nz);
