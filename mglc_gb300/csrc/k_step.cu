@@ -19,7 +19,7 @@
 namespace mglc {
 
 template <typename S, bool FIRST, typename IDX, bool SR>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, LidMinBlocks<S>::value)
     k_lid_step(const S* __restrict__ fin, S* __restrict__ fout, StepK<typename St<S>::C> K,
                IDX P, const double* __restrict__ mrho, const double* __restrict__ mu,
                const double* __restrict__ mv, const double* __restrict__ mw) {

@@ -13,7 +13,7 @@
 namespace mglc {
 
 template <typename S, bool FIRST, typename IDX, bool SR, bool ODD>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, LidMinBlocks<S>::value)
     k_lid_step_aa(S* f, StepK<typename St<S>::C> K, IDX P, const double* __restrict__ mrho,
                   const double* __restrict__ mu, const double* __restrict__ mv,
                   const double* __restrict__ mw) {

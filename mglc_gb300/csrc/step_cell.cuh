@@ -166,6 +166,17 @@ __device__ __forceinline__ double recip(double x) {
     return fma(r, e, r);
 }
 
+// Minimum resident blocks of 128 threads per SM for the lid step kernels: the
+// FP64 kernels are bound by the FP64 pipe, and 8 blocks (64 registers, a few
+// spilled values) measured 5% faster at 384^3 than the compiler's own 80
+// registers and 6 blocks (7 blocks: 4%); the other forms keep the compiler's
+// choice (0: no bound; a bound of 12 or 16 blocks slowed the 16-bit kernels by
+// 7-30%).
+template <typename S>
+struct LidMinBlocks {
+    static constexpr int value = std::is_same<S, double>::value ? 8 : 0;
+};
+
 // Scalar constants converted once on the host to the arithmetic type.
 template <typename C>
 struct StepK {

@@ -1,7 +1,9 @@
 """Moving spheres (D3Q19): the CUDA particle path against the 3-D oracle.
 
-The oracle's 3-D mode generalises the reference's case4 algorithm (its 2-D
-mode is pinned to the reference's own statements).  Both use the analytic
+The reference's particle code is 2-D only, so no reference-executed fixture
+exists for spheres: the oracle's 3-D mode generalises the reference's case4
+algorithm, and it is pinned through its 2-D parent (the 2-D mode reproduces
+the reference's own statements bit for bit).  Both use the analytic
 ray-sphere q (calQ2).  FP64: relative L2 <= 1e-10 on the fluid populations and
 1e-9 on the particle state after 60 steps; FP32 storage/arithmetic: 1e-4."""
 import numpy as np
