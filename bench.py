@@ -557,7 +557,8 @@ def side_workload(torch, mg, key, steps, warmup, peak, probe, cpu=True, errors=T
               "bytes_per_cell": head["bytes_per_cell"],
               "kernel": "particle step (k_pbulk + 10 small kernels)" if kind == "particle"
               else f"k_thermal_step<{forms[0]}>"}
-        for k in ("fp64_achieved", "fp64_peak", "fp64_unit", "fp64_frac", "alt_layout_bytes_per_cell"):
+        for k in ("fp64_achieved", "fp64_peak", "fp64_unit", "fp64_frac", "fp64_mix_roof_mlups",
+                  "fp64_mix_frac", "fp64_instr_per_cell", "alt_layout_bytes_per_cell"):
             if k in head:
                 rf[k] = head[k]
         out["roofline"] = rf
