@@ -9,8 +9,9 @@ The FP32 form evaluates the root in FP32 and keeps it only where
 every other link (a nearly tangent ray, or q near the range ends that the
 range check tests) takes the FP64 root.  Here the kernel's FP32 arithmetic is
 emulated with numpy float32 on about 700,000 boundary links of a sphere of
-radius 5 at 400 random centres: every FP32 root kept lies inside [0, 1] and within 2e-5 of the FP64
-root, so the FP32 and FP64 forms accept and reject the same links."""
+radius 5 at 400 random centres: every FP32 root kept lies inside [0, 1] and
+within 2e-5 of the FP64 root, so the FP32 and FP64 forms accept and reject
+the same links."""
 import numpy as np
 
 E = np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1],
@@ -41,7 +42,7 @@ def test_fp32_roots_kept_agree_with_fp64():
     R = 5.0
     kept = taken = 0
     worst = 0.0
-    for _ in range(400):  # ~2500 links per random centre
+    for _ in range(400):  # ~1800 links per random centre
         o, e = boundary_links(rng, R)
         s = (o * e).sum(1)  # e.(x - X)
         cc = (o ** 2).sum(1) - R * R
